@@ -1,0 +1,428 @@
+"""Benchmark of the SPH step: particle-steps/s on one GB300.
+
+Workload (default): the 1,048,576-particle dam break with a held sphere
+(128x64x128 lattice, spacing 0.02, seeded jitter, box 4x2x3, h 0.08,
+rest density 8000, 4 PCISPH iterations, dt 0.008). A step is one substep of
+the reference's SphSimulation3DGrid::step() over all particles. The timed
+region replays K steps (from step W+1 of the rollout) as CUDA graphs; the
+state (>= 250 MB) is larger than L2, so no flush is needed between steps.
+
+Arms
+  default           this library (libfluidsph.so) through its C ABI
+  --impl reference  the reference step's CPU restatement (the oracle, the
+                    only runnable form of the reference here: its WGSL needs
+                    wgpu + a Vulkan adapter, which this machine lacks), all
+                    host cores, on a bounded sample of the same workload
+Multi-GPU: replicas only (each rank runs its own scene; no collective on the
+data path); value = all ranks' particle-steps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT / "fluid-toy_gb300", ROOT):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s"
+# algorithmic bytes per particle-step and per stage (SoA, compulsory traffic)
+STAGE_BYTES = {"hash": 16, "reorder": 60, "density": 32, "xsph": 40, "force_predict": 68 + 68,
+               "pcisph_solve": 100, "finalize_integrate": 48 + 48}
+CELL_BYTES = {"clear": 4, "hash": 8, "scan": 8}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---- distributed plumbing (replicas) -----------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        return self._reduce(x, "max")
+
+    def sum(self, x: float) -> float:
+        return self._reduce(x, "sum")
+
+    def _reduce(self, x: float, op: str) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() and self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def aggregate(units_local: float, seconds_local: float, dist: Dist) -> tuple[float, float]:
+    """Whole-job throughput: all ranks' units over the slowest rank's time."""
+    units = dist.sum(units_local)
+    secs = dist.max(seconds_local)
+    return units / secs if secs > 0 else 0.0, secs
+
+
+# ---- clocks during the timed region --------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---- arms ------------------------------------------------------------------------
+def make_scene(config: int):
+    from fluidsph import scenes
+    return scenes.CONFIGS[config]()
+
+
+def fp32_peak_tflops(device: int) -> tuple[float, str]:
+    import torch
+    p = torch.cuda.get_device_properties(device)
+    sms = p.multi_processor_count
+    mhz = 2070.0
+    try:
+        out = subprocess.run(["nvidia-smi", f"--id={device}", "--query-gpu=clocks.max.sm",
+                              "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                             timeout=10).stdout.strip()
+        mhz = float(out.splitlines()[0])
+    except Exception:
+        pass
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    return peak, f"nominal: {sms} SMs x 128 FP32 lanes x 2 FLOP x {mhz:.0f} MHz"
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+def profile_traffic(kernel: str) -> float | None:
+    """dram bytes per launch of `kernel` from the committed ncu summary."""
+    for f in (ROOT / "profiles").glob("*.md"):
+        for line in f.read_text().splitlines():
+            if line.startswith(f"traffic_bytes_per_launch[{kernel}]"):
+                try:
+                    return float(line.split("=", 1)[1].split()[0])
+                except (IndexError, ValueError):
+                    return None
+    return None
+
+
+def cpu_sample(scene, parts_np, steps: int, threads: int = 0) -> dict:
+    """The oracle on the host cores, from the given state, for `steps` steps."""
+    from oracle import oracle
+    nthreads = oracle.set_threads(threads)
+    o = oracle.OracleSim(parts_np, scene.sph, scene.geom)
+    o.update_gravity(scene.gravity)
+    o.set_pcisph_iterations(scene.iterations)
+    if scene.rigid is not None:
+        o.update_rigid_body(scene.rigid)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    return {"value": scene.n * steps / dt, "unit": METRIC, "cores": nthreads, "kind": "port",
+            "seconds": dt, "steps": steps}
+
+
+def run_ours(args, dist: Dist) -> dict | None:
+    import torch
+    from fluidsph.sim import SphSimulation3DGrid
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    scene = make_scene(args.config)
+    n = scene.n
+    K, W = args.steps, args.warmup
+
+    def fresh():
+        sim = SphSimulation3DGrid(scene.particles, scene.sph, scene.geom, device=dev)
+        sim.update_gravity(scene.gravity)
+        sim.set_pcisph_iterations(scene.iterations)
+        if scene.rigid is not None:
+            sim.update_rigid_body(scene.rigid)
+        sim.clear_rigid_body_accum()
+        return sim
+
+    # --- headline: K graph-replayed steps after W warm-up steps -------------------
+    sim = fresh()
+    stream = torch.cuda.Stream(device=dev)  # events and steps on one stream
+    sim.set_stream(stream.cuda_stream)
+    sim.step(W)
+    sim.sync()
+    state_after_warmup = sim.particles() if dist.rank == 0 and not args.no_cpu else None
+    sim.neighbor_stats(reset=True)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.step(K)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    clk = clocks.stop()
+    secs = e0.elapsed_time(e1) / 1e3
+    stats = sim.neighbor_stats(reset=True)
+    value, secs_max = aggregate(n * K, secs, dist)
+    sim.close()
+
+    # --- per-stage timing of the same K steps (roofline inputs) --------------------
+    sim = fresh()
+    sim.step(W)
+    sim.enable_stage_timing(True)
+    sim.stage_times(reset=True)
+    sim.step(K)
+    stages, timed = sim.stage_times(reset=True)
+    sim.close()
+    per_step_ms = {k: v / max(timed, 1) for k, v in stages.items()}
+
+    # --- e2e through the public API with host buffers ------------------------------
+    # the reference app's per-substep pattern (app.rs:962-1019, 1205-1220): upload
+    # the parameter structs from host memory, step, read the rigid-body
+    # accumulator back (synchronising)
+    sim = fresh()
+    sim.step(W)
+    sim.sync()
+    h2d = 64 + 128 + 16 + 48 + 96
+    d2h = 32
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        sim.update_sph_params(scene.sph)
+        sim.update_container_geometry(scene.geom)
+        sim.update_gravity(scene.gravity)
+        if scene.rigid is not None:
+            sim.update_rigid_body(scene.rigid)
+        sim.step(1)
+        sim.read_rigid_body_accum()
+    e2e_secs = time.perf_counter() - t0
+    dist.barrier()
+    e2e_value, _ = aggregate(n * K, e2e_secs, dist)
+    sim.close()
+
+    if dist.rank != 0:
+        return None
+
+    # --- roofline of the dominant kernel -----------------------------------------------
+    nb = {k: v for k, v in per_step_ms.items() if k != "step"}
+    dom = max(nb, key=nb.get)
+    cand = stats["cand_density"] / K
+    hits = stats["hits_density"] / K
+    nonself = stats["hits_nonself"] / K
+    cand_s = stats["cand_solve"] / K
+    hits_s = stats["hits_solve"] / K
+    flops = {
+        "density": 6 * cand + 16 * hits,
+        "xsph": 6 * cand + 16 * nonself,
+        "force_predict": 6 * cand + 64 * nonself,
+        "pcisph_solve": 6 * cand_s + 32 * hits_s,
+    }
+    fp32_peak, fp32_src = fp32_peak_tflops(dev)
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
+    G = 52 ** 3
+
+    def hbm_achieved(stage):
+        b = STAGE_BYTES.get(stage, 0) * n + CELL_BYTES.get(stage, 0) * G
+        return b / (per_step_ms[stage] * 1e-3) / 1e9 if per_step_ms[stage] > 0 else 0.0
+
+    stage_report = {}
+    for st, ms in nb.items():
+        r = {"ms": round(ms, 4)}
+        if st in flops:
+            tf = flops[st] / (ms * 1e-3) / 1e12
+            r.update({"tflops": round(tf, 3), "fp32_frac": round(tf / fp32_peak, 4)})
+        r.update({"hbm_gbs": round(hbm_achieved(st), 1),
+                  "hbm_frac": round(hbm_achieved(st) / hbm_peak, 4)})
+        stage_report[st] = r
+    kernel_name = {"pcisph_solve": "k_solve", "force_predict": "k_force_predict",
+                   "density": "k_density", "xsph": "k_xsph"}.get(dom, dom)
+    if dom in flops:
+        iters = scene.iterations if dom == "pcisph_solve" else 1
+        achieved = flops[dom] / (per_step_ms[dom] * 1e-3) / 1e12
+        traffic = profile_traffic(kernel_name)
+        roofline = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(fp32_peak, 1),
+                    "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4),
+                    "traffic": traffic, "kernel": kernel_name, "launches_per_step": iters,
+                    "flop_per_step": flops[dom], "peak_source": fp32_src,
+                    "flop_model": "6 per candidate pair test + per in-range pair 16 density, "
+                                  "16 xsph, 64 force, 32 solve; counts measured each step"}
+    else:
+        achieved = hbm_achieved(dom)
+        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                    "traffic": profile_traffic(kernel_name), "kernel": kernel_name,
+                    "peak_source": hbm_src}
+
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": METRIC, "n_gpus": dist.world,
+        "steps": K, "warmup": W, "ms_per_step": round(secs_max / K * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 lattice jitter)",
+        "config": {"workload": scene.name, "particles": n, "steps_timed": f"{W + 1}..{W + K}",
+                   "kernel_radius": 0.08, "pcisph_iterations": scene.iterations,
+                   "parallelism": f"replicas{dist.world}" if dist.world > 1 else "single",
+                   "l2": "state > 250 MB exceeds the 129 MB L2 (no flush)"},
+        "roofline": roofline,
+        "roofline_stages": stage_report,
+        "neighbors_per_step": {"candidates": cand, "hits": hits, "solve_candidates": cand_s},
+        "e2e": {"value": round(e2e_value, 1), "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+                "pattern": "per step: upload sph/geometry/gravity/rigid-body structs, "
+                           "fs_step(1), read rigid-body accumulator (sync)"},
+        "gpu_launches": K * (8 + scene.iterations),
+        "clocks": clk,
+    }
+    if state_after_warmup is not None:
+        cs = cpu_sample(scene, state_after_warmup, args.cpu_steps)
+        cs["sample"] = (f"{scene.name}: oracle (FP32 C++ restatement, OpenMP) from the GPU "
+                        f"state after step {W}, {args.cpu_steps} steps")
+        out["cpu_baseline"] = cs
+    return out
+
+
+def run_reference(args, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    scene = make_scene(args.config)
+    W, K = args.warmup, args.steps
+    # the reference arm runs the bounded sample W warm-up + K timed steps, with
+    # K capped so the run stays within minutes on the host cores
+    from oracle import oracle
+    nthreads = oracle.set_threads(0)
+    o = oracle.oracle_for_scene(scene)
+    k_cpu = min(K, args.cpu_steps)
+    o.step(min(W, 1))
+    t0 = time.perf_counter()
+    o.step(k_cpu)
+    secs = time.perf_counter() - t0
+    value = scene.n * k_cpu / secs
+    sample = (f"{scene.name}: oracle (FP32 C++ restatement of the step WGSL, OpenMP), "
+              f"steps {min(W, 1) + 1}..{min(W, 1) + k_cpu}")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": METRIC,
+            "n_gpus": dist.world, "steps": k_cpu, "warmup": min(W, 1),
+            "ms_per_step": round(secs / k_cpu * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": scene.name, "particles": scene.n},
+            "cpu_baseline": {"value": round(value, 1), "unit": METRIC, "cores": nthreads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 1), "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warm-up raised to 3 steps")
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            out = run_reference(args, dist)
+        else:
+            from fluidsph.build import build_library
+            if dist.local_rank == 0:
+                build_library()
+            dist.barrier()
+            out = run_ours(args, dist)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

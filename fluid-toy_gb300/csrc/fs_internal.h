@@ -1,0 +1,101 @@
+// fs_internal.h — internal types shared by the host orchestration (sim.cu)
+// and the sm_103a kernels (grid_kernels.cu, sph_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fluidsph.h"
+
+namespace fs {
+
+// Parameter block resident in device memory. The update_* entry points copy
+// their struct here with cudaMemcpyAsync on the simulation's stream, which
+// orders them before later steps exactly like the reference's
+// queue.write_buffer uploads (sph_3d_grid.rs:1446-1473), and lets captured
+// step graphs stay valid across parameter changes.
+struct DevUniforms {
+  GpuSphParams3D sph;
+  GpuGridParams grid;
+  GpuContainerGeometry geom;
+  GpuGravity gravity;
+  GpuMouseForce mouse;
+  GpuRigidBody rigid;
+  uint32_t n;        // effective particle count for every stage
+  uint32_t sdf_res;  // SDF texture edge length (1 = the reference's dummy)
+  uint32_t pad[2];
+};
+
+// Neighbour-statistics counters written by the density and solve kernels.
+enum StatIndex : int {
+  STAT_CAND_DENSITY = 0,  // candidate pair tests in the density pass
+  STAT_HIT_DENSITY = 1,   // pairs with r^2 < h^2 (self included)
+  STAT_HIT_NONSELF = 2,   // pairs with 1e-12 < r^2 < h^2
+  STAT_CAND_SOLVE = 3,    // candidate tests summed over solve iterations
+  STAT_HIT_SOLVE = 4,     // predicted-position pairs with r^2 < h^2
+  STAT_COUNT = 8
+};
+
+// Device error word bits.
+enum ErrorBits : uint32_t {
+  ERR_SCAN_TIMEOUT = 1u,  // decoupled-lookback poll limit reached
+};
+
+// Particle state in HBM: structure-of-arrays, one 16-byte record per particle
+// per field so every particle read is one coalesced 128-bit load.
+struct DevState {
+  // canonical order (index = particle identity, the reference's particle_buffer)
+  float4 *p_pos;    // x, y, z, _pad0
+  float4 *p_vel;    // vx, vy, vz, _pad1
+  float4 *p_force;  // fx, fy, fz, 0  (a_np during the step, dv after it)
+  float4 *p_aux;    // 2 per particle: (density, near, nx, ny), (nz, 0, 0, 0)
+  // grid-sorted order (index = sorted slot, the reference's sorted buffer)
+  float4 *s_pos;    // x, y, z, _pad0
+  float4 *s_vel;    // pre-XSPH velocity, _pad1
+  float4 *s_frc;    // force field copied at reorder (sorted-view fidelity)
+  float2 *s_dens;   // density (boundary-corrected), near density
+  float4 *s_nrm;    // Akinci normal, 0
+  float4 *vel_x;    // post-XSPH velocity (the canonical velocity mid-step)
+  float4 *anp;      // non-pressure acceleration a_np
+  float4 *pred_xp[2];  // predicted position, pressure (ping-pong)
+  float *pred_rho[2];  // predicted density (ping-pong)
+  float4 *pred_v;      // final predicted (corrected) velocity
+  // grid
+  uint32_t *cell_of;     // particle -> cell (hash output)
+  uint32_t *rank_of;     // particle -> arrival rank within its cell
+  uint32_t *t_tmp;       // unsorted slot -> particle
+  uint32_t *s2o;         // sorted slot -> particle (sorted_to_orig)
+  uint32_t *cidx;        // particle -> sorted slot (particle_cell_indices)
+  uint32_t *counts;      // cell_counts[total_cells]
+  uint32_t *cell_begin;  // [total_cells + 1]; cell_begin + 1 = cell_starts
+  unsigned long long *tile_status;  // decoupled-lookback descriptors
+  uint32_t *tile_ticket;
+  float *sdf;
+  GpuRigidBodyAccum *accum;
+  uint32_t *err;
+  unsigned long long *stats;
+  DevUniforms *u;
+};
+
+// ---- kernel launchers (grid_kernels.cu / sph_kernels.cu) --------------------
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+inline uint32_t scan_tiles(uint32_t total_cells) {
+  return (total_cells + SCAN_TILE - 1) / SCAN_TILE;
+}
+
+cudaError_t launch_hash(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st);
+cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last,
+                         cudaStream_t st);
+cudaError_t launch_finalize_integrate(const DevState &d, uint32_t n, int final_buf,
+                                      cudaStream_t st);
+
+}  // namespace fs

@@ -1,0 +1,280 @@
+// grid_kernels.cu — uniform-grid build for the SPH step on sm_103a:
+// hash + count, single-pass decoupled-lookback scan, and a stable counting
+// sort that gathers the particle records into grid order.
+//
+// Reference stages (WGSL, src/shaders/): grid_clear.wgsl:23-29,
+// grid_build.wgsl:33-62, prefix_scan.wgsl:38-122 (+ the counts->starts copy at
+// sph_3d_grid.rs:1295-1301), grid_reorder.wgsl:37-63.
+//
+// Output conventions match the reference buffers bit for bit:
+//   cell_counts[c]            particles hashed into cell c
+//   cell_starts[c]            INCLUSIVE prefix end of cell c; this library
+//                             stores cell_begin[0..total] with cell_begin[0]=0
+//                             so that cell_starts == cell_begin + 1
+//   particle_cell_indices[i]  sorted slot of particle i (after reorder)
+//   sorted_to_orig[s]         particle in sorted slot s
+// Slot order inside a cell is ascending particle index (stable). The
+// reference's atomicAdd slot makes that order unspecified; a stable order makes
+// every later summation deterministic.
+#include <cuda/atomic>
+
+#include "fs_internal.h"
+
+namespace fs {
+namespace {
+
+// position_to_cell + clamped cell_to_index, grid_build.wgsl:33-44.
+// floor((p - origin) * inv) converted with saturation (cvt.rmi), then clamped.
+__device__ __forceinline__ uint32_t hash_cell(float4 p, const GpuGridParams &g) {
+  int cx = __float2int_rd((p.x - g.grid_origin_x) * g.inv_cell_size);
+  int cy = __float2int_rd((p.y - g.grid_origin_y) * g.inv_cell_size);
+  int cz = __float2int_rd((p.z - g.grid_origin_z) * g.inv_cell_size);
+  cx = min(max(cx, 0), int(g.grid_size_x) - 1);
+  cy = min(max(cy, 0), int(g.grid_size_y) - 1);
+  cz = min(max(cz, 0), int(g.grid_size_z) - 1);
+  return uint32_t(cx) + uint32_t(cy) * g.grid_size_x +
+         uint32_t(cz) * g.grid_size_x * g.grid_size_y;
+}
+
+// Hash + count with warp-aggregated atomics: lanes holding the same cell
+// (found with __match_any_sync) elect one leader that adds the group's size;
+// every lane keeps its arrival rank (leader's old count + rank among peers).
+__global__ void __launch_bounds__(256) k_hash(const float4 *__restrict__ pos,
+                                              const DevUniforms *__restrict__ U,
+                                              uint32_t *__restrict__ cell_of,
+                                              uint32_t *__restrict__ rank_of,
+                                              uint32_t *__restrict__ counts) {
+  const uint32_t n = U->n;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < n;
+  uint32_t cell = 0;
+  if (active) cell = hash_cell(pos[i], U->grid);
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned peers = __match_any_sync(act, cell);
+  const int leader = __ffs(peers) - 1;
+  const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+  uint32_t base = 0;
+  if (int(lane) == leader) base = atomicAdd(&counts[cell], uint32_t(__popc(peers)));
+  base = __shfl_sync(peers, base, leader);
+  cell_of[i] = cell;
+  rank_of[i] = base + rank;
+}
+
+// ---- single-pass scan (decoupled look-back) --------------------------------
+// Tile descriptor: bits 32-33 flag (0 none, 1 tile aggregate, 2 inclusive
+// prefix), bits 0-31 value. Tiles are processed in ticket order, so a tile
+// only waits for predecessors that are already running and publish their
+// aggregate before they wait on anyone: no deadlock. Each poll loop is still
+// bounded; on expiry the kernel records ERR_SCAN_TIMEOUT and continues.
+constexpr unsigned long long FLAG_AGG = 1ull << 32;
+constexpr unsigned long long FLAG_PRE = 2ull << 32;
+constexpr int LOOKBACK_POLL_LIMIT = 1 << 22;
+
+__device__ __forceinline__ void publish(unsigned long long *slot, unsigned long long v) {
+  cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*slot);
+  r.store(v, cuda::memory_order_release);
+}
+__device__ __forceinline__ unsigned long long peek(unsigned long long *slot) {
+  cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*slot);
+  return r.load(cuda::memory_order_acquire);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan(const uint32_t *__restrict__ counts, uint32_t *__restrict__ ends,
+           uint32_t total, unsigned long long *tile_status, uint32_t *tile_ticket,
+           uint32_t *err) {
+  // items staged through shared memory; padded to avoid bank conflicts when
+  // each thread walks its 16 consecutive items.
+  __shared__ uint32_t sm[SCAN_TILE + SCAN_TILE / 32];
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ uint32_t s_tile, s_exclusive;
+  const int t = threadIdx.x;
+  const int lane = t & 31, warp = t >> 5;
+  if (t == 0) s_tile = atomicAdd(tile_ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const size_t base = size_t(tile) * SCAN_TILE;
+
+#define PAD(k) ((k) + ((k) >> 5))
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    const size_t g = base + size_t(k) * SCAN_THREADS + t;
+    const int li = k * SCAN_THREADS + t;
+    sm[PAD(li)] = g < total ? counts[g] : 0u;
+  }
+  __syncthreads();
+  uint32_t v[SCAN_ITEMS];
+  uint32_t run = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    run += sm[PAD(t * SCAN_ITEMS + k)];
+    v[k] = run;
+  }
+  // block-wide exclusive scan of the per-thread totals
+  uint32_t x = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < SCAN_THREADS / 32) s_warp[lane] = w;  // inclusive warp sums
+  }
+  __syncthreads();
+  const uint32_t warp_excl = warp > 0 ? s_warp[warp - 1] : 0u;
+  const uint32_t thread_excl = warp_excl + x - run;
+  const uint32_t tile_sum = s_warp[SCAN_THREADS / 32 - 1];
+
+  // look-back by warp 0
+  if (warp == 0) {
+    if (tile == 0) {
+      if (lane == 0) {
+        publish(&tile_status[0], FLAG_PRE | tile_sum);
+        s_exclusive = 0;
+      }
+    } else {
+      if (lane == 0) publish(&tile_status[tile], FLAG_AGG | tile_sum);
+      uint32_t exclusive = 0;
+      int window_end = int(tile) - 1;  // closest predecessor
+      bool done = false;
+      bool timed_out = false;
+      while (!done) {
+        const int idx = window_end - lane;
+        unsigned long long d = FLAG_PRE;  // lanes before tile 0 read "prefix 0"
+        if (idx >= 0) {
+          int polls = 0;
+          d = peek(&tile_status[idx]);
+          while ((d >> 32) == 0ull) {
+            if (++polls > LOOKBACK_POLL_LIMIT) {
+              timed_out = true;
+              d = FLAG_PRE;  // give up: treat as zero prefix
+              break;
+            }
+            __nanosleep(64);
+            d = peek(&tile_status[idx]);
+          }
+        }
+        const unsigned pre_mask = __ballot_sync(0xffffffffu, (d >> 32) == 2ull);
+        const uint32_t val = idx >= 0 ? uint32_t(d & 0xffffffffull) : 0u;
+        if (pre_mask) {
+          const int first = __ffs(pre_mask) - 1;  // nearest inclusive prefix
+          uint32_t contrib = lane <= first ? val : 0u;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+          exclusive += contrib;
+          done = true;
+        } else {
+          uint32_t contrib = val;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+          exclusive += contrib;
+          window_end -= 32;
+        }
+      }
+      if (__any_sync(0xffffffffu, timed_out) && lane == 0) atomicOr(err, ERR_SCAN_TIMEOUT);
+      if (lane == 0) {
+        publish(&tile_status[tile], FLAG_PRE | (exclusive + tile_sum));
+        s_exclusive = exclusive;
+      }
+    }
+  }
+  __syncthreads();
+  const uint32_t off = s_exclusive + thread_excl;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) sm[PAD(t * SCAN_ITEMS + k)] = off + v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    const size_t g = base + size_t(k) * SCAN_THREADS + t;
+    if (g < total) ends[g] = sm[PAD(k * SCAN_THREADS + t)];
+  }
+#undef PAD
+}
+
+// Scatter every particle to its unsorted slot: begin[cell] + arrival rank.
+__global__ void __launch_bounds__(256) k_scatter(const DevUniforms *__restrict__ U,
+                                                 const uint32_t *__restrict__ cell_of,
+                                                 const uint32_t *__restrict__ rank_of,
+                                                 const uint32_t *__restrict__ begin,
+                                                 uint32_t *__restrict__ t_tmp) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= U->n) return;
+  t_tmp[begin[cell_of[i]] + rank_of[i]] = i;
+}
+
+// Stable counting sort, second half: slot s of the unsorted order holds
+// particle v; its final slot is begin[cell] + #{particles of the cell with a
+// smaller index}. The record is gathered into grid order (grid_reorder.wgsl:
+// 54-62) and both index maps are written.
+__global__ void __launch_bounds__(256)
+    k_sort_gather(const DevUniforms *__restrict__ U, const uint32_t *__restrict__ t_tmp,
+                  const uint32_t *__restrict__ cell_of, const uint32_t *__restrict__ begin,
+                  const float4 *__restrict__ p_pos, const float4 *__restrict__ p_vel,
+                  const float4 *__restrict__ p_force, float4 *__restrict__ s_pos,
+                  float4 *__restrict__ s_vel, float4 *__restrict__ s_frc,
+                  uint32_t *__restrict__ s2o, uint32_t *__restrict__ cidx) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= U->n) return;
+  const uint32_t v = t_tmp[s];
+  const uint32_t c = cell_of[v];
+  const uint32_t b = begin[c], e = begin[c + 1];
+  uint32_t rank = 0;
+  for (uint32_t k = b; k < e; k++) rank += (t_tmp[k] < v) ? 1u : 0u;
+  const uint32_t d = b + rank;
+  s2o[d] = v;
+  cidx[v] = d;
+  s_pos[d] = p_pos[v];
+  s_vel[d] = p_vel[v];
+  s_frc[d] = p_force[v];
+}
+
+inline unsigned blocks_for(uint32_t n, unsigned threads) {
+  return unsigned((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+// counts must be zeroed by the caller (the grid_clear stage).
+cudaError_t launch_hash(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_hash<<<blocks_for(n, 256), 256, 0, st>>>(d.p_pos, d.u, d.cell_of, d.rank_of, d.counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st) {
+  const uint32_t tiles = scan_tiles(total_cells);
+  // descriptors and the ticket counter (stored right after them) start at 0
+  cudaError_t e = cudaMemsetAsync(d.tile_status, 0,
+                                  sizeof(unsigned long long) * (size_t(tiles) + 1), st);
+  if (e != cudaSuccess) return e;
+  k_scan<<<tiles, SCAN_THREADS, 0, st>>>(d.counts, d.cell_begin + 1, total_cells,
+                                         d.tile_status, d.tile_ticket, d.err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.cell_of, d.rank_of, d.cell_begin,
+                                                d.t_tmp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_sort_gather<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.t_tmp, d.cell_of, d.cell_begin,
+                                                    d.p_pos, d.p_vel, d.p_force, d.s_pos,
+                                                    d.s_vel, d.s_frc, d.s2o, d.cidx);
+  return cudaGetLastError();
+}
+
+}  // namespace fs

@@ -1,0 +1,685 @@
+// sph_kernels.cu — per-particle SPH stages of the step on sm_103a.
+//
+// Reference stages (WGSL, src/shaders/):
+//   density + near density + Akinci normal   sph_density_3d_grid.wgsl:56-194
+//   XSPH velocity smoothing                  xsph.wgsl:60-138
+//   near-pressure/viscosity/cohesion force   sph_force_3d_grid.wgsl:63-227
+//   PCISPH predict (fused into force)        pcisph_predict.wgsl:50-73
+//   PCISPH solve, one iteration              pcisph_solve.wgsl:71-208
+//   PCISPH finalize + integrate (fused)      pcisph_finalize.wgsl:50-74,
+//                                            sph_integrate_3d.wgsl:91-388
+//
+// Numerics. This translation unit is compiled with -fmad=false and IEEE
+// division/sqrt, and every expression keeps the shaders' evaluation order, so
+// results are bit-identical to the FP32 restatement of the shaders. sin/cos
+// (the close-pair fallback direction) are evaluated in double and rounded.
+//
+// Neighbour walk. For a particle in unclamped cell (cx,cy,cz) the shaders
+// visit the valid cells of the 3x3x3 block in dz, dy, dx order and each cell
+// in slot order. Cells adjacent in x are adjacent in the sorted arrays, so the
+// three dx cells of a (dy,dz) row form ONE contiguous slot range
+// [begin[row+x0], begin[row+x1+1]): nine contiguous runs per particle, visited
+// in exactly the shaders' order.
+#include "fs_internal.h"
+
+namespace fs {
+namespace {
+
+constexpr float PI_F = 3.14159265359f;  // `const PI: f32` of the shaders
+
+// ---- float3 helpers: one IEEE op per component, no fusion -------------------
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 xyz(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 xyz(const float *a) { return make_float3(a[0], a[1], a[2]); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ float3 normalize3(float3 a) { return a / len3(a); }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float clampf(float e, float lo, float hi) { return fminf(fmaxf(e, lo), hi); }
+__device__ __forceinline__ float signf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+__device__ __forceinline__ float sin_d(float x) { return float(sin(double(x))); }
+__device__ __forceinline__ float cos_d(float x) { return float(cos(double(x))); }
+
+// container_common.wgsl:28-64
+__device__ __forceinline__ float3 world_to_local(const GpuContainerGeometry &c, float3 p) {
+  float3 q = f3(p.x, p.y - c.center_y, p.z);
+  return f3(dot3(xyz(c.inverse_row0), q), dot3(xyz(c.inverse_row1), q), dot3(xyz(c.inverse_row2), q));
+}
+__device__ __forceinline__ float3 local_to_world(const GpuContainerGeometry &c, float3 l) {
+  float3 r = f3(dot3(xyz(c.forward_row0), l), dot3(xyz(c.forward_row1), l), dot3(xyz(c.forward_row2), l));
+  return f3(r.x, r.y + c.center_y, r.z);
+}
+__device__ __forceinline__ float3 world_dir_to_local(const GpuContainerGeometry &c, float3 d) {
+  return f3(dot3(xyz(c.inverse_row0), d), dot3(xyz(c.inverse_row1), d), dot3(xyz(c.inverse_row2), d));
+}
+__device__ __forceinline__ float3 local_dir_to_world(const GpuContainerGeometry &c, float3 d) {
+  return f3(dot3(xyz(c.forward_row0), d), dot3(xyz(c.forward_row1), d), dot3(xyz(c.forward_row2), d));
+}
+
+// Nine contiguous slot runs around the UNCLAMPED cell of `pos`
+// (position_to_cell / is_valid_cell of the neighbour shaders).
+struct Runs {
+  uint32_t lo[9], hi[9];
+  int count;
+};
+__device__ __forceinline__ void neighbor_runs(float3 pos, const GpuGridParams &g,
+                                              const uint32_t *__restrict__ begin, Runs &R) {
+  const long long cx = __float2int_rd((pos.x - g.grid_origin_x) * g.inv_cell_size);
+  const long long cy = __float2int_rd((pos.y - g.grid_origin_y) * g.inv_cell_size);
+  const long long cz = __float2int_rd((pos.z - g.grid_origin_z) * g.inv_cell_size);
+  const long long gx = g.grid_size_x, gy = g.grid_size_y, gz = g.grid_size_z;
+  const long long x0 = cx - 1 < 0 ? 0 : cx - 1;
+  const long long x1 = cx + 1 > gx - 1 ? gx - 1 : cx + 1;
+  R.count = 0;
+  if (x0 > x1) return;
+#pragma unroll
+  for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++) {
+      const long long z = cz + dz, y = cy + dy;
+      if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
+      const uint32_t row = uint32_t(y) * g.grid_size_x + uint32_t(z) * g.grid_size_x * g.grid_size_y;
+      R.lo[R.count] = __ldg(begin + row + uint32_t(x0));
+      R.hi[R.count] = __ldg(begin + row + uint32_t(x1) + 1u);
+      R.count++;
+    }
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---- density ----------------------------------------------------------------
+// boundary_gamma, sph_density_3d_grid.wgsl:86-109
+__device__ __forceinline__ float boundary_gamma(const GpuContainerGeometry &c, float h, float3 pos) {
+  float3 l = world_to_local(c, pos);
+  float gamma = 1.0f;
+  const float d_nx = l.x - (-c.half_width);
+  const float d_px = c.half_width - l.x;
+  const float d_fl = l.y - (-c.half_height);
+  const float d_ce = c.half_height - l.y;
+  const float d_nz = l.z - (-c.half_depth);
+  const float d_pz = c.half_depth - l.z;
+  if (d_nx < h) gamma *= 0.5f + 0.5f * clampf(d_nx / h, 0.0f, 1.0f);
+  if (d_px < h) gamma *= 0.5f + 0.5f * clampf(d_px / h, 0.0f, 1.0f);
+  if (d_fl < h) gamma *= 0.5f + 0.5f * clampf(d_fl / h, 0.0f, 1.0f);
+  if (d_ce < h) gamma *= 0.5f + 0.5f * clampf(d_ce / h, 0.0f, 1.0f);
+  if (d_nz < h) gamma *= 0.5f + 0.5f * clampf(d_nz / h, 0.0f, 1.0f);
+  if (d_pz < h) gamma *= 0.5f + 0.5f * clampf(d_pz / h, 0.0f, 1.0f);
+  return fmaxf(gamma, 0.1f);
+}
+
+__global__ void __launch_bounds__(128) k_density(const DevUniforms *__restrict__ U,
+                                                 const float4 *__restrict__ s_pos,
+                                                 const uint32_t *__restrict__ begin,
+                                                 float2 *__restrict__ s_dens,
+                                                 float4 *__restrict__ s_nrm,
+                                                 unsigned long long *__restrict__ stats) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const GpuSphParams3D &P = U->sph;
+  const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
+  const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
+  const float scale_n = 15.0f / (PI_F * P.kernel_radius_pow6);
+  const float m_over_rho0 = mass / P.rest_density;
+  unsigned long long cand = 0, hits = 0, nonself = 0;
+  if (s < U->n) {
+    const float3 pos_i = xyz(s_pos[s]);
+    float density = 0.0f, near_density = 0.0f;
+    float3 normal = f3(0.f, 0.f, 0.f);
+    Runs R;
+    neighbor_runs(pos_i, U->grid, begin, R);
+    for (int r = 0; r < R.count; r++) {
+      cand += R.hi[r] - R.lo[r];
+      for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
+        const float4 pj = __ldg(s_pos + j);
+        const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+        const float r_sq = rx * rx + ry * ry + rz * rz;
+        if (r_sq < h2) {
+          hits++;
+          const float rr = sqrtf(r_sq);
+          const float diff = h2 - r_sq;
+          density += mass * (scale_d * diff * diff * diff);
+          const float dn = h - rr;
+          near_density += mass * (scale_n * dn * dn * dn);
+          if (r_sq > 1e-12f) {
+            nonself++;
+            normal.x = normal.x + m_over_rho0 * rx * diff * diff;
+            normal.y = normal.y + m_over_rho0 * ry * diff * diff;
+            normal.z = normal.z + m_over_rho0 * rz * diff * diff;
+          }
+        }
+      }
+    }
+    const float gamma = boundary_gamma(U->geom, h, pos_i);
+    density = density / gamma;
+    const float h8 = P.kernel_radius_pow6 * h * h;
+    const float normal_scale = 945.0f / (32.0f * PI_F * h8);
+    normal = normal * normal_scale;
+    s_dens[s] = make_float2(density, near_density);
+    s_nrm[s] = make_float4(normal.x, normal.y, normal.z, 0.0f);
+  }
+  cand = warp_sum_u64(cand);
+  hits = warp_sum_u64(hits);
+  nonself = warp_sum_u64(nonself);
+  if ((threadIdx.x & 31) == 0 && cand) {
+    atomicAdd(stats + STAT_CAND_DENSITY, cand);
+    atomicAdd(stats + STAT_HIT_DENSITY, hits);
+    atomicAdd(stats + STAT_HIT_NONSELF, nonself);
+  }
+}
+
+// ---- XSPH -------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_xsph(const DevUniforms *__restrict__ U,
+                                              const float4 *__restrict__ s_pos,
+                                              const float4 *__restrict__ s_vel,
+                                              const float2 *__restrict__ s_dens,
+                                              const uint32_t *__restrict__ begin,
+                                              float4 *__restrict__ vel_x) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= U->n) return;
+  const GpuSphParams3D &P = U->sph;
+  const float4 vi4 = s_vel[s];
+  const float3 vel_i = xyz(vi4);
+  const float eps = P.xsph_epsilon;
+  if (eps <= 0.0f) {  // xsph.wgsl:94-97: canonical velocity stays pre-XSPH
+    vel_x[s] = vi4;
+    return;
+  }
+  const float h2 = P.kernel_radius_sq, mass = P.mass;
+  const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
+  const float3 pos_i = xyz(s_pos[s]);
+  float3 corr = f3(0.f, 0.f, 0.f);
+  Runs R;
+  neighbor_runs(pos_i, U->grid, begin, R);
+  for (int r = 0; r < R.count; r++) {
+    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
+      const float4 pj = __ldg(s_pos + j);
+      const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+      const float r_sq = rx * rx + ry * ry + rz * rz;
+      if (r_sq < h2 && r_sq > 1e-12f) {
+        const float density_j = fmaxf(__ldg(&s_dens[j].x), 1.0f);
+        const float3 vel_j = xyz(__ldg(s_vel + j));
+        const float diff = h2 - r_sq;
+        const float w = scale_d * diff * diff * diff;
+        corr = corr + (mass / density_j) * (vel_j - vel_i) * w;
+      }
+    }
+  }
+  const float3 v = vel_i + eps * corr;
+  vel_x[s] = make_float4(v.x, v.y, v.z, vi4.w);
+}
+
+// ---- force + PCISPH predict ---------------------------------------------------
+__global__ void __launch_bounds__(128)
+    k_force_predict(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+                    const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
+                    const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
+                    const uint32_t *__restrict__ begin, float4 *__restrict__ anp,
+                    float4 *__restrict__ pred_xp, float *__restrict__ pred_rho) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= U->n) return;
+  const GpuSphParams3D &P = U->sph;
+  const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
+  const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
+  const float scale_c = 32.0f / (PI_F * P.kernel_radius_pow9);
+  const float near_k = P.near_stiffness, visc = P.viscosity, rho0 = P.rest_density;
+  const float3 pos_i = xyz(s_pos[s]);
+  const float3 vel_i = xyz(vel_x[s]);
+  const float2 di = s_dens[s];
+  const float density_i = fmaxf(di.x, 1.0f);
+  const float near_density_i = fmaxf(di.y, 1.0f);
+  const float3 n_i = xyz(s_nrm[s]);
+  const float near_pressure_i = near_k * near_density_i;
+  const float min_dist = h * 0.1f;
+  float3 a_p = f3(0.f, 0.f, 0.f), a_v = f3(0.f, 0.f, 0.f), a_c = f3(0.f, 0.f, 0.f);
+  Runs R;
+  neighbor_runs(pos_i, U->grid, begin, R);
+  for (int r = 0; r < R.count; r++) {
+    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
+      const float3 pos_j = xyz(__ldg(s_pos + j));
+      const float3 r_vec = pos_i - pos_j;
+      const float r_sq = dot3(r_vec, r_vec);
+      if (r_sq < h2 && r_sq > 1e-12f) {
+        const float rr = sqrtf(r_sq);
+        float3 dir;
+        if (rr < min_dist) {
+          const float idx_diff = float(s) - float(j);
+          dir = normalize3(f3(sin_d(idx_diff * 1.0f), cos_d(idx_diff * 2.0f), sin_d(idx_diff * 3.0f)));
+        } else {
+          dir = normalize3(pos_j - pos_i);
+        }
+        const float2 dj = __ldg(s_dens + j);
+        const float density_j = fmaxf(dj.x, 1.0f);
+        const float near_density_j = fmaxf(dj.y, 1.0f);
+        const float near_pressure_j = near_k * near_density_j;
+        const float dg = h - rr;
+        const float grad = scale_g * dg * dg;
+        a_p = a_p + (-mass * (near_pressure_i + near_pressure_j) /
+                     (2.0f * density_i * near_density_j)) * dir * grad;
+        if (rr < min_dist) {
+          const float sep = 200.0f * (1.0f - rr / min_dist);
+          a_p = a_p + (-sep) * dir;
+        }
+        const float3 vel_j = xyz(__ldg(s_vel + j));
+        const float3 v_ij = vel_i - vel_j;
+        const float3 x_ij = pos_i - pos_j;
+        const float v_dot_x = dot3(v_ij, x_ij);
+        if (v_dot_x < 0.0f) {
+          const float mu = h * v_dot_x / (r_sq + 0.01f * h2);
+          const float avg_density = (density_i + density_j) * 0.5f;
+          const float pi_visc = -visc * mu / avg_density;
+          a_v = a_v + (-mass * pi_visc * grad) * dir;
+        }
+        const float K_ij = 2.0f * rho0 / (density_i + density_j);
+        const float r3 = rr * rr * rr;
+        float coh;
+        if (rr >= h * 0.5f) {
+          coh = scale_c * dg * dg * dg * r3;
+        } else {
+          coh = scale_c * (2.0f * dg * dg * dg * r3 - P.kernel_radius_pow6 / 64.0f);
+        }
+        a_c = a_c + (mass * K_ij * coh) * dir;
+        const float3 n_j = xyz(__ldg(s_nrm + j));
+        a_c = a_c - (mass * K_ij) * (n_i - n_j);
+      }
+    }
+  }
+  a_c = a_c * P.surface_tension;
+  const float3 a_g = xyz(U->gravity.direction);
+  const float3 a = a_p + a_v + a_c + a_g;
+  anp[s] = make_float4(a.x, a.y, a.z, 0.0f);
+  // pcisph_predict.wgsl:61-72 on the same particle
+  const float dt = P.dt;
+  const float3 v_star = vel_i + dt * a;
+  const float3 x_star = pos_i + dt * v_star;
+  pred_xp[s] = make_float4(x_star.x, x_star.y, x_star.z, 0.0f);
+  pred_rho[s] = 0.0f;
+}
+
+// ---- PCISPH solve -------------------------------------------------------------
+// One iteration in -> out. Iteration 0 reads the predict output, where every
+// pressure is 0: the pressure-acceleration sum is then +0 exactly, so it is
+// skipped (HAS_PRESSURE=false) with bit-identical results. The last
+// iteration only produces the corrected velocity (finalize's input).
+template <bool HAS_PRESSURE, bool LAST>
+__global__ void __launch_bounds__(128)
+    k_solve(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+            const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
+            const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
+            const float *__restrict__ rho_in, float4 *__restrict__ xp_out,
+            float *__restrict__ rho_out, float4 *__restrict__ v_out,
+            unsigned long long *__restrict__ stats) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const GpuSphParams3D &P = U->sph;
+  const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
+  const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
+  const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
+  unsigned long long cand = 0, hits = 0;
+  if (s < U->n) {
+    const float4 self_xp = xp_in[s];
+    const float3 pred_pos = xyz(self_xp);
+    const float old_p = self_xp.w;
+    const float sd = fmaxf(rho_in[s], 1.0f);
+    const float4 pi4 = s_pos[s];
+    const float3 pos_i = xyz(pi4);
+    float pred_density = 0.0f;
+    float3 a_p = f3(0.f, 0.f, 0.f);
+    Runs R;
+    neighbor_runs(pos_i, U->grid, begin, R);
+    for (int r = 0; r < R.count; r++) {
+      cand += R.hi[r] - R.lo[r];
+      for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
+        const float4 nb = __ldg(xp_in + j);
+        const float3 r_vec = pred_pos - xyz(nb);
+        const float r_sq = dot3(r_vec, r_vec);
+        if (r_sq < h2) {
+          hits++;
+          const float diff = h2 - r_sq;
+          pred_density += mass * (scale_d * diff * diff * diff);
+          if (HAS_PRESSURE && r_sq > 1e-12f) {
+            const float rr = sqrtf(r_sq);
+            const float nd = fmaxf(__ldg(rho_in + j), 1.0f);
+            const float np = nb.w;
+            const float3 dir = (-r_vec) / rr;
+            const float dg = h - rr;
+            const float grad = scale_g * dg * dg;
+            a_p = a_p + (-mass * (old_p / (sd * sd) + np / (nd * nd)) * grad) * dir;
+          }
+        }
+      }
+    }
+    const float density_error = fmaxf(0.0f, pred_density - P.rest_density);
+    const float new_p = old_p + P.pcisph_delta * density_error;
+    const float dt = P.dt;
+    const float max_accel = 0.25f * h / (dt * dt);
+    const float mag_sq = dot3(a_p, a_p);
+    const float max_sq = max_accel * max_accel;
+    if (mag_sq > max_sq) a_p = a_p * (max_accel / sqrtf(mag_sq));
+    const float3 a_total = xyz(anp[s]) + a_p;
+    const float3 v_star = xyz(vel_x[s]) + dt * a_total;
+    if (LAST) {
+      v_out[s] = make_float4(v_star.x, v_star.y, v_star.z, 0.0f);
+    } else {
+      const float3 x_star = pos_i + dt * v_star;
+      xp_out[s] = make_float4(x_star.x, x_star.y, x_star.z, new_p);
+      rho_out[s] = pred_density;
+    }
+  }
+  cand = warp_sum_u64(cand);
+  hits = warp_sum_u64(hits);
+  if ((threadIdx.x & 31) == 0 && cand) {
+    atomicAdd(stats + STAT_CAND_SOLVE, cand);
+    atomicAdd(stats + STAT_HIT_SOLVE, hits);
+  }
+}
+
+// ---- finalize + integrate ----------------------------------------------------
+// SDF texture with clamp-to-edge trilinear filtering (exact FP32 weights).
+__device__ __forceinline__ float sample_sdf(const float *__restrict__ sdf, int res, float3 uvw) {
+  auto texel = [&](int x, int y, int z) -> float {
+    x = min(max(x, 0), res - 1);
+    y = min(max(y, 0), res - 1);
+    z = min(max(z, 0), res - 1);
+    return __ldg(sdf + size_t(x) + size_t(y) * res + size_t(z) * res * res);
+  };
+  const float tx = uvw.x * float(res) - 0.5f;
+  const float ty = uvw.y * float(res) - 0.5f;
+  const float tz = uvw.z * float(res) - 0.5f;
+  const float fx0 = floorf(tx), fy0 = floorf(ty), fz0 = floorf(tz);
+  const float ax = tx - fx0, ay = ty - fy0, az = tz - fz0;
+  // clamp before the +1 neighbour so the index arithmetic cannot overflow
+  const int x0 = min(max(__float2int_rz(fx0), -1), res);
+  const int y0 = min(max(__float2int_rz(fy0), -1), res);
+  const int z0 = min(max(__float2int_rz(fz0), -1), res);
+  auto mix = [](float a, float b, float t) { return a * (1.0f - t) + b * t; };
+  const float c00 = mix(texel(x0, y0, z0), texel(x0 + 1, y0, z0), ax);
+  const float c10 = mix(texel(x0, y0 + 1, z0), texel(x0 + 1, y0 + 1, z0), ax);
+  const float c01 = mix(texel(x0, y0, z0 + 1), texel(x0 + 1, y0, z0 + 1), ax);
+  const float c11 = mix(texel(x0, y0 + 1, z0 + 1), texel(x0 + 1, y0 + 1, z0 + 1), ax);
+  const float c0 = mix(c00, c10, ay);
+  const float c1 = mix(c01, c11, ay);
+  return mix(c0, c1, az);
+}
+
+__device__ __forceinline__ int f2i_rz(float x) { return __float2int_rz(x); }  // saturating, NaN -> 0
+
+__global__ void __launch_bounds__(128)
+    k_finalize_integrate(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+                         const float4 *__restrict__ s_vel, const float4 *__restrict__ vel_x,
+                         const float4 *__restrict__ v_fin, const uint32_t *__restrict__ s2o,
+                         const float *__restrict__ sdf, float4 *__restrict__ p_pos,
+                         float4 *__restrict__ p_vel, float4 *__restrict__ p_force,
+                         GpuRigidBodyAccum *__restrict__ accum) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  int32_t rfx = 0, rfy = 0, rfz = 0, rtx = 0, rty = 0, rtz = 0;
+  uint32_t contact = 0;
+  if (s < U->n) {
+    const GpuSphParams3D &P = U->sph;
+    const GpuContainerGeometry &c = U->geom;
+    const uint32_t orig = s2o[s];
+    // pcisph_finalize.wgsl:57-72
+    const float3 corrected = xyz(v_fin[s]);
+    const float3 original = xyz(vel_x[s]);
+    const float3 dv = corrected - original;
+    p_force[orig] = make_float4(dv.x, dv.y, dv.z, 0.0f);
+    // sph_integrate_3d.wgsl:98-388
+    const float4 pos4 = s_pos[s];
+    float3 pos = xyz(pos4);
+    float3 vel = corrected;
+    const float h = P.kernel_radius;
+    float3 accel = f3(0.f, 0.f, 0.f);
+    const float3 lp = world_to_local(c, pos);
+    const float3 lv = world_dir_to_local(c, vel);
+    const float bl = h * 0.4f;
+    const float wd = 8.0f;
+    float3 wa = f3(0.f, 0.f, 0.f);
+    float d;
+    d = lp.x - (-c.half_width);
+    if (d < bl) { const float t = 1.0f - d / bl; wa.x += c.wall_stiffness * t * t; if (lv.x < 0.0f) wa.x -= lv.x * wd * t; }
+    d = c.half_width - lp.x;
+    if (d < bl) { const float t = 1.0f - d / bl; wa.x -= c.wall_stiffness * t * t; if (lv.x > 0.0f) wa.x -= lv.x * wd * t; }
+    d = lp.y - (-c.half_height);
+    if (d < bl) { const float t = 1.0f - d / bl; wa.y += c.wall_stiffness * t * t; if (lv.y < 0.0f) wa.y -= lv.y * wd * t; }
+    d = c.half_height - lp.y;
+    if (d < bl) { const float t = 1.0f - d / bl; wa.y -= c.wall_stiffness * t * t; if (lv.y > 0.0f) wa.y -= lv.y * wd * t; }
+    d = lp.z - (-c.half_depth);
+    if (d < bl) { const float t = 1.0f - d / bl; wa.z += c.wall_stiffness * t * t; if (lv.z < 0.0f) wa.z -= lv.z * wd * t; }
+    d = c.half_depth - lp.z;
+    if (d < bl) { const float t = 1.0f - d / bl; wa.z -= c.wall_stiffness * t * t; if (lv.z > 0.0f) wa.z -= lv.z * wd * t; }
+    accel = accel + local_dir_to_world(c, wa);
+
+    const GpuMouseForce &M = U->mouse;
+    if (M.is_active == 1u) {
+      const float3 to_mouse = xyz(M.position) - pos;
+      const float dist = len3(to_mouse);
+      if (dist < M.radius && dist > 0.001f) {
+        const float falloff = 1.0f - dist / M.radius;
+        const float3 fd = normalize3(to_mouse);
+        const float sm = M.strength * falloff;
+        switch (M.mode) {
+          case 1: accel = accel + fd * sm; break;
+          case 2: {
+            const float3 axis = normalize3(xyz(M.direction));
+            const float3 tangent = cross3(fd, axis);
+            const float tlen = len3(tangent);
+            if (tlen > 0.001f) accel = accel + (tangent / tlen) * sm;
+            break;
+          }
+          case 3: accel = accel - fd * sm * 3.0f; break;
+          case 4: {
+            const float3 dd = normalize3(fd + f3(0.0f, -1.0f, 0.0f));
+            accel = accel + dd * sm;
+            break;
+          }
+          default: accel = accel - fd * sm; break;
+        }
+      }
+    }
+
+    const GpuRigidBody &B = U->rigid;
+    if (B.is_active != 0u) {
+      const float3 world_rel = pos - xyz(B.position);
+      const float3 rr0 = xyz(B.rot_row0), rr1 = xyz(B.rot_row1), rr2 = xyz(B.rot_row2);
+      const float3 rl = f3(dot3(rr0, world_rel), dot3(rr1, world_rel), dot3(rr2, world_rel));
+      const float he = B.half_extent;
+      float sdf_v;
+      float3 ln = f3(0.f, 0.f, 0.f);
+      switch (B.shape) {
+        case 1: {
+          const float dist = len3(rl);
+          sdf_v = dist - he;
+          ln = dist > 0.001f ? rl / dist : f3(0.f, 1.f, 0.f);
+          break;
+        }
+        case 2: {
+          const float radial = sqrtf(rl.x * rl.x + rl.z * rl.z);
+          const float d_radial = radial - he;
+          const float d_cap = fabsf(rl.y) - he;
+          sdf_v = fmaxf(d_radial, d_cap);
+          if (d_radial > d_cap) {
+            ln = radial > 0.001f ? f3(rl.x / radial, 0.f, rl.z / radial) : f3(1.f, 0.f, 0.f);
+          } else {
+            ln = f3(0.f, signf(rl.y), 0.f);
+          }
+          break;
+        }
+        case 3: {
+          const float minor_r = he * 0.3f;
+          const float xz_len = sqrtf(rl.x * rl.x + rl.z * rl.z);
+          const float qx = xz_len - he, qy = rl.y;
+          const float q_len = sqrtf(qx * qx + qy * qy);
+          sdf_v = q_len - minor_r;
+          if (q_len > 0.001f && xz_len > 0.001f) {
+            const float rdx = qx / q_len, rdy = qy / q_len;
+            ln = f3(rdx * rl.x / xz_len, rdy, rdx * rl.z / xz_len);
+          } else {
+            ln = f3(0.f, 1.f, 0.f);
+          }
+          break;
+        }
+        case 4: {
+          const int res = int(U->sdf_res);
+          const float3 nrm = rl / he;
+          const float3 uvw = nrm * 0.5f + f3(0.5f, 0.5f, 0.5f);
+          const float raw = sample_sdf(sdf, res, uvw);
+          sdf_v = raw * he;
+          const float e = 1.0f / 32.0f;
+          const float gx = sample_sdf(sdf, res, uvw + f3(e, 0.f, 0.f)) - sample_sdf(sdf, res, uvw - f3(e, 0.f, 0.f));
+          const float gy = sample_sdf(sdf, res, uvw + f3(0.f, e, 0.f)) - sample_sdf(sdf, res, uvw - f3(0.f, e, 0.f));
+          const float gz = sample_sdf(sdf, res, uvw + f3(0.f, 0.f, e)) - sample_sdf(sdf, res, uvw - f3(0.f, 0.f, e));
+          const float3 g = f3(gx, gy, gz);
+          const float gl = len3(g);
+          ln = gl > 1e-6f ? g / gl : normalize3(rl + f3(0.f, 1e-6f, 0.f));
+          break;
+        }
+        default: {
+          const float3 dd = f3(fabsf(rl.x) - he, fabsf(rl.y) - he, fabsf(rl.z) - he);
+          sdf_v = fmaxf(dd.x, fmaxf(dd.y, dd.z));
+          if (dd.x >= dd.y && dd.x >= dd.z) ln = f3(signf(rl.x), 0.f, 0.f);
+          else if (dd.y >= dd.x && dd.y >= dd.z) ln = f3(0.f, signf(rl.y), 0.f);
+          else ln = f3(0.f, 0.f, signf(rl.z));
+          break;
+        }
+      }
+      const float range = h * 0.7f;
+      if (sdf_v < range) {
+        const float3 nw = f3(rr0.x * ln.x + rr1.x * ln.y + rr2.x * ln.z,
+                             rr0.y * ln.x + rr1.y * ln.y + rr2.y * ln.z,
+                             rr0.z * ln.x + rr1.z * ln.y + rr2.z * ln.z);
+        const float pen = range - sdf_v;
+        const float t = pen / range;
+        const float3 penalty = nw * B.stiffness * t * t;
+        accel = accel + penalty;
+        float3 damp = f3(0.f, 0.f, 0.f);
+        const float3 rel_vel = vel - xyz(B.velocity);
+        const float vn = dot3(rel_vel, nw);
+        if (vn < 0.0f) {
+          damp = (-nw) * vn * 5.0f;
+          accel = accel + damp;
+        }
+        const float3 reaction = (-(penalty + damp)) * P.mass;
+        rfx = f2i_rz(reaction.x * 1000.0f);
+        rfy = f2i_rz(reaction.y * 1000.0f);
+        rfz = f2i_rz(reaction.z * 1000.0f);
+        contact = 1u;
+        const float3 torque = cross3(world_rel, reaction);
+        rtx = f2i_rz(torque.x * 1000.0f);
+        rty = f2i_rz(torque.y * 1000.0f);
+        rtz = f2i_rz(torque.z * 1000.0f);
+      }
+    }
+
+    const float dt = P.dt;
+    vel = vel + dt * accel;
+    pos = pos + dt * vel;
+    float3 lpn = world_to_local(c, pos);
+    float3 lvn = world_dir_to_local(c, vel);
+    const float rest = c.damping;
+    if (lpn.x < -c.half_width) { lpn.x = -c.half_width; lvn.x = fabsf(lvn.x) * rest; }
+    else if (lpn.x > c.half_width) { lpn.x = c.half_width; lvn.x = -fabsf(lvn.x) * rest; }
+    if (lpn.y < -c.half_height) { lpn.y = -c.half_height; lvn.y = fabsf(lvn.y) * rest; }
+    else if (lpn.y > c.half_height) { lpn.y = c.half_height; lvn.y = -fabsf(lvn.y) * rest; }
+    if (lpn.z < -c.half_depth) { lpn.z = -c.half_depth; lvn.z = fabsf(lvn.z) * rest; }
+    else if (lpn.z > c.half_depth) { lpn.z = c.half_depth; lvn.z = -fabsf(lvn.z) * rest; }
+    const float3 pw = local_to_world(c, lpn);
+    const float3 vw = local_dir_to_world(c, lvn);
+    p_pos[orig] = make_float4(pw.x, pw.y, pw.z, pos4.w);
+    p_vel[orig] = make_float4(vw.x, vw.y, vw.z, s_vel[s].w);
+  }
+  // rigid-body reaction: integer sums are order independent, so reduce in
+  // the warp and add once per warp (sph_integrate_3d.wgsl:328-339)
+  const unsigned any = __ballot_sync(0xffffffffu, contact != 0u);
+  if (any) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      rfx += __shfl_xor_sync(0xffffffffu, rfx, o);
+      rfy += __shfl_xor_sync(0xffffffffu, rfy, o);
+      rfz += __shfl_xor_sync(0xffffffffu, rfz, o);
+      rtx += __shfl_xor_sync(0xffffffffu, rtx, o);
+      rty += __shfl_xor_sync(0xffffffffu, rty, o);
+      rtz += __shfl_xor_sync(0xffffffffu, rtz, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&accum->force_x, rfx);
+      atomicAdd(&accum->force_y, rfy);
+      atomicAdd(&accum->force_z, rfz);
+      atomicAdd(&accum->contact_count, uint32_t(__popc(any)));
+      atomicAdd(&accum->torque_x, rtx);
+      atomicAdd(&accum->torque_y, rty);
+      atomicAdd(&accum->torque_z, rtz);
+    }
+  }
+}
+
+inline unsigned blocks_for(uint32_t n, unsigned threads) {
+  return unsigned((n + threads - 1) / threads);
+}
+
+}  // namespace
+
+cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_density<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.cell_begin, d.s_dens, d.s_nrm,
+                                                d.stats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_xsph<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.s_dens, d.cell_begin,
+                                             d.vel_x);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_force_predict<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.s_dens, d.s_nrm,
+                                                      d.vel_x, d.cell_begin, d.anp,
+                                                      d.pred_xp[0], d.pred_rho[0]);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int in = iter & 1, out = in ^ 1;
+  const unsigned g = blocks_for(n, 128);
+  if (iter == 0 && last)
+    k_solve<false, true><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
+                                            d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
+                                            d.pred_rho[out], d.pred_v, d.stats);
+  else if (iter == 0)
+    k_solve<false, false><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
+                                             d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
+                                             d.pred_rho[out], d.pred_v, d.stats);
+  else if (last)
+    k_solve<true, true><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
+                                           d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
+                                           d.pred_rho[out], d.pred_v, d.stats);
+  else
+    k_solve<true, false><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
+                                            d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
+                                            d.pred_rho[out], d.pred_v, d.stats);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_integrate(const DevState &d, uint32_t n, int /*final_buf*/,
+                                      cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_finalize_integrate<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.vel_x,
+                                                           d.pred_v, d.s2o, d.sdf, d.p_pos,
+                                                           d.p_vel, d.p_force, d.accum);
+  return cudaGetLastError();
+}
+
+}  // namespace fs

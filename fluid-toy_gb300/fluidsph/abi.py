@@ -1,0 +1,201 @@
+"""ctypes binding of libfluidsph.so (include/fluidsph.h).
+
+The structs are the reference's ``#[repr(C)]`` POD structs
+(src/simulation/particle.rs, src/state/simulation.rs, src/state/interaction.rs,
+src/state/rigid_body.rs, src/simulation/sph_3d_grid.rs). Particles cross the
+boundary as ``numpy.float32`` arrays of shape (N, 16), one row per 64-byte
+``SphParticle3D`` record; the column layout is given by the ``COL_*`` slices.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB_PATH
+
+FS_ABI_VERSION = 0x00010040
+FS_OK = 0
+FS_STAGE_COUNT = 10
+FS_STAT_COUNT = 5
+STAGE_NAMES = ("clear", "hash", "scan", "reorder", "density", "xsph", "force_predict",
+               "pcisph_solve", "finalize_integrate", "step")
+
+# SphParticle3D columns (particle.rs:8-17)
+COL_POS = slice(0, 3)
+COL_PAD0 = 3
+COL_VEL = slice(4, 7)
+COL_PAD1 = 7
+COL_FORCE = slice(8, 11)
+COL_DENSITY = 11
+COL_NEAR = 12
+COL_NORMAL = slice(13, 16)
+
+
+class GpuSphParams3D(C.Structure):
+    _fields_ = [("kernel_radius", C.c_float), ("kernel_radius_sq", C.c_float),
+                ("kernel_radius_pow5", C.c_float), ("kernel_radius_pow6", C.c_float),
+                ("kernel_radius_pow9", C.c_float), ("mass", C.c_float),
+                ("rest_density", C.c_float), ("stiffness", C.c_float),
+                ("near_stiffness", C.c_float), ("viscosity", C.c_float), ("dt", C.c_float),
+                ("num_particles", C.c_uint32), ("surface_tension", C.c_float),
+                ("pcisph_delta", C.c_float), ("xsph_epsilon", C.c_float),
+                ("_padding_st", C.c_float)]
+
+
+class GpuContainerGeometry(C.Structure):
+    _fields_ = [("half_width", C.c_float), ("half_height", C.c_float),
+                ("half_depth", C.c_float), ("center_y", C.c_float),
+                ("forward_row0", C.c_float * 4), ("forward_row1", C.c_float * 4),
+                ("forward_row2", C.c_float * 4), ("inverse_row0", C.c_float * 4),
+                ("inverse_row1", C.c_float * 4), ("inverse_row2", C.c_float * 4),
+                ("wall_stiffness", C.c_float), ("damping", C.c_float),
+                ("clip_enabled", C.c_uint32), ("clip_margin", C.c_float)]
+
+
+class GpuGravity(C.Structure):
+    _fields_ = [("direction", C.c_float * 3), ("_padding", C.c_float)]
+
+
+class GpuMouseForce(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("radius", C.c_float), ("strength", C.c_float),
+                ("is_active", C.c_uint32), ("mode", C.c_uint32), ("_pad", C.c_float),
+                ("direction", C.c_float * 3), ("_pad2", C.c_float)]
+
+
+class GpuRigidBody(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("half_extent", C.c_float),
+                ("velocity", C.c_float * 3), ("is_active", C.c_uint32),
+                ("stiffness", C.c_float), ("shape", C.c_uint32), ("_pad1", C.c_float),
+                ("_pad2", C.c_float), ("rot_row0", C.c_float * 4), ("rot_row1", C.c_float * 4),
+                ("rot_row2", C.c_float * 4)]
+
+
+class GpuRigidBodyAccum(C.Structure):
+    _fields_ = [("force_x", C.c_int32), ("force_y", C.c_int32), ("force_z", C.c_int32),
+                ("contact_count", C.c_uint32), ("torque_x", C.c_int32),
+                ("torque_y", C.c_int32), ("torque_z", C.c_int32), ("_pad", C.c_uint32)]
+
+    def as_tuple(self):
+        return (self.force_x, self.force_y, self.force_z, self.contact_count,
+                self.torque_x, self.torque_y, self.torque_z)
+
+
+class GpuGridParams(C.Structure):
+    _fields_ = [("grid_size_x", C.c_uint32), ("grid_size_y", C.c_uint32),
+                ("grid_size_z", C.c_uint32), ("total_cells", C.c_uint32),
+                ("cell_size", C.c_float), ("inv_cell_size", C.c_float),
+                ("grid_origin_x", C.c_float), ("grid_origin_y", C.c_float),
+                ("grid_origin_z", C.c_float), ("num_particles", C.c_uint32),
+                ("_padding", C.c_uint32 * 2)]
+
+
+class FsDevicePointers(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "pos", "vel", "force", "sorted_pos", "sorted_vel", "sorted_density", "sorted_normal",
+        "cell_counts", "cell_starts", "cell_begin", "particle_cell_indices", "sorted_to_orig",
+        "stream")]
+
+
+STRUCT_SIZES = {
+    GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
+    GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48,
+}
+for _t, _n in STRUCT_SIZES.items():
+    assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))
+
+_P = C.POINTER
+_vp = C.c_void_p
+_u32 = C.c_uint32
+_f = C.c_float
+
+# name -> (restype, argtypes); exactly the functions include/fluidsph.h declares
+SIGNATURES = {
+    "fs_last_error": (C.c_char_p, []),
+    "fs_abi_version": (_u32, []),
+    "fs_compute_rest_density": (_f, [_f, _f]),
+    "fs_compute_pcisph_delta": (_f, [_f, _f, _f, _f]),
+    "fs_sph_params_3d": (C.c_int, [_f, _f, _f, _f, _f, _f, _f, _f, _f, _u32,
+                                   _P(GpuSphParams3D)]),
+    "fs_container_geometry": (C.c_int, [_f, _f, _f, _f, _f, _f, _f, _f, _u32, _f,
+                                        _P(GpuContainerGeometry)]),
+    "fs_quat_to_rotation_rows": (C.c_int, [_P(_f), _P(_f)]),
+    "fs_grid_params_for": (C.c_int, [_f, _u32, _P(GpuGridParams)]),
+    "fs_create": (C.c_int, [_vp, _u32, _P(GpuSphParams3D), _P(GpuContainerGeometry), _u32,
+                            _vp, _u32, C.c_int, _u32, _P(_vp)]),
+    "fs_destroy": (C.c_int, [_vp]),
+    "fs_step": (C.c_int, [_vp, _u32]),
+    "fs_update_sph_params": (C.c_int, [_vp, _P(GpuSphParams3D)]),
+    "fs_update_container_geometry": (C.c_int, [_vp, _P(GpuContainerGeometry)]),
+    "fs_update_mouse_force": (C.c_int, [_vp, _P(GpuMouseForce)]),
+    "fs_update_gravity": (C.c_int, [_vp, _P(GpuGravity)]),
+    "fs_update_rigid_body": (C.c_int, [_vp, _P(GpuRigidBody)]),
+    "fs_set_pcisph_iterations": (C.c_int, [_vp, _u32]),
+    "fs_clear_rigid_body_accum": (C.c_int, [_vp]),
+    "fs_read_rigid_body_accum": (C.c_int, [_vp, _P(GpuRigidBodyAccum)]),
+    "fs_num_particles": (C.c_int, [_vp, _P(_u32)]),
+    "fs_grid_params": (C.c_int, [_vp, _P(GpuGridParams)]),
+    "fs_spawn_particles": (C.c_int, [_vp, _P(_f), _u32, _f, _P(_u32)]),
+    "fs_download_particles": (C.c_int, [_vp, _vp, _u32]),
+    "fs_download_sorted": (C.c_int, [_vp, _vp, _u32]),
+    "fs_download_cells": (C.c_int, [_vp, _vp, _vp, _u32]),
+    "fs_download_index_maps": (C.c_int, [_vp, _vp, _vp, _u32]),
+    "fs_upload_particles": (C.c_int, [_vp, _vp, _u32]),
+    "fs_device_pointers": (C.c_int, [_vp, _P(FsDevicePointers)]),
+    "fs_set_stream": (C.c_int, [_vp, _vp]),
+    "fs_sync": (C.c_int, [_vp]),
+    "fs_enable_stage_timing": (C.c_int, [_vp, C.c_int]),
+    "fs_stage_times": (C.c_int, [_vp, _P(C.c_double), _P(_u32), C.c_int]),
+    "fs_neighbor_stats": (C.c_int, [_vp, _P(C.c_uint64), C.c_int]),
+}
+
+_lib = None
+
+
+class FluidSphError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"fluidsph error {code}: {message}")
+        self.code = code
+
+
+def load(path: Path | str | None = None):
+    """Load libfluidsph.so (built by fluidsph.build). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is missing: build it with fluidsph.build.build_library() "
+            "(there is no CPU fallback for the SPH step)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.fs_abi_version() != FS_ABI_VERSION:
+        raise FluidSphError(-2, "library ABI version differs from this binding")
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != FS_OK:
+        msg = _lib.fs_last_error().decode() if _lib is not None else "library not loaded"
+        raise FluidSphError(rc, msg)
+
+
+def exported_symbols(header: Path) -> list[str]:
+    """Function names declared in a C header (``fs_*(`` declarations)."""
+    import re
+    text = header.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fs_[a-z0-9_]+)\s*\(", text)))
+
+
+def as_particles(arr: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(arr, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] != 16:
+        raise ValueError("particles must be an (N, 16) float32 array of SphParticle3D rows")
+    return a

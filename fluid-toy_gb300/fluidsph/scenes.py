@@ -1,0 +1,163 @@
+"""Seeded synthetic scenes for the SPH step (the workloads' inputs).
+
+The reference seeds its lattice jitter from the wall clock
+(src/simulation/particle.rs:54-55, 64-76), so its inputs are not reproducible;
+these generators replace it with SplitMix64 streams.
+
+Frame mapping: a box [0,Lx]x[0,Ly]x[0,Lz] becomes the reference container
+with half extents L/2, floor_y = 0 (center_y = Ly/2), no tilt, and particles
+shifted by (-Lx/2, 0, -Lz/2). A lattice block sits at the box's min corner
+offset by one spacing (a dam break); every coordinate gets independent jitter
+U[-0.002, 0.002].
+
+Common parameters: h 0.08, rest density 8000 (set directly), mass 1,
+near_stiffness 0.45, viscosity 15, surface_tension 6.5, wall_stiffness 250,
+damping 0.55, dt 0.008, gravity (0,-9.81,0), xsph_epsilon 0.305, 4 PCISPH
+iterations, stiffness 35 (read by no stage), pcisph_delta from
+compute_pcisph_delta(0.08, 1, 8000, 0.008).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import params as P
+from .abi import COL_POS, COL_VEL, GpuContainerGeometry, GpuGravity, GpuRigidBody, GpuSphParams3D
+
+GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(seed: int, count: int) -> np.ndarray:
+    """First `count` outputs of SplitMix64 seeded with `seed` (uint64)."""
+    with np.errstate(over="ignore"):
+        k = np.arange(1, count + 1, dtype=np.uint64)
+        x = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + k * GOLDEN
+        z = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform01(seed: int, count: int) -> np.ndarray:
+    """Uniform doubles in [0, 1) from the top 53 bits of SplitMix64."""
+    return (splitmix64(seed, count) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+@dataclass
+class Common:
+    h: float = 0.08
+    rest_density: float = 8000.0
+    mass: float = 1.0
+    stiffness: float = 35.0
+    near_stiffness: float = 0.45
+    viscosity: float = 15.0
+    surface_tension: float = 6.5
+    wall_stiffness: float = 250.0
+    damping: float = 0.55
+    dt: float = 0.008
+    gravity: float = -9.81
+    xsph_epsilon: float = 0.305
+    iterations: int = 4
+
+
+@dataclass
+class Scene:
+    name: str
+    particles: np.ndarray
+    sph: GpuSphParams3D
+    geom: GpuContainerGeometry
+    gravity: GpuGravity
+    rigid: GpuRigidBody | None
+    iterations: int
+    steps: int
+    box: tuple
+    info: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return len(self.particles)
+
+
+def lattice_block(nx: int, ny: int, nz: int, box, spacing: float = 0.02, jitter: float = 0.002,
+                  seed: int = 0) -> np.ndarray:
+    """(N,16) SphParticle3D rows of an nx*ny*nz lattice at the box's min corner
+    (offset one spacing), x fastest then z then y, in the container frame."""
+    Lx, Ly, Lz = box
+    iy, iz, ix = np.meshgrid(np.arange(ny), np.arange(nz), np.arange(nx), indexing="ij")
+    ix, iy, iz = ix.ravel(), iy.ravel(), iz.ravel()
+    n = ix.size
+    u = uniform01(seed, 3 * n).reshape(n, 3)
+    j = -jitter + 2.0 * jitter * u
+    pos = np.empty((n, 3), np.float64)
+    pos[:, 0] = (ix + 1) * spacing - Lx / 2.0 + j[:, 0]
+    pos[:, 1] = (iy + 1) * spacing + j[:, 1]
+    pos[:, 2] = (iz + 1) * spacing - Lz / 2.0 + j[:, 2]
+    out = np.zeros((n, 16), np.float32)
+    out[:, COL_POS] = pos.astype(np.float32)
+    return out
+
+
+def make_scene(name: str, particles: np.ndarray, box, c: Common | None = None, steps: int = 1,
+               rigid: GpuRigidBody | None = None, tilt_x: float = 0.0, tilt_z: float = 0.0,
+               info: dict | None = None) -> Scene:
+    c = c or Common()
+    Lx, Ly, Lz = box
+    sph = P.sph_params_3d(c.h, c.mass, c.rest_density, c.stiffness, c.near_stiffness,
+                          c.viscosity, c.surface_tension, c.xsph_epsilon, c.dt, len(particles))
+    geom = P.container_geometry(Lx, Lz, 0.0, Ly, tilt_x, tilt_z, c.wall_stiffness, c.damping)
+    return Scene(name, particles, sph, geom, P.gravity(c.gravity), rigid, c.iterations, steps,
+                 tuple(box), info or {})
+
+
+def config0(seed: int = 0) -> Scene:
+    """Plain dam break: 40x40x31 = 49,600 particles in a 1.6x1.2x0.8 box, 1000 steps."""
+    box = (1.6, 1.2, 0.8)
+    return make_scene("dam_break_49600", lattice_block(40, 40, 31, box, seed=seed), box, steps=1000)
+
+
+def config1(seed: int = 0) -> Scene:
+    """Plain at scale: 128x64x128 = 1,048,576 particles in a 4x2x3 box with a held
+    sphere (radius 0.3, box centre (3.0,0.4,1.5) -> container (1.0,0.4,0.0)), 500 steps."""
+    box = (4.0, 2.0, 3.0)
+    c = Common()
+    rb = P.rigid_body(position=(3.0 - box[0] / 2, 0.4, 1.5 - box[2] / 2), half_extent=0.3,
+                      active=True, stiffness=c.wall_stiffness, shape=1)
+    return make_scene("dam_break_1048576_sphere", lattice_block(128, 64, 128, box, seed=seed),
+                      box, c, steps=500, rigid=rb)
+
+
+def small_scene(nx: int = 10, ny: int = 8, nz: int = 6, box=(0.6, 0.5, 0.4), seed: int = 1,
+                c: Common | None = None, **kw) -> Scene:
+    """A few hundred particles for quick parity checks."""
+    return make_scene(f"small_{nx}x{ny}x{nz}", lattice_block(nx, ny, nz, box, seed=seed), box,
+                      c, **kw)
+
+
+def fourier_velocity(pos: np.ndarray, seed: int, modes: int = 8, amplitude: float = 0.5,
+                     box=(1.2, 1.0, 1.0)) -> np.ndarray:
+    """Smooth random velocity field: sum of `modes` Fourier modes with random
+    wave vectors (integer multiples of 2*pi/L), directions and phases, scaled
+    so the largest speed is `amplitude`."""
+    u = uniform01(seed, modes * 7).reshape(modes, 7)
+    k = np.floor(1 + 3 * u[:, 0:3]) * (2 * np.pi / np.asarray(box))
+    d = u[:, 3:6] - 0.5
+    d /= np.linalg.norm(d, axis=1, keepdims=True) + 1e-12
+    phase = 2 * np.pi * u[:, 6]
+    v = np.zeros_like(pos, dtype=np.float64)
+    for m in range(modes):
+        v += np.sin(pos @ k[m] + phase[m])[:, None] * d[m][None, :]
+    v *= amplitude / max(np.abs(v).max(), 1e-12)
+    return v
+
+
+def config3(seed: int = 0) -> Scene:
+    """Differentiable rollout: 32^3 = 32,768 particles in a 1.2x1x1 box with a
+    smooth random initial velocity (8 Fourier modes, 0.5 m/s), 200 steps."""
+    box = (1.2, 1.0, 1.0)
+    parts = lattice_block(32, 32, 32, box, seed=seed)
+    v = fourier_velocity(parts[:, COL_POS].astype(np.float64), seed + 1000, box=box)
+    parts[:, COL_VEL] = v.astype(np.float32)
+    return make_scene("rollout_32768", parts, box, steps=200)
+
+
+CONFIGS = {0: config0, 1: config1, 3: config3}

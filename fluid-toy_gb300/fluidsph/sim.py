@@ -1,0 +1,170 @@
+"""Python mirror of the reference's ``SphSimulation3DGrid``
+(src/simulation/sph_3d_grid.rs:33-1569) over the C ABI of libfluidsph.so.
+
+Method names and argument meaning follow the Rust type: ``new`` becomes the
+constructor, ``step`` runs one substep (or ``nsteps``), the ``update_*``
+methods upload parameter structs, ``set_pcisph_iterations`` clamps to >= 1,
+``read_rigid_body_accum`` synchronises, ``spawn_particles`` clips at capacity.
+Read-outs return numpy arrays. Errors raise ``FluidSphError`` (the reference
+panics on wgpu validation errors; this library reports a status instead).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import (FS_ABI_VERSION, FS_STAGE_COUNT, FS_STAT_COUNT, GpuContainerGeometry,
+                  GpuGravity, GpuGridParams, GpuMouseForce, GpuRigidBody, GpuRigidBodyAccum,
+                  GpuSphParams3D, check)
+
+
+class SphSimulation3DGrid:
+    def __init__(self, particles: np.ndarray, sph_params: GpuSphParams3D,
+                 container_geom: GpuContainerGeometry, max_particles: int = 0,
+                 sdf: np.ndarray | None = None, device: int = 0):
+        self._lib = abi.load()
+        parts = abi.as_particles(particles) if len(particles) else np.zeros((0, 16), np.float32)
+        self._parts_keep = parts
+        sdf_ptr, sdf_res = None, 0
+        if sdf is not None:
+            sdf = np.ascontiguousarray(sdf, dtype=np.float32)
+            sdf_res = int(round(sdf.size ** (1.0 / 3.0)))
+            if sdf_res ** 3 != sdf.size:
+                raise ValueError("sdf must hold res^3 values")
+            sdf_ptr = sdf.ctypes.data
+        h = C.c_void_p()
+        check(self._lib.fs_create(parts.ctypes.data if len(parts) else None, len(parts),
+                                  C.byref(sph_params), C.byref(container_geom),
+                                  int(max_particles), sdf_ptr, sdf_res, int(device),
+                                  FS_ABI_VERSION, C.byref(h)))
+        self._h = h
+        self._grid = GpuGridParams()
+        check(self._lib.fs_grid_params(self._h, C.byref(self._grid)))
+
+    # -- lifetime ---------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.fs_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- step and parameter uploads (sph_3d_grid.rs:1261-1477) --------------------
+    def step(self, nsteps: int = 1) -> None:
+        check(self._lib.fs_step(self._h, int(nsteps)))
+
+    def update_sph_params(self, params: GpuSphParams3D) -> None:
+        check(self._lib.fs_update_sph_params(self._h, C.byref(params)))
+
+    def update_container_geometry(self, geom: GpuContainerGeometry) -> None:
+        check(self._lib.fs_update_container_geometry(self._h, C.byref(geom)))
+
+    def update_mouse_force(self, mouse: GpuMouseForce) -> None:
+        check(self._lib.fs_update_mouse_force(self._h, C.byref(mouse)))
+
+    def update_gravity(self, gravity: GpuGravity) -> None:
+        check(self._lib.fs_update_gravity(self._h, C.byref(gravity)))
+
+    def update_rigid_body(self, body: GpuRigidBody) -> None:
+        check(self._lib.fs_update_rigid_body(self._h, C.byref(body)))
+
+    def set_pcisph_iterations(self, iterations: int) -> None:
+        check(self._lib.fs_set_pcisph_iterations(self._h, int(iterations)))
+
+    def clear_rigid_body_accum(self) -> None:
+        check(self._lib.fs_clear_rigid_body_accum(self._h))
+
+    def read_rigid_body_accum(self) -> GpuRigidBodyAccum:
+        out = GpuRigidBodyAccum()
+        check(self._lib.fs_read_rigid_body_accum(self._h, C.byref(out)))
+        self._last_accum = out
+        return out
+
+    def rigid_body_accum(self) -> GpuRigidBodyAccum:
+        return getattr(self, "_last_accum", GpuRigidBodyAccum())
+
+    def num_particles(self) -> int:
+        v = C.c_uint32()
+        check(self._lib.fs_num_particles(self._h, C.byref(v)))
+        return v.value
+
+    def grid_params(self) -> GpuGridParams:
+        g = GpuGridParams()
+        check(self._lib.fs_grid_params(self._h, C.byref(g)))
+        return g
+
+    def spawn_particles(self, position, count: int, spread: float) -> int:
+        pos = (C.c_float * 3)(*[float(v) for v in position])
+        out = C.c_uint32()
+        check(self._lib.fs_spawn_particles(self._h, pos, int(count), float(spread), C.byref(out)))
+        return out.value
+
+    def sync(self) -> None:
+        check(self._lib.fs_sync(self._h))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(self._lib.fs_set_stream(self._h, stream_ptr))
+
+    # -- read-outs ------------------------------------------------------------------
+    def particles(self, count: int | None = None) -> np.ndarray:
+        n = self.num_particles() if count is None else int(count)
+        out = np.empty((n, 16), np.float32)
+        check(self._lib.fs_download_particles(self._h, out.ctypes.data, n))
+        return out
+
+    def upload_particles(self, particles: np.ndarray) -> None:
+        p = abi.as_particles(particles)
+        check(self._lib.fs_upload_particles(self._h, p.ctypes.data, len(p)))
+
+    def sorted_particles(self, count: int | None = None) -> np.ndarray:
+        n = self.num_particles() if count is None else int(count)
+        out = np.empty((n, 16), np.float32)
+        check(self._lib.fs_download_sorted(self._h, out.ctypes.data, n))
+        return out
+
+    def cells(self) -> tuple[np.ndarray, np.ndarray]:
+        g = self._grid.total_cells
+        counts = np.empty(g, np.uint32)
+        starts = np.empty(g, np.uint32)
+        check(self._lib.fs_download_cells(self._h, counts.ctypes.data, starts.ctypes.data, g))
+        return counts, starts
+
+    def index_maps(self) -> tuple[np.ndarray, np.ndarray]:
+        n = self.num_particles()
+        ci = np.empty(n, np.uint32)
+        so = np.empty(n, np.uint32)
+        check(self._lib.fs_download_index_maps(self._h, ci.ctypes.data, so.ctypes.data, n))
+        return ci, so
+
+    def device_pointers(self) -> abi.FsDevicePointers:
+        p = abi.FsDevicePointers()
+        check(self._lib.fs_device_pointers(self._h, C.byref(p)))
+        return p
+
+    # -- measurement ------------------------------------------------------------------
+    def enable_stage_timing(self, enable: bool = True) -> None:
+        check(self._lib.fs_enable_stage_timing(self._h, 1 if enable else 0))
+
+    def stage_times(self, reset: bool = True) -> tuple[dict, int]:
+        ms = (C.c_double * FS_STAGE_COUNT)()
+        steps = C.c_uint32()
+        check(self._lib.fs_stage_times(self._h, ms, C.byref(steps), 1 if reset else 0))
+        return {name: ms[i] for i, name in enumerate(abi.STAGE_NAMES)}, steps.value
+
+    def neighbor_stats(self, reset: bool = True) -> dict:
+        out = (C.c_uint64 * FS_STAT_COUNT)()
+        check(self._lib.fs_neighbor_stats(self._h, out, 1 if reset else 0))
+        keys = ("cand_density", "hits_density", "hits_nonself", "cand_solve", "hits_solve")
+        return {k: int(out[i]) for i, k in enumerate(keys)}

@@ -1,0 +1,317 @@
+/*
+ * fluidsph.h — C ABI of the GB300 (sm_103a) SPH step library, libfluidsph.so.
+ *
+ * This is the drop-in boundary for fluid-toy's per-substep SPH compute path,
+ * `SphSimulation3DGrid` (src/simulation/sph_3d_grid.rs:33-1569 in the
+ * reference). Every parameter struct below is byte-for-byte the reference's
+ * `#[repr(C)]` POD struct, so a Rust caller passes its existing values through
+ * `extern "C"` unchanged.
+ *
+ * Conventions
+ *   - Every function returns an `int` status: FS_OK (0) or a negative FS_E_*.
+ *     Nothing aborts and no C++ exception crosses the ABI. `fs_last_error()`
+ *     returns a thread-local message describing the last failure.
+ *   - A simulation owns one CUDA stream. `fs_step` is asynchronous on it (the
+ *     reference's `queue.submit` is asynchronous too); the download and
+ *     `fs_read_rigid_body_accum` calls synchronise the stream.
+ *   - Device memory is allocated in `fs_create` for `max_particles` and never
+ *     grows, like the reference's buffers (sph_3d_grid.rs:196-305).
+ *   - Kernels that wait on other blocks (the single-pass scan) give up after a
+ *     bounded number of polls and raise a device error word; the next
+ *     synchronising call returns FS_E_DEVICE_TIMEOUT instead of hanging.
+ */
+#ifndef FLUIDSPH_H
+#define FLUIDSPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ABI version: bumped whenever a struct layout or signature changes. It also
+ * encodes the struct sizes so a caller built against another layout fails in
+ * fs_create instead of corrupting memory. */
+#define FS_ABI_VERSION 0x00010040u
+
+/* ---- status codes -------------------------------------------------------- */
+#define FS_OK 0
+#define FS_E_INVALID_ARGUMENT (-1) /* null pointer, zero/NaN size, bad enum  */
+#define FS_E_ABI_MISMATCH (-2)     /* caller built against another layout   */
+#define FS_E_CAPACITY (-3)         /* N or a size beyond the allocated max   */
+#define FS_E_CUDA (-4)             /* a CUDA runtime call failed             */
+#define FS_E_DEVICE_TIMEOUT (-5)   /* a bounded device-side wait gave up     */
+#define FS_E_NO_DEVICE (-6)        /* no CUDA device / library not usable    */
+#define FS_E_STATE (-7)            /* call not valid in the current state    */
+
+/* ---- boundary structs (reference layouts) -------------------------------- */
+
+/* SphParticle3D, src/simulation/particle.rs:8-17 — 64-byte AoS record. */
+typedef struct SphParticle3D {
+    float position[3]; /* @0  */
+    float _pad0;       /* @12 */
+    float velocity[3]; /* @16 */
+    float _pad1;       /* @28 */
+    float force[3];    /* @32: non-pressure accel, then dv after finalize */
+    float density;     /* @44 */
+    float near_density;/* @48 */
+    float normal[3];   /* @52: Akinci surface normal */
+} SphParticle3D;
+
+/* GpuSphParams3D, src/state/simulation.rs:344-361 — 64 bytes. `stiffness` is
+ * carried for layout parity; no step stage reads it (the reference's pressure
+ * stiffness is `pcisph_delta`). */
+typedef struct GpuSphParams3D {
+    float kernel_radius;
+    float kernel_radius_sq;
+    float kernel_radius_pow5;
+    float kernel_radius_pow6;
+    float kernel_radius_pow9;
+    float mass;
+    float rest_density;
+    float stiffness;
+    float near_stiffness;
+    float viscosity;
+    float dt;
+    uint32_t num_particles;
+    float surface_tension;
+    float pcisph_delta;
+    float xsph_epsilon;
+    float _padding_st;
+} GpuSphParams3D;
+
+/* GpuContainerGeometry, src/state/simulation.rs:367-386 — 128 bytes. Forward
+ * rows are R = Rz*Rx (local->world), inverse rows are R^T. */
+typedef struct GpuContainerGeometry {
+    float half_width;
+    float half_height;
+    float half_depth;
+    float center_y;
+    float forward_row0[4];
+    float forward_row1[4];
+    float forward_row2[4];
+    float inverse_row0[4];
+    float inverse_row1[4];
+    float inverse_row2[4];
+    float wall_stiffness;
+    float damping;
+    uint32_t clip_enabled;
+    float clip_margin;
+} GpuContainerGeometry;
+
+/* GpuGravity, src/state/simulation.rs:391-394 — 16 bytes. */
+typedef struct GpuGravity {
+    float direction[3];
+    float _padding;
+} GpuGravity;
+
+/* GpuMouseForce, src/state/interaction.rs:102-111 — 48 bytes.
+ * mode: 0 push, 1 pull, 2 vortex, 3 explode, 4 drain (interaction.rs:5-11). */
+typedef struct GpuMouseForce {
+    float position[3];
+    float radius;
+    float strength;
+    uint32_t is_active;
+    uint32_t mode;
+    float _pad;
+    float direction[3];
+    float _pad2;
+} GpuMouseForce;
+
+/* GpuRigidBody, src/state/rigid_body.rs:212-224 — 96 bytes.
+ * shape: 0 cube, 1 sphere, 2 cylinder, 3 torus, 4 custom SDF. Rotation rows
+ * are world->local (rigid_body.rs:188-205). */
+typedef struct GpuRigidBody {
+    float position[3];
+    float half_extent;
+    float velocity[3];
+    uint32_t is_active;
+    float stiffness;
+    uint32_t shape;
+    float _pad1;
+    float _pad2;
+    float rot_row0[4];
+    float rot_row1[4];
+    float rot_row2[4];
+} GpuRigidBody;
+
+/* GpuRigidBodyAccum, src/state/rigid_body.rs:247-256 — 32 bytes, fixed point
+ * x1000 (each particle's contribution truncated toward zero). */
+typedef struct GpuRigidBodyAccum {
+    int32_t force_x;
+    int32_t force_y;
+    int32_t force_z;
+    uint32_t contact_count;
+    int32_t torque_x;
+    int32_t torque_y;
+    int32_t torque_z;
+    uint32_t _pad;
+} GpuRigidBodyAccum;
+
+/* GpuGridParams, src/simulation/sph_3d_grid.rs:15-30 — 48 bytes. */
+typedef struct GpuGridParams {
+    uint32_t grid_size_x;
+    uint32_t grid_size_y;
+    uint32_t grid_size_z;
+    uint32_t total_cells;
+    float cell_size;
+    float inv_cell_size;
+    float grid_origin_x;
+    float grid_origin_y;
+    float grid_origin_z;
+    uint32_t num_particles;
+    uint32_t _padding[2];
+} GpuGridParams;
+
+/* Device pointers of a simulation, the analogue of the reference's buffer
+ * getters (sph_3d_grid.rs:1500-1530). The library keeps particles as
+ * structure-of-arrays float4 records (one coalesced 16-byte load per field),
+ * not the reference's 64-byte AoS; fs_download_particles/_sorted rebuild the
+ * AoS view. */
+typedef struct FsDevicePointers {
+    void *pos;            /* float4[max] canonical (x,y,z,_pad0)            */
+    void *vel;            /* float4[max] canonical (vx,vy,vz,_pad1)         */
+    void *force;          /* float4[max] canonical (fx,fy,fz,0)             */
+    void *sorted_pos;     /* float4[max] grid-sorted positions              */
+    void *sorted_vel;     /* float4[max] grid-sorted pre-XSPH velocities    */
+    void *sorted_density; /* float2[max] (density, near_density)            */
+    void *sorted_normal;  /* float4[max] (nx,ny,nz,0)                       */
+    void *cell_counts;    /* uint32[total_cells]                            */
+    void *cell_starts;    /* uint32[total_cells] inclusive ends (reference) */
+    void *cell_begin;     /* uint32[total_cells+1] exclusive begins         */
+    void *particle_cell_indices; /* uint32[max] orig -> sorted slot         */
+    void *sorted_to_orig; /* uint32[max] sorted slot -> orig                */
+    void *stream;         /* cudaStream_t the simulation launches on        */
+} FsDevicePointers;
+
+typedef struct FsSim FsSim; /* opaque SphSimulation3DGrid */
+
+/* ---- library ------------------------------------------------------------- */
+
+/* Thread-local description of the last error (never NULL). */
+const char *fs_last_error(void);
+/* FS_ABI_VERSION of the built library. */
+uint32_t fs_abi_version(void);
+
+/* ---- host-side constants (restating src/state/simulation.rs) ------------- */
+
+/* compute_rest_density, src/state/simulation.rs:402-425. */
+float fs_compute_rest_density(float h, float mass);
+/* compute_pcisph_delta, src/state/simulation.rs:429-480. */
+float fs_compute_pcisph_delta(float h, float mass, float rest_density, float dt);
+/* SphConfig::to_gpu_params_3d, src/state/simulation.rs:315-337, with the rest
+ * density passed in (the reference derives it from h and mass; pass
+ * fs_compute_rest_density(h, mass) for the reference's own value). */
+int fs_sph_params_3d(float kernel_radius, float mass, float rest_density,
+                     float stiffness, float near_stiffness, float viscosity,
+                     float surface_tension, float xsph_epsilon, float dt,
+                     uint32_t num_particles, GpuSphParams3D *out);
+/* ContainerConfig::to_gpu_geometry, src/state/simulation.rs:139-184. */
+int fs_container_geometry(float width, float depth, float floor_y, float height,
+                          float tilt_x, float tilt_z, float wall_stiffness,
+                          float damping, uint32_t clip_enabled, float clip_margin,
+                          GpuContainerGeometry *out);
+/* quat_to_rotation_rows, src/state/rigid_body.rs:188-205 (q = x,y,z,w). */
+int fs_quat_to_rotation_rows(const float q[4], float rows[12]);
+/* Grid sizing of SphSimulation3DGrid::new, sph_3d_grid.rs:121-143. */
+int fs_grid_params_for(float kernel_radius, uint32_t num_particles,
+                       GpuGridParams *out);
+
+/* ---- SphSimulation3DGrid ------------------------------------------------- */
+
+/* SphSimulation3DGrid::new, sph_3d_grid.rs:104-1258. `sdf` may be NULL (the
+ * reference then binds a 1x1x1 texture holding 1.0, i.e. "outside"); else it
+ * is sdf_res^3 floats, x fastest, sampled with clamp-to-edge trilinear
+ * filtering. `device` selects the CUDA device. max_particles is raised to n
+ * like the reference (sph_3d_grid.rs:114). Gravity starts at (0,-9.8,0), the
+ * mouse force and rigid body start inactive at their reference defaults. */
+int fs_create(const SphParticle3D *particles, uint32_t num_particles,
+              const GpuSphParams3D *params, const GpuContainerGeometry *geom,
+              uint32_t max_particles, const float *sdf, uint32_t sdf_res,
+              int device, uint32_t abi_version, FsSim **out);
+int fs_destroy(FsSim *sim);
+
+/* step(), sph_3d_grid.rs:1261-1444, run `nsteps` times back to back on the
+ * simulation's stream. With nsteps > 1 the step sequence is replayed from a
+ * captured CUDA graph. Asynchronous. */
+int fs_step(FsSim *sim, uint32_t nsteps);
+
+/* update_* uploads, sph_3d_grid.rs:1446-1473. Ordered before later steps. */
+int fs_update_sph_params(FsSim *sim, const GpuSphParams3D *params);
+int fs_update_container_geometry(FsSim *sim, const GpuContainerGeometry *geom);
+int fs_update_mouse_force(FsSim *sim, const GpuMouseForce *mouse);
+int fs_update_gravity(FsSim *sim, const GpuGravity *gravity);
+int fs_update_rigid_body(FsSim *sim, const GpuRigidBody *body);
+/* set_pcisph_iterations, sph_3d_grid.rs:1475-1477 (clamped to >= 1). */
+int fs_set_pcisph_iterations(FsSim *sim, uint32_t iterations);
+
+/* clear_rigid_body_accum / read_rigid_body_accum, sph_3d_grid.rs:1479-1498.
+ * The read synchronises the stream. */
+int fs_clear_rigid_body_accum(FsSim *sim);
+int fs_read_rigid_body_accum(FsSim *sim, GpuRigidBodyAccum *out);
+
+/* num_particles(), sph_3d_grid.rs:1528-1530. */
+int fs_num_particles(const FsSim *sim, uint32_t *out);
+/* grid parameters the simulation was built with (grid_params_buffer). */
+int fs_grid_params(const FsSim *sim, GpuGridParams *out);
+
+/* spawn_particles, sph_3d_grid.rs:1534-1569: golden-angle spiral, clipped at
+ * capacity; *spawned receives the count actually added. */
+int fs_spawn_particles(FsSim *sim, const float position[3], uint32_t count,
+                       float spread, uint32_t *spawned);
+
+/* ---- read-outs (synchronising) ------------------------------------------- */
+
+/* Canonical particle buffer as the reference's 64-byte AoS (particle_buffer). */
+int fs_download_particles(FsSim *sim, SphParticle3D *out, uint32_t count);
+/* Grid-sorted particle buffer as 64-byte AoS (sorted_particle_buffer): the
+ * record copied at reorder, with density, near_density and normal as written
+ * by the density pass. */
+int fs_download_sorted(FsSim *sim, SphParticle3D *out, uint32_t count);
+/* cell_counts_buffer and cell_starts_buffer (inclusive prefix ends). Either
+ * pointer may be NULL. */
+int fs_download_cells(FsSim *sim, uint32_t *counts, uint32_t *starts,
+                      uint32_t total_cells);
+/* particle_cell_indices (orig -> sorted slot after reorder) and
+ * sorted_to_orig. Either pointer may be NULL. */
+int fs_download_index_maps(FsSim *sim, uint32_t *cell_indices,
+                           uint32_t *sorted_to_orig, uint32_t count);
+/* Overwrite the canonical particle records (all fields) of [0, count). */
+int fs_upload_particles(FsSim *sim, const SphParticle3D *particles,
+                        uint32_t count);
+
+/* Borrow device memory zero-copy (buffer getters). */
+int fs_device_pointers(FsSim *sim, FsDevicePointers *out);
+/* Launch on a caller-provided cudaStream_t from now on (NULL = own stream). */
+int fs_set_stream(FsSim *sim, void *cuda_stream);
+/* Wait for all queued work; reports a device-side wait timeout if one fired. */
+int fs_sync(FsSim *sim);
+
+/* ---- per-stage timing ---------------------------------------------------- */
+
+#define FS_STAGE_COUNT 10
+/* Stage ids for fs_stage_times: 0 clear, 1 hash, 2 scan, 3 reorder,
+ * 4 density, 5 xsph, 6 force+predict, 7 pcisph solve (all iterations),
+ * 8 finalize+integrate, 9 whole step. */
+/* Enable CUDA-event timing of every stage of subsequent fs_step calls (graph
+ * replay is disabled while enabled). */
+int fs_enable_stage_timing(FsSim *sim, int enable);
+/* Accumulated milliseconds per stage and the number of timed steps since the
+ * last reset; synchronises. */
+int fs_stage_times(FsSim *sim, double ms[FS_STAGE_COUNT], uint32_t *steps,
+                   int reset);
+/* Neighbour statistics accumulated by the steps since the last reset (the
+ * FLOP model's inputs, measured from the data): out[0] candidate pair tests
+ * of the density pass (also the XSPH and force passes' candidates), out[1]
+ * density-pass pairs with r^2 < h^2 (self included), out[2] pairs with
+ * 1e-12 < r^2 < h^2 (XSPH/force hits), out[3] candidate tests summed over all
+ * PCISPH solve iterations, out[4] solve pairs with r^2 < h^2. Synchronises. */
+#define FS_STAT_COUNT 5
+int fs_neighbor_stats(FsSim *sim, uint64_t out[FS_STAT_COUNT], int reset);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* FLUIDSPH_H */

@@ -1,0 +1,192 @@
+"""ctypes wrapper of the CPU oracle (oracle/sph_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check in
+__graft_entry__.py and by bench.py's CPU-baseline and reference arms, as the
+checker or the timed CPU baseline — never by the product path.
+
+``build()`` compiles the FP32 restatement and its FP64 twin (one source,
+template on the arithmetic type) into ``oracle/liboracle.so`` with
+``-ffp-contract=off`` so results are identical on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "sph_oracle.cpp"
+LIB = HERE / "liboracle.so"
+
+CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+            "-shared"]
+
+
+def build(force: bool = False) -> Path:
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    cxx = shutil.which("g++") or "c++"
+    tmp = LIB.with_suffix(".so.tmp")
+    r = subprocess.run([cxx, *CXXFLAGS, "-o", str(tmp), str(SRC)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        vp, u32 = C.c_void_p, C.c_uint32
+        lib.or_create.restype = vp
+        lib.or_create.argtypes = [vp, u32, vp, vp, u32, vp, u32, C.c_int]
+        lib.or_destroy.argtypes = [vp]
+        lib.or_step.argtypes = [vp, u32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        lib.or_stage.argtypes = [vp, C.c_int, u32]
+        for name in ("or_set_params", "or_set_geometry", "or_set_mouse", "or_set_rigid",
+                     "or_get_accum", "or_get_grid"):
+            getattr(lib, name).argtypes = [vp, vp]
+        lib.or_set_gravity.argtypes = [vp, C.POINTER(C.c_float)]
+        lib.or_set_iterations.argtypes = [vp, u32]
+        lib.or_clear_accum.argtypes = [vp]
+        lib.or_get_particles.argtypes = [vp, vp, u32]
+        lib.or_get_sorted.argtypes = [vp, vp, u32]
+        lib.or_get_particles_f64.argtypes = [vp, vp, u32, C.c_int]
+        lib.or_get_cells.argtypes = [vp, vp, vp]
+        lib.or_get_index_maps.argtypes = [vp, vp, vp, u32]
+        lib.or_get_predicted.argtypes = [vp, C.c_int, vp, u32]
+        lib.or_set_threads.argtypes = [C.c_int]
+        lib.or_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def set_threads(n: int) -> int:
+    lib = load()
+    lib.or_set_threads(int(n))
+    return int(lib.or_max_threads())
+
+
+class OracleSim:
+    """The reference step on the CPU, precision 32 (FP32 restatement) or 64
+    (FP64 twin). Same method names as fluidsph.sim.SphSimulation3DGrid."""
+
+    def __init__(self, particles: np.ndarray, sph_params, container_geom, max_particles: int = 0,
+                 sdf: np.ndarray | None = None, precision: int = 32):
+        self._lib = load()
+        parts = np.ascontiguousarray(particles, np.float32)
+        self._n = len(parts)
+        sdf_ptr, res = None, 0
+        if sdf is not None:
+            sdf = np.ascontiguousarray(sdf, np.float32)
+            res = int(round(sdf.size ** (1 / 3)))
+            sdf_ptr = sdf.ctypes.data
+        self._h = self._lib.or_create(parts.ctypes.data if self._n else None, self._n,
+                                      C.addressof(sph_params), C.addressof(container_geom),
+                                      int(max_particles), sdf_ptr, res, int(precision))
+        self.precision = precision
+        self.last_candidates = 0
+        self.last_hits = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.or_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, nsteps: int = 1):
+        cand, hits = C.c_uint64(), C.c_uint64()
+        self._lib.or_step(self._h, int(nsteps), C.byref(cand), C.byref(hits))
+        self.last_candidates, self.last_hits = cand.value, hits.value
+
+    def stage(self, stage: int, arg: int = 0):
+        self._lib.or_stage(self._h, int(stage), int(arg))
+
+    def update_sph_params(self, p):
+        self._lib.or_set_params(self._h, C.addressof(p))
+
+    def update_container_geometry(self, g):
+        self._lib.or_set_geometry(self._h, C.addressof(g))
+
+    def update_gravity(self, g):
+        arr = (C.c_float * 3)(*g.direction)
+        self._lib.or_set_gravity(self._h, arr)
+
+    def update_mouse_force(self, m):
+        self._lib.or_set_mouse(self._h, C.addressof(m))
+
+    def update_rigid_body(self, b):
+        self._lib.or_set_rigid(self._h, C.addressof(b))
+
+    def set_pcisph_iterations(self, k: int):
+        self._lib.or_set_iterations(self._h, int(k))
+
+    def clear_rigid_body_accum(self):
+        self._lib.or_clear_accum(self._h)
+
+    def read_rigid_body_accum(self) -> tuple:
+        out = (C.c_int32 * 8)()
+        self._lib.or_get_accum(self._h, out)
+        return tuple(out[:7])
+
+    def particles(self) -> np.ndarray:
+        out = np.empty((self._n, 16), np.float32)
+        self._lib.or_get_particles(self._h, out.ctypes.data, self._n)
+        return out
+
+    def sorted_particles(self) -> np.ndarray:
+        out = np.empty((self._n, 16), np.float32)
+        self._lib.or_get_sorted(self._h, out.ctypes.data, self._n)
+        return out
+
+    def particles_f64(self, sorted_: bool = False) -> np.ndarray:
+        out = np.empty((self._n, 14), np.float64)
+        self._lib.or_get_particles_f64(self._h, out.ctypes.data, self._n, 1 if sorted_ else 0)
+        return out
+
+    def grid(self):
+        from_buf = (C.c_uint32 * 12)()
+        self._lib.or_get_grid(self._h, from_buf)
+        return list(from_buf)
+
+    def cells(self) -> tuple[np.ndarray, np.ndarray]:
+        g = self.grid()[3]
+        counts = np.empty(g, np.uint32)
+        starts = np.empty(g, np.uint32)
+        self._lib.or_get_cells(self._h, counts.ctypes.data, starts.ctypes.data)
+        return counts, starts
+
+    def index_maps(self) -> tuple[np.ndarray, np.ndarray]:
+        ci = np.empty(self._n, np.uint32)
+        so = np.empty(self._n, np.uint32)
+        self._lib.or_get_index_maps(self._h, ci.ctypes.data, so.ctypes.data, self._n)
+        return ci, so
+
+    def predicted(self, which: int) -> np.ndarray:
+        out = np.empty((self._n, 8), np.float32)
+        self._lib.or_get_predicted(self._h, int(which), out.ctypes.data, self._n)
+        return out
+
+
+def oracle_for_scene(scene, precision: int = 32) -> OracleSim:
+    """An oracle simulation configured like a fluidsph.scenes.Scene."""
+    o = OracleSim(scene.particles, scene.sph, scene.geom, precision=precision)
+    o.update_gravity(scene.gravity)
+    o.set_pcisph_iterations(scene.iterations)
+    if scene.rigid is not None:
+        o.update_rigid_body(scene.rigid)
+    return o

@@ -1,0 +1,195 @@
+"""GPU parity: the sm_103a step through the C ABI against the FP32 oracle on
+the same seeded inputs. The library keeps the shaders' evaluation order with
+no fused multiply-add, so the bar is bit-exact for every buffer: cell ids,
+counts, inclusive starts, both index maps, sorted density / near density /
+normals, canonical positions, velocities and forces, and the fixed-point
+rigid-body accumulator."""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import assert_same_floats, check_grid_invariants, gpu_sim_for_scene, rel_err_stats
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(sim, orc, n, what=""):
+    counts_g, starts_g = sim.cells()
+    counts_o, starts_o = orc.cells()
+    np.testing.assert_array_equal(counts_g, counts_o, err_msg=f"{what} cell_counts")
+    np.testing.assert_array_equal(starts_g, starts_o, err_msg=f"{what} cell_starts")
+    ci_g, so_g = sim.index_maps()
+    ci_o, so_o = orc.index_maps()
+    np.testing.assert_array_equal(ci_g, ci_o, err_msg=f"{what} particle_cell_indices")
+    np.testing.assert_array_equal(so_g, so_o, err_msg=f"{what} sorted_to_orig")
+    check_grid_invariants(counts_g, starts_g, ci_g, so_g, n)
+    sg, so = sim.sorted_particles(), orc.sorted_particles()
+    assert_same_floats(sg[:, 11], so[:, 11], f"{what} sorted density")
+    assert_same_floats(sg[:, 12], so[:, 12], f"{what} sorted near_density")
+    assert_same_floats(sg[:, 13:16], so[:, 13:16], f"{what} sorted normal")
+    assert_same_floats(sg[:, 0:3], so[:, 0:3], f"{what} sorted position")
+    assert_same_floats(sg[:, 4:7], so[:, 4:7], f"{what} sorted velocity")
+    pg, po = sim.particles(), orc.particles()
+    assert_same_floats(pg[:, 0:3], po[:, 0:3], f"{what} position")
+    assert_same_floats(pg[:, 4:7], po[:, 4:7], f"{what} velocity")
+    assert_same_floats(pg[:, 8:11], po[:, 8:11], f"{what} force (dv)")
+
+
+def _run_pair(scene, steps, oracle_mod, sdf=None, mouse=None):
+    sim = gpu_sim_for_scene(scene, sdf=sdf)
+    orc = oracle_mod.OracleSim(scene.particles, scene.sph, scene.geom, sdf=sdf)
+    orc.update_gravity(scene.gravity)
+    orc.set_pcisph_iterations(scene.iterations)
+    if scene.rigid is not None:
+        orc.update_rigid_body(scene.rigid)
+    if mouse is not None:
+        sim.update_mouse_force(mouse)
+        orc.update_mouse_force(mouse)
+    sim.clear_rigid_body_accum()
+    orc.clear_rigid_body_accum()
+    for _ in range(steps):
+        sim.step(1)
+        orc.step(1)
+    return sim, orc
+
+
+@pytest.fixture(scope="module")
+def sc():
+    from fluidsph import scenes
+    return scenes
+
+
+def test_small_scene_one_step(fslib, oracle_mod, sc):
+    scene = sc.small_scene()
+    sim, orc = _run_pair(scene, 1, oracle_mod)
+    _compare(sim, orc, scene.n, "small")
+
+
+def test_config0_one_step_then_twenty(fslib, oracle_mod, sc):
+    scene = sc.config0()
+    sim, orc = _run_pair(scene, 1, oracle_mod)
+    _compare(sim, orc, scene.n, "config0 step 1")
+    for _ in range(19):
+        sim.step(1)
+        orc.step(1)
+    _compare(sim, orc, scene.n, "config0 step 20")
+
+
+def test_graph_replay_matches_single_steps(fslib, sc):
+    scene = sc.small_scene(seed=3)
+    a = gpu_sim_for_scene(scene)
+    b = gpu_sim_for_scene(scene)
+    a.step(6)
+    for _ in range(6):
+        b.step(1)
+    assert_same_floats(a.particles(), b.particles(), "graph vs launches")
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4])
+def test_rigid_body_shapes(fslib, oracle_mod, sc, shape):
+    from fluidsph import params as P
+    scene = sc.small_scene(nx=14, ny=10, nz=10, box=(0.6, 0.5, 0.4), seed=11)
+    scene.rigid = P.rigid_body(position=(0.0, 0.12, 0.0), half_extent=0.1, active=True,
+                               stiffness=250.0, shape=shape, velocity=(0.1, -0.2, 0.05),
+                               orientation=(0.1, 0.2, 0.3, 0.927))
+    sdf = None
+    if shape == 4:
+        # a sphere-like SDF on a 16^3 texture, in units of half_extent
+        r = 16
+        c = (np.arange(r) + 0.5) / r * 2 - 1
+        z, y, x = np.meshgrid(c, c, c, indexing="ij")
+        sdf = (np.sqrt(x * x + y * y + z * z) - 0.8).astype(np.float32)
+    sim, orc = _run_pair(scene, 2, oracle_mod, sdf=sdf)
+    _compare(sim, orc, scene.n, f"shape {shape}")
+    acc_g = sim.read_rigid_body_accum().as_tuple()
+    acc_o = orc.read_rigid_body_accum()
+    assert acc_g == tuple(acc_o)
+    assert acc_g[3] > 0, "expected contacts with the body"
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+def test_mouse_force_modes(fslib, oracle_mod, sc, mode):
+    from fluidsph import params as P
+    scene = sc.small_scene(seed=5)
+    m = P.mouse_force(position=(0.0, 0.1, 0.0), radius=0.3, strength=40.0, active=True,
+                      mode=mode, direction=(0.3, -0.2, -1.0))
+    sim, orc = _run_pair(scene, 2, oracle_mod, mouse=m)
+    _compare(sim, orc, scene.n, f"mouse mode {mode}")
+
+
+def test_tilted_container_and_iterations(fslib, oracle_mod, sc):
+    from fluidsph import params as P
+    for k, tilt in ((1, 0.2), (2, -0.25), (5, 0.1)):
+        scene = sc.small_scene(seed=9)
+        scene.geom = P.container_geometry(0.6, 0.4, 0.0, 0.5, tilt, -tilt / 2, 250.0, 0.55)
+        scene.iterations = k
+        sim, orc = _run_pair(scene, 3, oracle_mod)
+        _compare(sim, orc, scene.n, f"tilt {tilt} K={k}")
+
+
+def test_xsph_off_and_outside_particles(fslib, oracle_mod, sc):
+    scene = sc.small_scene(seed=2)
+    scene.sph.xsph_epsilon = 0.0
+    # particles beyond the +-2 grid: clamped in hashing, unclamped in lookups
+    scene.particles[:4, 0:3] = [[2.5, 0.1, 0.0], [-3.0, 0.2, 0.1], [0.0, 4.0, 0.0],
+                                [0.1, 0.1, 2.3]]
+    sim, orc = _run_pair(scene, 2, oracle_mod)
+    _compare(sim, orc, scene.n, "xsph off / outside")
+
+
+def test_empty_and_spawn(fslib, oracle_mod, sc):
+    from fluidsph.sim import SphSimulation3DGrid
+    scene = sc.make_scene("empty", np.zeros((0, 16), np.float32), (1, 1, 1))
+    sim = SphSimulation3DGrid(scene.particles, scene.sph, scene.geom, max_particles=300)
+    sim.step(2)
+    assert sim.num_particles() == 0
+    # spawn clips at capacity (sph_3d_grid.rs:1534-1569)
+    assert sim.spawn_particles((0.0, 0.3, 0.0), 250, 0.05) == 250
+    assert sim.spawn_particles((0.0, 0.3, 0.0), 100, 0.05) == 50
+    assert sim.num_particles() == 300
+    p = sim.particles()
+    assert np.isfinite(p).all()
+    # the spawned block then steps like any other input
+    params = scene.sph
+    params.num_particles = 300
+    sim.update_sph_params(params)
+    orc = oracle_mod.OracleSim(p, params, scene.geom)
+    sim.step(1)
+    orc.step(1)
+    _compare(sim, orc, 300, "spawned")
+
+
+def test_config1_full_size_one_step(fslib, oracle_mod, sc):
+    """1,048,576 particles with the held sphere: every buffer bit-exact."""
+    scene = sc.config1()
+    sim, orc = _run_pair(scene, 1, oracle_mod)
+    _compare(sim, orc, scene.n, "config1")
+    assert sim.read_rigid_body_accum().as_tuple() == tuple(orc.read_rigid_body_accum())
+
+
+def test_fp64_error_report(fslib, oracle_mod, sc, capsys):
+    """GPU vs the FP64 twin after one step of config 0, per quantity (reported;
+    density gated at the 1e-5 tolerance)."""
+    scene = sc.config0()
+    sim = gpu_sim_for_scene(scene)
+    sim.step(1)
+    o64 = oracle_mod.oracle_for_scene(scene, precision=64)
+    o64.step(1)
+    ci_g, _ = sim.index_maps()
+    ci_o, _ = o64.index_maps()
+    sg = sim.sorted_particles()[ci_g]
+    s64 = o64.particles_f64(sorted_=True)[ci_o]
+    pg = sim.particles()
+    p64 = o64.particles_f64()
+    rep = {
+        "density": rel_err_stats(sg[:, 11], s64[:, 9]),
+        "near_density": rel_err_stats(sg[:, 12], s64[:, 10]),
+        "position": rel_err_stats(pg[:, 0:3], p64[:, 0:3]),
+        "velocity": rel_err_stats(pg[:, 4:7], p64[:, 3:6]),
+    }
+    with capsys.disabled():
+        print("\nFP64 relative error (GPU FP32 vs FP64 twin, config 0, 1 step):", rep)
+    assert rep["density"]["max"] < 1e-5
+    assert rep["near_density"]["max"] < 1e-5
+    assert rep["position"]["p99"] < 1e-4
