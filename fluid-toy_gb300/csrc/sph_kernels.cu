@@ -12,7 +12,8 @@
 // Numerics. This translation unit is compiled with -fmad=false and IEEE
 // division/sqrt, and every expression keeps the shaders' evaluation order, so
 // results are bit-identical to the FP32 restatement of the shaders. sin/cos
-// (the close-pair fallback direction) are evaluated in double and rounded.
+// (the close-pair fallback direction) use one fixed FP32 evaluation shared
+// with the restatement (see sin_d below).
 //
 // Neighbour walk. For a particle in unclamped cell (cx,cy,cz) the shaders
 // visit the valid cells of the 3x3x3 block in dz, dy, dx order and each cell
@@ -45,8 +46,48 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
 }
 __device__ __forceinline__ float clampf(float e, float lo, float hi) { return fminf(fmaxf(e, lo), hi); }
 __device__ __forceinline__ float signf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
-__device__ __forceinline__ float sin_d(float x) { return float(sin(double(x))); }
-__device__ __forceinline__ float cos_d(float x) { return float(cos(double(x))); }
+// sin/cos of the close-pair fallback direction (sph_force_3d_grid.wgsl:
+// 167-172), whose accuracy WGSL leaves to the implementation. One fixed FP32
+// evaluation: Cody-Waite reduction by pi/2 with a three-part constant (each
+// step one correctly rounded fma), then the Taylor polynomials of sin and cos
+// on [-pi/4, pi/4] in Horner form. Explicit __fmaf_rn calls are exact IEEE
+// operations, so the CPU restatement reproduces these bits. Arguments are
+// integer-valued slot differences times 1, 2 or 3.
+__device__ __forceinline__ float reduce_half_pi(float x, int &quadrant) {
+  const float k = rintf(x * 0.636619747f);
+  float r = __fmaf_rn(-k, 1.57079637f, x);
+  r = __fmaf_rn(-k, -4.37113883e-08f, r);
+  r = __fmaf_rn(-k, -1.71512451e-15f, r);
+  quadrant = int(k) & 3;
+  return r;
+}
+__device__ __forceinline__ float sin_poly(float r) {
+  const float r2 = r * r;
+  float p = __fmaf_rn(r2, 2.75573188e-06f, -1.98412701e-04f);
+  p = __fmaf_rn(r2, p, 8.33333377e-03f);
+  p = __fmaf_rn(r2, p, -0.166666672f);
+  return __fmaf_rn(r * r2, p, r);
+}
+__device__ __forceinline__ float cos_poly(float r) {
+  const float r2 = r * r;
+  float p = __fmaf_rn(r2, -2.755732e-07f, 2.48015876e-05f);
+  p = __fmaf_rn(r2, p, -1.38888892e-03f);
+  p = __fmaf_rn(r2, p, 4.16666679e-02f);
+  p = __fmaf_rn(r2, p, -0.5f);
+  return __fmaf_rn(r2, p, 1.0f);
+}
+__device__ __forceinline__ float sin_d(float x) {
+  int q;
+  const float r = reduce_half_pi(x, q);
+  const float s = sin_poly(r), c = cos_poly(r);
+  return q == 0 ? s : (q == 1 ? c : (q == 2 ? -s : -c));
+}
+__device__ __forceinline__ float cos_d(float x) {
+  int q;
+  const float r = reduce_half_pi(x, q);
+  const float s = sin_poly(r), c = cos_poly(r);
+  return q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
+}
 
 // container_common.wgsl:28-64
 __device__ __forceinline__ float3 world_to_local(const GpuContainerGeometry &c, float3 p) {

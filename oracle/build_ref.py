@@ -1,0 +1,89 @@
+"""Build oracle/_ref/libref.so: the reference's own step shaders, translated
+mechanically to C++ (oracle/wgsl2cpp.py) from the WGSL files in the reference
+tree, driven by ref_driver.cpp with the dispatch sequence of
+SphSimulation3DGrid::step() (src/simulation/sph_3d_grid.rs:1261-1444).
+
+TEST INFRASTRUCTURE ONLY. The reference tree is read where it lies; outputs go
+only to oracle/_ref/ (git-ignored). When the reference sources are absent (the
+GPU machine) but a translation made earlier is present in oracle/_ref/, only
+the C++ compile step runs.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+REF_SHADERS = Path(os.environ.get("FLUID_TOY_REFERENCE", "/root/reference")) / "src" / "shaders"
+
+# (namespace, shader file, prepend container_common.wgsl) — the prepend list
+# follows sph_3d_grid.rs:169-193
+SHADERS = [
+    ("grid_clear", "grid_clear.wgsl", False),
+    ("grid_build", "grid_build.wgsl", False),
+    ("prefix_scan", "prefix_scan.wgsl", False),
+    ("grid_reorder", "grid_reorder.wgsl", False),
+    ("sph_density", "sph_density_3d_grid.wgsl", True),
+    ("xsph", "xsph.wgsl", False),
+    ("sph_force", "sph_force_3d_grid.wgsl", False),
+    ("pcisph_predict", "pcisph_predict.wgsl", False),
+    ("pcisph_solve", "pcisph_solve.wgsl", False),
+    ("pcisph_finalize", "pcisph_finalize.wgsl", False),
+    ("sph_integrate", "sph_integrate_3d.wgsl", True),
+]
+
+CXXFLAGS = ["-std=c++20", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing",
+            "-fPIC", "-shared", "-pthread", "-w"]
+
+
+def translate_all() -> bool:
+    if not REF_SHADERS.exists():
+        return False
+    sys.path.insert(0, str(HERE))
+    from wgsl2cpp import translate
+    common = (REF_SHADERS / "container_common.wgsl").read_text()
+    parts = ["// generated by oracle/wgsl2cpp.py from the reference's WGSL; do not edit",
+             "#pragma once", '#include "../ref_runtime.hpp"']
+    for ns, fname, prepend in SHADERS:
+        src = (REF_SHADERS / fname).read_text()
+        if prepend:
+            src = common + "\n" + src
+        parts.append(f"// ---- {fname}")
+        parts.append(translate(src, ns))
+    OUT.mkdir(exist_ok=True)
+    text = "\n\n".join(parts) + "\n"
+    dst = OUT / "ref_shaders.hpp"
+    if not dst.exists() or dst.read_text() != text:
+        dst.write_text(text)
+    return True
+
+
+def build(quiet: bool = False, force: bool = False) -> Path | None:
+    translated = translate_all()
+    hdr = OUT / "ref_shaders.hpp"
+    if not hdr.exists():
+        if not quiet:
+            print("reference shaders not available; oracle/_ref not built", file=sys.stderr)
+        return None
+    lib = OUT / "libref.so"
+    deps = [hdr, HERE / "ref_driver.cpp", HERE / "ref_runtime.hpp"]
+    if lib.exists() and not force and all(lib.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return lib
+    cxx = shutil.which("g++") or "c++"
+    tmp = lib.with_suffix(".so.tmp")
+    r = subprocess.run([cxx, *CXXFLAGS, "-I", str(OUT), "-o", str(tmp), str(HERE / "ref_driver.cpp")],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference translation failed to compile:\n{r.stderr[-4000:]}")
+    os.replace(tmp, lib)
+    if not quiet:
+        print(f"built {lib} ({'translated now' if translated else 'from an earlier translation'})")
+    return lib
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv)

@@ -39,13 +39,39 @@ def build(force: bool = False) -> Path:
 
 
 _lib = None
+_ref_lib = None
+REF_LIB = HERE / "_ref" / "libref.so"
+
+
+def load_ref():
+    """The reference's own step shaders translated to C++ (oracle/_ref), or
+    None when they are not built (the reference sources are needed once)."""
+    global _ref_lib
+    if _ref_lib is None:
+        try:
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("build_ref", HERE / "build_ref.py")
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build(quiet=True)
+        except Exception:
+            pass
+        if not REF_LIB.exists():
+            return None
+        _ref_lib = _bind(C.CDLL(str(REF_LIB)))
+    return _ref_lib
 
 
 def load():
     global _lib
     if _lib is None:
         build()
-        lib = C.CDLL(str(LIB))
+        _lib = _bind(C.CDLL(str(LIB)))
+    return _lib
+
+
+def _bind(lib):
+    if True:
         vp, u32 = C.c_void_p, C.c_uint32
         lib.or_create.restype = vp
         lib.or_create.argtypes = [vp, u32, vp, vp, u32, vp, u32, C.c_int]
@@ -64,10 +90,20 @@ def load():
         lib.or_get_cells.argtypes = [vp, vp, vp]
         lib.or_get_index_maps.argtypes = [vp, vp, vp, u32]
         lib.or_get_predicted.argtypes = [vp, C.c_int, vp, u32]
+        lib.or_sincos_f32.argtypes = [vp, vp, vp, u32]
         lib.or_set_threads.argtypes = [C.c_int]
         lib.or_max_threads.restype = C.c_int
-        _lib = lib
-    return _lib
+    return lib
+
+
+def sincos_f32(x: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """The FP32 sin/cos the restatement (and the GPU) use for the close-pair
+    direction."""
+    x = np.ascontiguousarray(x, np.float32)
+    s = np.empty_like(x)
+    c = np.empty_like(x)
+    load().or_sincos_f32(x.ctypes.data, s.ctypes.data, c.ctypes.data, x.size)
+    return s, c
 
 
 def set_threads(n: int) -> int:
@@ -81,8 +117,8 @@ class OracleSim:
     (FP64 twin). Same method names as fluidsph.sim.SphSimulation3DGrid."""
 
     def __init__(self, particles: np.ndarray, sph_params, container_geom, max_particles: int = 0,
-                 sdf: np.ndarray | None = None, precision: int = 32):
-        self._lib = load()
+                 sdf: np.ndarray | None = None, precision: int = 32, lib=None):
+        self._lib = lib if lib is not None else load()
         parts = np.ascontiguousarray(particles, np.float32)
         self._n = len(parts)
         sdf_ptr, res = None, 0
@@ -182,9 +218,10 @@ class OracleSim:
         return out
 
 
-def oracle_for_scene(scene, precision: int = 32) -> OracleSim:
-    """An oracle simulation configured like a fluidsph.scenes.Scene."""
-    o = OracleSim(scene.particles, scene.sph, scene.geom, precision=precision)
+def oracle_for_scene(scene, precision: int = 32, lib=None, sdf=None) -> OracleSim:
+    """An oracle simulation configured like a fluidsph.scenes.Scene (pass
+    lib=load_ref() for the translated reference shaders)."""
+    o = OracleSim(scene.particles, scene.sph, scene.geom, precision=precision, lib=lib, sdf=sdf)
     o.update_gravity(scene.gravity)
     o.set_pcisph_iterations(scene.iterations)
     if scene.rigid is not None:

@@ -116,10 +116,52 @@ template <class R> inline R fmax_(R a, R b) { return std::fmax(a, b); }
 template <class R> inline R fmin_(R a, R b) { return std::fmin(a, b); }
 template <class R> inline R clamp_(R e, R lo, R hi) { return fmin_(fmax_(e, lo), hi); }
 template <class R> inline R sign_(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
-// sin/cos: evaluated in double and rounded, so the FP32 result does not
-// depend on which libm (or GPU) evaluates it.
-template <class R> inline R sin_(R x) { return R(std::sin(double(x))); }
-template <class R> inline R cos_(R x) { return R(std::cos(double(x))); }
+// sin/cos of the close-pair fallback direction (sph_force_3d_grid.wgsl:
+// 167-172). WGSL leaves their accuracy to the implementation; the FP32
+// restatement fixes one deterministic evaluation so that CPU and GPU agree
+// bit for bit: Cody-Waite reduction by pi/2 (three-part constant, each step
+// one correctly rounded fma), then the Taylor polynomials of sin and cos on
+// [-pi/4, pi/4] in Horner form. The arguments are integer-valued
+// (slot differences times 1, 2, 3). The FP64 twin uses libm.
+inline float reduce_half_pi(float x, int *quadrant) {
+  const float k = std::rint(x * 0.636619747f);
+  float r = std::fma(-k, 1.57079637f, x);
+  r = std::fma(-k, -4.37113883e-08f, r);
+  r = std::fma(-k, -1.71512451e-15f, r);
+  *quadrant = int(k) & 3;
+  return r;
+}
+inline float sin_poly(float r) {
+  const float r2 = r * r;
+  float p = std::fma(r2, 2.75573188e-06f, -1.98412701e-04f);
+  p = std::fma(r2, p, 8.33333377e-03f);
+  p = std::fma(r2, p, -0.166666672f);
+  return std::fma(r * r2, p, r);
+}
+inline float cos_poly(float r) {
+  const float r2 = r * r;
+  float p = std::fma(r2, -2.755732e-07f, 2.48015876e-05f);
+  p = std::fma(r2, p, -1.38888892e-03f);
+  p = std::fma(r2, p, 4.16666679e-02f);
+  p = std::fma(r2, p, -0.5f);
+  return std::fma(r2, p, 1.0f);
+}
+inline float sin_f32(float x) {
+  int q;
+  const float r = reduce_half_pi(x, &q);
+  const float s = sin_poly(r), c = cos_poly(r);
+  return q == 0 ? s : (q == 1 ? c : (q == 2 ? -s : -c));
+}
+inline float cos_f32(float x) {
+  int q;
+  const float r = reduce_half_pi(x, &q);
+  const float s = sin_poly(r), c = cos_poly(r);
+  return q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
+}
+inline float sin_(float x) { return sin_f32(x); }
+inline float cos_(float x) { return cos_f32(x); }
+inline double sin_(double x) { return std::sin(x); }
+inline double cos_(double x) { return std::cos(x); }
 
 // WGSL f32 -> i32 conversion: truncate toward zero, saturate, NaN -> 0.
 inline int32_t f2i_sat(double x) {
@@ -993,6 +1035,14 @@ void or_get_predicted(void *hv, int which, float *out, uint32_t n) {
     }
   });
 }
+// The FP32 sin/cos of the close-pair direction, for accuracy tests.
+void or_sincos_f32(const float *x, float *s, float *c, uint32_t n) {
+  for (uint32_t i = 0; i < n; i++) {
+    s[i] = sin_f32(x[i]);
+    c[i] = cos_f32(x[i]);
+  }
+}
+
 void or_get_grid(void *hv, void *out) {
   auto *h = (Handle *)hv;
   DISPATCH(h, std::memcpy(out, &o->grid, sizeof(GridF)));

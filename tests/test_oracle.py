@@ -160,3 +160,20 @@ def test_scene_generators_deterministic(scenes_mod):
     # SplitMix64 reference values (seed 0)
     z = scenes_mod.splitmix64(0, 2)
     assert int(z[0]) == 0xE220A8397B1DCDAF and int(z[1]) == 0x6E789E6AA1B965F4
+
+
+def test_fp32_sincos_accuracy(oracle_mod):
+    """The fixed FP32 sin/cos of the close-pair direction against libm double
+    on the integer arguments it receives (slot differences times 1..3): about
+    one ulp up to 2^20, and under 3e-7 absolute up to 3 * 2^21."""
+    rng = np.random.default_rng(0)
+    near = np.concatenate([np.arange(-4096, 4097), rng.integers(-2**20, 2**20, 200000)])
+    far = rng.integers(-3 * 2**21, 3 * 2**21, 200000)
+    for x, tol in ((near, 8e-8), (far, 3e-7)):
+        x = x.astype(np.float32)
+        s, c = oracle_mod.sincos_f32(x)
+        xd = x.astype(np.float64)
+        assert np.abs(s - np.sin(xd)).max() < tol
+        assert np.abs(c - np.cos(xd)).max() < tol
+    s, c = oracle_mod.sincos_f32(np.zeros(1, np.float32))
+    assert s[0] == 0.0 and c[0] == 1.0
