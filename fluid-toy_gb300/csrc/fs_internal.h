@@ -71,6 +71,12 @@ struct DevState {
   unsigned long long *tile_status;  // decoupled-lookback descriptors
   uint32_t *tile_ticket;
   float *sdf;
+  uint32_t *mask_words;            // per-particle hit bitmasks (see sph_kernels.cu)
+  uint32_t *mask_off;              // word offset of each sorted slot's mask
+  unsigned long long *mask_alloc;  // bump allocator of mask words
+  unsigned long long mask_cap;     // mask capacity in words
+  float4 *dir_tab;  // close-pair fallback directions for slot differences
+  int dir_half;     // table covers d in [-dir_half, dir_half]
   GpuRigidBodyAccum *accum;
   uint32_t *err;
   unsigned long long *stats;
@@ -90,6 +96,7 @@ cudaError_t launch_hash(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st);
 cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_dir_table(const DevState &d, cudaStream_t st);
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st);

@@ -133,6 +133,14 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.tile_status = c.take<unsigned long long>(tiles + 1);
   d.tile_ticket = reinterpret_cast<uint32_t *>(d.tile_status ? d.tile_status + tiles : nullptr);
   d.sdf = c.take<float>(size_t(s->sdf_res) * s->sdf_res * s->sdf_res);
+  // hit masks: one bit per candidate; 128 words (4096 candidates) per
+  // particle of capacity, at least 2^22 words; overflow falls back to testing
+  d.mask_cap = std::max<size_t>(size_t(1) << 22, 128 * M);
+  d.mask_words = c.take<uint32_t>(d.mask_cap);
+  d.mask_off = c.take<uint32_t>(M);
+  d.mask_alloc = c.take<unsigned long long>(1);
+  d.dir_half = int(std::min<size_t>(M, size_t(1) << 20));
+  d.dir_tab = c.take<float4>(2 * size_t(d.dir_half) + 1);
   d.accum = c.take<GpuRigidBodyAccum>(1);
   d.err = c.take<uint32_t>(4);
   d.stats = c.take<unsigned long long>(STAT_COUNT);
@@ -351,6 +359,8 @@ int fs_create(const SphParticle3D *particles, uint32_t num_particles, const GpuS
                       cudaMemcpyHostToDevice, s->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "upload SDF"));
   if ((rc = upload_uniforms(s))) return bail(rc);
+  e = launch_dir_table(s->d, s->stream);
+  if (e != cudaSuccess) return bail(cuda_fail(e, "close-pair direction table"));
   if ((rc = write_particles(s, particles, 0, num_particles))) return bail(rc);
   e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "fs_create"));

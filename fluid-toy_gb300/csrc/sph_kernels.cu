@@ -110,6 +110,7 @@ __device__ __forceinline__ float3 local_dir_to_world(const GpuContainerGeometry 
 struct Runs {
   uint32_t lo[9], hi[9];
   int count;
+  uint32_t total;  // candidates over all runs
 };
 __device__ __forceinline__ void neighbor_runs(float3 pos, const GpuGridParams &g,
                                               const uint32_t *__restrict__ begin, Runs &R) {
@@ -120,6 +121,7 @@ __device__ __forceinline__ void neighbor_runs(float3 pos, const GpuGridParams &g
   const long long x0 = cx - 1 < 0 ? 0 : cx - 1;
   const long long x1 = cx + 1 > gx - 1 ? gx - 1 : cx + 1;
   R.count = 0;
+  R.total = 0;
   if (x0 > x1) return;
 #pragma unroll
   for (int dz = -1; dz <= 1; dz++) {
@@ -130,6 +132,7 @@ __device__ __forceinline__ void neighbor_runs(float3 pos, const GpuGridParams &g
       const uint32_t row = uint32_t(y) * g.grid_size_x + uint32_t(z) * g.grid_size_x * g.grid_size_y;
       R.lo[R.count] = __ldg(begin + row + uint32_t(x0));
       R.hi[R.count] = __ldg(begin + row + uint32_t(x1) + 1u);
+      R.total += R.hi[R.count] - R.lo[R.count];
       R.count++;
     }
   }
@@ -139,6 +142,90 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Visit the neighbours j with test(j) true in the shaders' order (rows in
+// dz, dy order, slots ascending inside a row), calling body(j) right after
+// its test. Used for cheap bodies and as the fallback of the mask walks.
+template <class Test, class Body>
+__device__ __forceinline__ void for_each_hit(const Runs &R, Test &&test, Body &&body) {
+  for (int r = 0; r < R.count; r++) {
+#pragma unroll 4
+    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++)
+      if (test(j)) body(j);
+  }
+}
+
+// ---- hit masks ----------------------------------------------------------------
+// The heavy per-hit bodies (force, XSPH, PCISPH pressure) run over a per-
+// particle bitmask of in-range neighbours: bit o is candidate o of the
+// particle's nine runs concatenated in visiting order. Walking the mask gives
+// every lane its own hits, one per loop iteration, in the shaders' order, so a
+// warp runs as long as its busiest lane (not as long as the union of its
+// lanes' candidate positions), and no candidate is tested twice.
+constexpr uint32_t MASK_NONE = 0xffffffffu;
+
+// Word offset of each particle's mask, allocated per warp from a bump counter.
+// Particles that do not fit the capacity get MASK_NONE and use the tested
+// (unmasked) path.
+__device__ __forceinline__ uint32_t alloc_mask(bool active, uint32_t nwords,
+                                               unsigned long long *__restrict__ alloc,
+                                               unsigned long long capacity) {
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t incl = active ? nwords : 0u;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (int(lane) >= o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned long long base = 0;
+  if (lane == 31u && total) base = atomicAdd(alloc, (unsigned long long)total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  const unsigned long long off = base + incl - (active ? nwords : 0u);
+  if (!active || off + nwords > capacity || off >= MASK_NONE) return MASK_NONE;
+  return uint32_t(off);
+}
+
+// Walk a particle's mask: one hit per iteration, empty words skipped inside
+// the iteration, so lanes progress independently.
+template <class Body>
+__device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, Body &&body) {
+  const uint32_t nwords = (R.total + 31u) >> 5;
+  if (nwords == 0u) return;
+  // `nxt` holds word w+1, loaded one word ahead to hide its latency
+  uint32_t w = 0u, cur = words[0], nxt = nwords > 1u ? words[1] : 0u;
+  int row = 0;
+  uint32_t row_start = 0u, row_end = R.hi[0] - R.lo[0];
+  while (true) {
+    while (cur == 0u && ++w < nwords) {
+      cur = nxt;
+      nxt = w + 1u < nwords ? words[w + 1u] : 0u;
+    }
+    if (cur == 0u) break;
+    const uint32_t o = (w << 5) + uint32_t(__ffs(cur) - 1);
+    cur &= cur - 1u;
+    while (o >= row_end) {
+      row++;
+      row_start = row_end;
+      row_end += R.hi[row] - R.lo[row];
+    }
+    body(R.lo[row] + (o - row_start));
+  }
+}
+
+// Close-pair fallback direction normalize(sin(d), cos(2d), sin(3d)) for the
+// slot difference d = s - j (sph_force_3d_grid.wgsl:163-172). It depends on d
+// only, so it is tabulated once per simulation for |d| <= dir_half (same
+// function, same bits) and evaluated directly beyond that.
+__device__ __forceinline__ float3 fallback_dir_eval(float idx_diff) {
+  return normalize3(f3(sin_d(idx_diff * 1.0f), cos_d(idx_diff * 2.0f), sin_d(idx_diff * 3.0f)));
+}
+__global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int dir_half) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t > 2 * dir_half) return;
+  const float3 d = fallback_dir_eval(float(t - dir_half));
+  tab[t] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
 // ---- density ----------------------------------------------------------------
@@ -161,27 +248,40 @@ __device__ __forceinline__ float boundary_gamma(const GpuContainerGeometry &c, f
   return fmaxf(gamma, 0.1f);
 }
 
-__global__ void __launch_bounds__(128) k_density(const DevUniforms *__restrict__ U,
-                                                 const float4 *__restrict__ s_pos,
-                                                 const uint32_t *__restrict__ begin,
-                                                 float2 *__restrict__ s_dens,
-                                                 float4 *__restrict__ s_nrm,
-                                                 unsigned long long *__restrict__ stats) {
+// sph_density_3d_grid.wgsl:111-194 (writes the sorted copy only). Besides the
+// density it records each particle's hit mask (1e-12 < r^2 < h^2, the XSPH and
+// force criterion) for the later passes.
+__global__ void __launch_bounds__(128)
+    k_density(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+              const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
+              float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
+              uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
+              unsigned long long *__restrict__ mask_alloc, unsigned long long mask_cap) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = s < U->n;
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
   const float scale_n = 15.0f / (PI_F * P.kernel_radius_pow6);
   const float m_over_rho0 = mass / P.rest_density;
-  unsigned long long cand = 0, hits = 0, nonself = 0;
-  if (s < U->n) {
-    const float3 pos_i = xyz(s_pos[s]);
+  unsigned long long hits = 0, nonself = 0;
+  float3 pos_i = f3(0.f, 0.f, 0.f);
+  Runs R;
+  R.count = 0;
+  R.total = 0;
+  if (active) {
+    pos_i = xyz(s_pos[s]);
+    neighbor_runs(pos_i, U->grid, begin, R);
+  }
+  const uint32_t off = alloc_mask(active, (R.total + 31u) >> 5, mask_alloc, mask_cap);
+  if (active) {
+    mask_off[s] = off;
+    uint32_t *words = mask_words + (off == MASK_NONE ? 0u : off);
     float density = 0.0f, near_density = 0.0f;
     float3 normal = f3(0.f, 0.f, 0.f);
-    Runs R;
-    neighbor_runs(pos_i, U->grid, begin, R);
+    uint32_t word = 0u, bit = 0u, widx = 0u;
     for (int r = 0; r < R.count; r++) {
-      cand += R.hi[r] - R.lo[r];
+#pragma unroll 4
       for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
         const float4 pj = __ldg(s_pos + j);
         const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
@@ -195,13 +295,21 @@ __global__ void __launch_bounds__(128) k_density(const DevUniforms *__restrict__
           near_density += mass * (scale_n * dn * dn * dn);
           if (r_sq > 1e-12f) {
             nonself++;
+            word |= 1u << bit;
             normal.x = normal.x + m_over_rho0 * rx * diff * diff;
             normal.y = normal.y + m_over_rho0 * ry * diff * diff;
             normal.z = normal.z + m_over_rho0 * rz * diff * diff;
           }
         }
+        if (++bit == 32u) {
+          if (off != MASK_NONE) words[widx] = word;
+          widx++;
+          word = 0u;
+          bit = 0u;
+        }
       }
     }
+    if (bit && off != MASK_NONE) words[widx] = word;
     const float gamma = boundary_gamma(U->geom, h, pos_i);
     density = density / gamma;
     const float h8 = P.kernel_radius_pow6 * h * h;
@@ -210,7 +318,7 @@ __global__ void __launch_bounds__(128) k_density(const DevUniforms *__restrict__
     s_dens[s] = make_float2(density, near_density);
     s_nrm[s] = make_float4(normal.x, normal.y, normal.z, 0.0f);
   }
-  cand = warp_sum_u64(cand);
+  const unsigned long long cand = warp_sum_u64(R.total);
   hits = warp_sum_u64(hits);
   nonself = warp_sum_u64(nonself);
   if ((threadIdx.x & 31) == 0 && cand) {
@@ -221,52 +329,67 @@ __global__ void __launch_bounds__(128) k_density(const DevUniforms *__restrict__
 }
 
 // ---- XSPH -------------------------------------------------------------------
+// xsph.wgsl:81-138; the result is the post-XSPH velocity in sorted order (the
+// reference scatters it to the canonical array).
 __global__ void __launch_bounds__(128) k_xsph(const DevUniforms *__restrict__ U,
                                               const float4 *__restrict__ s_pos,
                                               const float4 *__restrict__ s_vel,
                                               const float2 *__restrict__ s_dens,
                                               const uint32_t *__restrict__ begin,
+                                              const uint32_t *__restrict__ mask_words,
+                                              const uint32_t *__restrict__ mask_off,
                                               float4 *__restrict__ vel_x) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= U->n) return;
   const GpuSphParams3D &P = U->sph;
   const float4 vi4 = s_vel[s];
-  const float3 vel_i = xyz(vi4);
   const float eps = P.xsph_epsilon;
-  if (eps <= 0.0f) {  // xsph.wgsl:94-97: canonical velocity stays pre-XSPH
+  if (eps <= 0.0f) {  // xsph.wgsl:94-97: the velocity stays pre-XSPH
     vel_x[s] = vi4;
     return;
   }
+  const float3 vel_i = xyz(vi4);
   const float h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
   const float3 pos_i = xyz(s_pos[s]);
-  float3 corr = f3(0.f, 0.f, 0.f);
   Runs R;
   neighbor_runs(pos_i, U->grid, begin, R);
-  for (int r = 0; r < R.count; r++) {
-    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
-      const float4 pj = __ldg(s_pos + j);
-      const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
-      const float r_sq = rx * rx + ry * ry + rz * rz;
-      if (r_sq < h2 && r_sq > 1e-12f) {
-        const float density_j = fmaxf(__ldg(&s_dens[j].x), 1.0f);
-        const float3 vel_j = xyz(__ldg(s_vel + j));
-        const float diff = h2 - r_sq;
-        const float w = scale_d * diff * diff * diff;
-        corr = corr + (mass / density_j) * (vel_j - vel_i) * w;
-      }
-    }
+  float3 corr = f3(0.f, 0.f, 0.f);
+  auto body = [&](uint32_t j, float r_sq) {
+    const float density_j = fmaxf(__ldg(&s_dens[j].x), 1.0f);
+    const float3 vel_j = xyz(__ldg(s_vel + j));
+    const float diff = h2 - r_sq;
+    const float w = scale_d * diff * diff * diff;
+    corr = corr + (mass / density_j) * (vel_j - vel_i) * w;
+  };
+  auto dist2 = [&](uint32_t j) {
+    const float4 pj = __ldg(s_pos + j);
+    const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+    return rx * rx + ry * ry + rz * rz;
+  };
+  const uint32_t off = mask_off[s];
+  if (off != MASK_NONE) {
+    walk_mask(R, mask_words + off, [&](uint32_t j) { body(j, dist2(j)); });
+  } else {
+    float r_sq = 0.f;
+    for_each_hit(
+        R, [&](uint32_t j) { r_sq = dist2(j); return r_sq < h2 && r_sq > 1e-12f; },
+        [&](uint32_t j) { body(j, r_sq); });
   }
   const float3 v = vel_i + eps * corr;
   vel_x[s] = make_float4(v.x, v.y, v.z, vi4.w);
 }
 
 // ---- force + PCISPH predict ---------------------------------------------------
-__global__ void __launch_bounds__(128)
+// sph_force_3d_grid.wgsl:105-227, then pcisph_predict.wgsl:61-72 for the same
+// particle (sorted order).
+__global__ void __launch_bounds__(128, 4)
     k_force_predict(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
                     const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
                     const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
-                    const uint32_t *__restrict__ begin, float4 *__restrict__ anp,
+                    const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
+                    int dir_half, const uint32_t *__restrict__ mask_words,
+                    const uint32_t *__restrict__ mask_off, float4 *__restrict__ anp,
                     float4 *__restrict__ pred_xp, float *__restrict__ pred_rho) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= U->n) return;
@@ -275,6 +398,7 @@ __global__ void __launch_bounds__(128)
   const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
   const float scale_c = 32.0f / (PI_F * P.kernel_radius_pow9);
   const float near_k = P.near_stiffness, visc = P.viscosity, rho0 = P.rest_density;
+  const float min_dist = h * 0.1f;
   const float3 pos_i = xyz(s_pos[s]);
   const float3 vel_i = xyz(vel_x[s]);
   const float2 di = s_dens[s];
@@ -282,65 +406,72 @@ __global__ void __launch_bounds__(128)
   const float near_density_i = fmaxf(di.y, 1.0f);
   const float3 n_i = xyz(s_nrm[s]);
   const float near_pressure_i = near_k * near_density_i;
-  const float min_dist = h * 0.1f;
   float3 a_p = f3(0.f, 0.f, 0.f), a_v = f3(0.f, 0.f, 0.f), a_c = f3(0.f, 0.f, 0.f);
   Runs R;
   neighbor_runs(pos_i, U->grid, begin, R);
-  for (int r = 0; r < R.count; r++) {
-    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
-      const float3 pos_j = xyz(__ldg(s_pos + j));
-      const float3 r_vec = pos_i - pos_j;
-      const float r_sq = dot3(r_vec, r_vec);
-      if (r_sq < h2 && r_sq > 1e-12f) {
-        const float rr = sqrtf(r_sq);
-        float3 dir;
-        if (rr < min_dist) {
-          const float idx_diff = float(s) - float(j);
-          dir = normalize3(f3(sin_d(idx_diff * 1.0f), cos_d(idx_diff * 2.0f), sin_d(idx_diff * 3.0f)));
-        } else {
-          dir = normalize3(pos_j - pos_i);
-        }
-        const float2 dj = __ldg(s_dens + j);
-        const float density_j = fmaxf(dj.x, 1.0f);
-        const float near_density_j = fmaxf(dj.y, 1.0f);
-        const float near_pressure_j = near_k * near_density_j;
-        const float dg = h - rr;
-        const float grad = scale_g * dg * dg;
-        a_p = a_p + (-mass * (near_pressure_i + near_pressure_j) /
-                     (2.0f * density_i * near_density_j)) * dir * grad;
-        if (rr < min_dist) {
-          const float sep = 200.0f * (1.0f - rr / min_dist);
-          a_p = a_p + (-sep) * dir;
-        }
-        const float3 vel_j = xyz(__ldg(s_vel + j));
-        const float3 v_ij = vel_i - vel_j;
-        const float3 x_ij = pos_i - pos_j;
-        const float v_dot_x = dot3(v_ij, x_ij);
-        if (v_dot_x < 0.0f) {
-          const float mu = h * v_dot_x / (r_sq + 0.01f * h2);
-          const float avg_density = (density_i + density_j) * 0.5f;
-          const float pi_visc = -visc * mu / avg_density;
-          a_v = a_v + (-mass * pi_visc * grad) * dir;
-        }
-        const float K_ij = 2.0f * rho0 / (density_i + density_j);
-        const float r3 = rr * rr * rr;
-        float coh;
-        if (rr >= h * 0.5f) {
-          coh = scale_c * dg * dg * dg * r3;
-        } else {
-          coh = scale_c * (2.0f * dg * dg * dg * r3 - P.kernel_radius_pow6 / 64.0f);
-        }
-        a_c = a_c + (mass * K_ij * coh) * dir;
-        const float3 n_j = xyz(__ldg(s_nrm + j));
-        a_c = a_c - (mass * K_ij) * (n_i - n_j);
-      }
-    }
+  // Every arm of the shader's branches is evaluated and the accumulators are
+  // updated with selects (x = c ? x + t : x), which leaves their bits exactly
+  // as the branches would: lanes of a warp then never split inside the body.
+  auto body = [&](uint32_t j) {
+    const float3 pos_j = xyz(__ldg(s_pos + j));
+    const float2 dj = __ldg(s_dens + j);
+    const float3 vel_j = xyz(__ldg(s_vel + j));
+    const float3 n_j = xyz(__ldg(s_nrm + j));
+    const float3 r_vec = pos_i - pos_j;
+    const float r_sq = dot3(r_vec, r_vec);
+    const float rr = sqrtf(r_sq);
+    const bool close = rr < min_dist;
+    // normalize(pos_j - pos_i): its length is sqrt(dot(-r, -r)) == rr bit for
+    // bit, so dividing by rr is the same operation sequence
+    const float3 dir_far = (pos_j - pos_i) / rr;
+    const int d = int(s) - int(j);
+    const bool tabulated = d >= -dir_half && d <= dir_half;
+    float3 dir_close = tabulated ? xyz(__ldg(dir_tab + (tabulated ? d + dir_half : 0))) : dir_far;
+    if (close && !tabulated) dir_close = fallback_dir_eval(float(s) - float(j));
+    const float3 dir = close ? dir_close : dir_far;
+    const float density_j = fmaxf(dj.x, 1.0f);
+    const float near_density_j = fmaxf(dj.y, 1.0f);
+    const float near_pressure_j = near_k * near_density_j;
+    const float dg = h - rr;
+    const float grad = scale_g * dg * dg;
+    a_p = a_p + (-mass * (near_pressure_i + near_pressure_j) /
+                 (2.0f * density_i * near_density_j)) * dir * grad;
+    const float sep = 200.0f * (1.0f - rr / min_dist);
+    const float3 a_p_sep = a_p + (-sep) * dir;
+    a_p = close ? a_p_sep : a_p;
+    const float3 v_ij = vel_i - vel_j;
+    const float v_dot_x = dot3(v_ij, r_vec);
+    const float mu = h * v_dot_x / (r_sq + 0.01f * h2);
+    const float avg_density = (density_i + density_j) * 0.5f;
+    const float pi_visc = -visc * mu / avg_density;
+    const float3 a_v_new = a_v + (-mass * pi_visc * grad) * dir;
+    a_v = v_dot_x < 0.0f ? a_v_new : a_v;
+    const float K_ij = 2.0f * rho0 / (density_i + density_j);
+    const float r3 = rr * rr * rr;
+    const float coh_far = scale_c * dg * dg * dg * r3;
+    const float coh_near = scale_c * (2.0f * dg * dg * dg * r3 - P.kernel_radius_pow6 / 64.0f);
+    const float coh = rr >= h * 0.5f ? coh_far : coh_near;
+    a_c = a_c + (mass * K_ij * coh) * dir;
+    a_c = a_c - (mass * K_ij) * (n_i - n_j);
+  };
+  const uint32_t off = mask_off[s];
+  if (off != MASK_NONE) {
+    walk_mask(R, mask_words + off, body);
+  } else {
+    for_each_hit(
+        R,
+        [&](uint32_t j) {
+          const float4 pj = __ldg(s_pos + j);
+          const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+          const float r_sq = rx * rx + ry * ry + rz * rz;
+          return r_sq < h2 && r_sq > 1e-12f;
+        },
+        body);
   }
   a_c = a_c * P.surface_tension;
   const float3 a_g = xyz(U->gravity.direction);
   const float3 a = a_p + a_v + a_c + a_g;
   anp[s] = make_float4(a.x, a.y, a.z, 0.0f);
-  // pcisph_predict.wgsl:61-72 on the same particle
   const float dt = P.dt;
   const float3 v_star = vel_i + dt * a;
   const float3 x_star = pos_i + dt * v_star;
@@ -349,53 +480,77 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---- PCISPH solve -------------------------------------------------------------
-// One iteration in -> out. Iteration 0 reads the predict output, where every
-// pressure is 0: the pressure-acceleration sum is then +0 exactly, so it is
-// skipped (HAS_PRESSURE=false) with bit-identical results. The last
-// iteration only produces the corrected velocity (finalize's input).
+// One iteration in -> out (pcisph_solve.wgsl:99-208). The predicted density is
+// summed inline while the candidates are tested; with pressure, the hits with
+// r^2 > 1e-12 are recorded in the particle's mask (the density pass's word
+// range, same candidate list) and the pressure term is then summed by walking
+// it. Iteration 0 reads the predict output, where every pressure is 0: the
+// pressure sum is +0 exactly, so it is skipped (HAS_PRESSURE=false) with
+// bit-identical results. The last iteration only produces the corrected
+// velocity.
 template <bool HAS_PRESSURE, bool LAST>
 __global__ void __launch_bounds__(128)
     k_solve(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
-            const float *__restrict__ rho_in, float4 *__restrict__ xp_out,
+            const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
+            const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float4 *__restrict__ v_out,
             unsigned long long *__restrict__ stats) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = s < U->n;
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
   const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
-  unsigned long long cand = 0, hits = 0;
-  if (s < U->n) {
+  unsigned long long hits = 0;
+  Runs R;
+  R.count = 0;
+  R.total = 0;
+  if (active) {
     const float4 self_xp = xp_in[s];
     const float3 pred_pos = xyz(self_xp);
     const float old_p = self_xp.w;
     const float sd = fmaxf(rho_in[s], 1.0f);
-    const float4 pi4 = s_pos[s];
-    const float3 pos_i = xyz(pi4);
+    const float3 pos_i = xyz(s_pos[s]);  // current position decides the cells
+    neighbor_runs(pos_i, U->grid, begin, R);
     float pred_density = 0.0f;
     float3 a_p = f3(0.f, 0.f, 0.f);
-    Runs R;
-    neighbor_runs(pos_i, U->grid, begin, R);
+    const float self_term = old_p / (sd * sd);
+    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq, float np) {
+      const float rr = sqrtf(r_sq);
+      const float nd = fmaxf(__ldg(rho_in + j), 1.0f);
+      const float3 dir = (-r_vec) / rr;
+      const float dg = h - rr;
+      const float grad = scale_g * dg * dg;
+      a_p = a_p + (-mass * (self_term + np / (nd * nd)) * grad) * dir;
+    };
+    // candidates in chunks of up to 32: the predicted density is summed while
+    // testing; the pressure hits of the chunk go to a per-lane bitmask that
+    // each lane then walks (its own hits only, ascending)
     for (int r = 0; r < R.count; r++) {
-      cand += R.hi[r] - R.lo[r];
-      for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
-        const float4 nb = __ldg(xp_in + j);
-        const float3 r_vec = pred_pos - xyz(nb);
-        const float r_sq = dot3(r_vec, r_vec);
-        if (r_sq < h2) {
-          hits++;
-          const float diff = h2 - r_sq;
-          pred_density += mass * (scale_d * diff * diff * diff);
-          if (HAS_PRESSURE && r_sq > 1e-12f) {
-            const float rr = sqrtf(r_sq);
-            const float nd = fmaxf(__ldg(rho_in + j), 1.0f);
-            const float np = nb.w;
-            const float3 dir = (-r_vec) / rr;
-            const float dg = h - rr;
-            const float grad = scale_g * dg * dg;
-            a_p = a_p + (-mass * (old_p / (sd * sd) + np / (nd * nd)) * grad) * dir;
+      for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
+        const uint32_t cnt = min(32u, R.hi[r] - base);
+        uint32_t chunk = 0u;
+#pragma unroll 4
+        for (uint32_t k = 0; k < cnt; k++) {
+          const float4 nb = __ldg(xp_in + base + k);
+          const float3 r_vec = pred_pos - xyz(nb);
+          const float r_sq = dot3(r_vec, r_vec);
+          if (r_sq < h2) {
+            hits++;
+            const float diff = h2 - r_sq;
+            pred_density += mass * (scale_d * diff * diff * diff);
+            if (HAS_PRESSURE && r_sq > 1e-12f) chunk |= 1u << k;
+          }
+        }
+        if (HAS_PRESSURE) {
+          while (chunk) {
+            const uint32_t j = base + uint32_t(__ffs(chunk) - 1);
+            chunk &= chunk - 1u;
+            const float4 nb = __ldg(xp_in + j);
+            const float3 r_vec = pred_pos - xyz(nb);
+            pressure(j, r_vec, dot3(r_vec, r_vec), nb.w);
           }
         }
       }
@@ -417,7 +572,7 @@ __global__ void __launch_bounds__(128)
       rho_out[s] = pred_density;
     }
   }
-  cand = warp_sum_u64(cand);
+  const unsigned long long cand = warp_sum_u64(R.total);
   hits = warp_sum_u64(hits);
   if ((threadIdx.x & 31) == 0 && cand) {
     atomicAdd(stats + STAT_CAND_SOLVE, cand);
@@ -669,25 +824,34 @@ inline unsigned blocks_for(uint32_t n, unsigned threads) {
 
 }  // namespace
 
+cudaError_t launch_dir_table(const DevState &d, cudaStream_t st) {
+  const int count = 2 * d.dir_half + 1;
+  k_dir_table<<<(count + 255) / 256, 256, 0, st>>>(d.dir_tab, d.dir_half);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d.mask_alloc, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
   k_density<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.cell_begin, d.s_dens, d.s_nrm,
-                                                d.stats);
+                                                d.stats, d.mask_words, d.mask_off, d.mask_alloc,
+                                                d.mask_cap);
   return cudaGetLastError();
 }
 
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_xsph<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.s_dens, d.cell_begin,
-                                             d.vel_x);
+                                             d.mask_words, d.mask_off, d.vel_x);
   return cudaGetLastError();
 }
 
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_force_predict<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.s_dens, d.s_nrm,
-                                                      d.vel_x, d.cell_begin, d.anp,
-                                                      d.pred_xp[0], d.pred_rho[0]);
+  k_force_predict<<<blocks_for(n, 128), 128, 0, st>>>(
+      d.u, d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x, d.cell_begin, d.dir_tab, d.dir_half,
+      d.mask_words, d.mask_off, d.anp, d.pred_xp[0], d.pred_rho[0]);
   return cudaGetLastError();
 }
 
@@ -695,22 +859,15 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   if (n == 0) return cudaSuccess;
   const int in = iter & 1, out = in ^ 1;
   const unsigned g = blocks_for(n, 128);
-  if (iter == 0 && last)
-    k_solve<false, true><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
-                                            d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
-                                            d.pred_rho[out], d.pred_v, d.stats);
-  else if (iter == 0)
-    k_solve<false, false><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
-                                             d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
-                                             d.pred_rho[out], d.pred_v, d.stats);
-  else if (last)
-    k_solve<true, true><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
-                                           d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
-                                           d.pred_rho[out], d.pred_v, d.stats);
-  else
-    k_solve<true, false><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,
-                                            d.pred_xp[in], d.pred_rho[in], d.pred_xp[out],
-                                            d.pred_rho[out], d.pred_v, d.stats);
+#define FS_SOLVE(P_, L_)                                                                     \
+  k_solve<P_, L_><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,            \
+                                     d.pred_xp[in], d.pred_rho[in], d.mask_words, d.mask_off, \
+                                     d.pred_xp[out], d.pred_rho[out], d.pred_v, d.stats)
+  if (iter == 0 && last) FS_SOLVE(false, true);
+  else if (iter == 0) FS_SOLVE(false, false);
+  else if (last) FS_SOLVE(true, true);
+  else FS_SOLVE(true, false);
+#undef FS_SOLVE
   return cudaGetLastError();
 }
 
