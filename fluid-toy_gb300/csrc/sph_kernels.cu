@@ -89,6 +89,25 @@ __device__ __forceinline__ float cos_d(float x) {
   return q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
 }
 
+// a / b correctly rounded, from y = RN(1/b): Markstein's correction
+// q = RN(q0 + y * RN(a - b * q0)) with q0 = RN(a * y) (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Dev. 34(1), 1990; exact when y is the correctly
+// rounded reciprocal and no intermediate under- or overflows). Operands are
+// restricted to |a|, |b| in [2^-60, 2^60] (quotient and residual stay normal)
+// or a == 0; anything else takes the IEEE division. Used where one
+// reciprocal serves several quotients, so results are bit-identical to a / b.
+__device__ __forceinline__ float div_by_rcp(float a, float b, float y) {
+  const float q0 = a * y;
+  const float q1 = __fmaf_rn(__fmaf_rn(-b, q0, a), y, q0);
+  const float aa = fabsf(a), ab = fabsf(b);
+  if (ab >= 0x1p-60f && ab <= 0x1p60f) {
+    if (aa >= 0x1p-60f && aa <= 0x1p60f) return q1;
+    if (aa == 0.0f) return q0;  // +-0 with the quotient's sign
+  }
+  return a / b;
+}
+
 // container_common.wgsl:28-64
 __device__ __forceinline__ float3 world_to_local(const GpuContainerGeometry &c, float3 p) {
   float3 q = f3(p.x, p.y - c.center_y, p.z);
@@ -399,6 +418,7 @@ __global__ void __launch_bounds__(128, 4)
   const float scale_c = 32.0f / (PI_F * P.kernel_radius_pow9);
   const float near_k = P.near_stiffness, visc = P.viscosity, rho0 = P.rest_density;
   const float min_dist = h * 0.1f;
+  const float y_min_dist = __frcp_rn(min_dist);
   const float3 pos_i = xyz(s_pos[s]);
   const float3 vel_i = xyz(vel_x[s]);
   const float2 di = s_dens[s];
@@ -423,7 +443,11 @@ __global__ void __launch_bounds__(128, 4)
     const bool close = rr < min_dist;
     // normalize(pos_j - pos_i): its length is sqrt(dot(-r, -r)) == rr bit for
     // bit, so dividing by rr is the same operation sequence
-    const float3 dir_far = (pos_j - pos_i) / rr;
+    // (pos_j - pos_i) / rr with one shared reciprocal, bit-identical
+    const float3 dv = pos_j - pos_i;
+    const float y_rr = __frcp_rn(rr);
+    const float3 dir_far = f3(div_by_rcp(dv.x, rr, y_rr), div_by_rcp(dv.y, rr, y_rr),
+                              div_by_rcp(dv.z, rr, y_rr));
     const int d = int(s) - int(j);
     const bool tabulated = d >= -dir_half && d <= dir_half;
     float3 dir_close = tabulated ? xyz(__ldg(dir_tab + (tabulated ? d + dir_half : 0))) : dir_far;
@@ -436,7 +460,7 @@ __global__ void __launch_bounds__(128, 4)
     const float grad = scale_g * dg * dg;
     a_p = a_p + (-mass * (near_pressure_i + near_pressure_j) /
                  (2.0f * density_i * near_density_j)) * dir * grad;
-    const float sep = 200.0f * (1.0f - rr / min_dist);
+    const float sep = 200.0f * (1.0f - div_by_rcp(rr, min_dist, y_min_dist));
     const float3 a_p_sep = a_p + (-sep) * dir;
     a_p = close ? a_p_sep : a_p;
     const float3 v_ij = vel_i - vel_j;
@@ -520,7 +544,10 @@ __global__ void __launch_bounds__(128)
     auto pressure = [&](uint32_t j, float3 r_vec, float r_sq, float np) {
       const float rr = sqrtf(r_sq);
       const float nd = fmaxf(__ldg(rho_in + j), 1.0f);
-      const float3 dir = (-r_vec) / rr;
+      const float y_rr = __frcp_rn(rr);
+      const float3 nr = -r_vec;
+      const float3 dir = f3(div_by_rcp(nr.x, rr, y_rr), div_by_rcp(nr.y, rr, y_rr),
+                            div_by_rcp(nr.z, rr, y_rr));
       const float dg = h - rr;
       const float grad = scale_g * dg * dg;
       a_p = a_p + (-mass * (self_term + np / (nd * nd)) * grad) * dir;
