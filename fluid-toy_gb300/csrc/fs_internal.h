@@ -83,6 +83,9 @@ struct DevState {
   DevUniforms *u;
 };
 
+// Set the thread-local text fs_last_error() returns (sim.cu).
+void set_last_error(const char *msg);
+
 // ---- kernel launchers (grid_kernels.cu / sph_kernels.cu) --------------------
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
@@ -94,6 +97,11 @@ inline uint32_t scan_tiles(uint32_t total_cells) {
 
 cudaError_t launch_hash(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st);
+// The scan kernel on caller-provided scratch: tile_status holds
+// scan_tiles(total_cells) descriptors followed by the ticket word, all zero.
+cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uint32_t total_cells,
+                                     unsigned long long *tile_status, uint32_t *err,
+                                     cudaStream_t st);
 cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_dir_table(const DevState &d, cudaStream_t st);

@@ -262,6 +262,16 @@ cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st
   return cudaGetLastError();
 }
 
+cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uint32_t total_cells,
+                                     unsigned long long *tile_status, uint32_t *err,
+                                     cudaStream_t st) {
+  if (total_cells == 0) return cudaSuccess;
+  const uint32_t tiles = scan_tiles(total_cells);
+  k_scan<<<tiles, SCAN_THREADS, 0, st>>>(counts, ends, total_cells, tile_status,
+                                         reinterpret_cast<uint32_t *>(tile_status + tiles), err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.cell_of, d.rank_of, d.cell_begin,

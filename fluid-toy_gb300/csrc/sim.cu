@@ -59,6 +59,8 @@ static_assert(offsetof(GpuRigidBody, rot_row0) == 48, "rigid offset");
 
 }  // namespace
 
+void fs::set_last_error(const char *msg) { g_last_error = msg; }
+
 struct FsSim {
   int device = 0;
   cudaStream_t own_stream = nullptr;

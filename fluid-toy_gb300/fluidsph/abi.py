@@ -148,7 +148,9 @@ SIGNATURES = {
     "fs_enable_stage_timing": (C.c_int, [_vp, C.c_int]),
     "fs_stage_times": (C.c_int, [_vp, _P(C.c_double), _P(_u32), C.c_int]),
     "fs_neighbor_stats": (C.c_int, [_vp, _P(C.c_uint64), C.c_int]),
+    "fs_prefix_scan_noalloc": (C.c_int, [_vp, _vp, _u32, _vp, _vp]),
 }
+FS_NOALLOC_SCAN_MAX_CELLS = 1 << 26
 
 _lib = None
 

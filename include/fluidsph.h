@@ -310,6 +310,29 @@ int fs_stage_times(FsSim *sim, double ms[FS_STAGE_COUNT], uint32_t *steps,
 #define FS_STAT_COUNT 5
 int fs_neighbor_stats(FsSim *sim, uint64_t out[FS_STAT_COUNT], int reset);
 
+/* ---- prefix scan without allocation -------------------------------------- */
+
+/* No counterpart in the reference. The inclusive prefix scan of a cell-count
+ * array (the reference's cell_starts, prefix_scan.wgsl) for callers that
+ * cannot allocate device memory: code inside a CUDA stream capture that must
+ * not add allocation nodes, real-time loops that forbid allocator calls and
+ * their implicit synchronisation after start-up, and hosts whose device
+ * memory is owned by another runtime. It allocates nothing: the scan's tile
+ * descriptors live in a fixed file-scope device array of 128 KiB that every
+ * GPU loading the library holds until the process exits. cell_counts and
+ * cell_starts are device arrays of total_cells entries, at most
+ * FS_NOALLOC_SCAN_MAX_CELLS (larger sizes return FS_E_CAPACITY).
+ * device_status, if not NULL, is a device word the kernel ORs 1 into if its
+ * bounded look-back wait ever gives up. Asynchronous on `stream` (a
+ * cudaStream_t, NULL = legacy default stream). All calls share the array:
+ * each clears it on its stream first, but calls that overlap on the GPU race.
+ * The first call on a device looks up the array's address (with that device
+ * current); make it before any stream capture. */
+#define FS_NOALLOC_SCAN_MAX_CELLS (1u << 26)
+int fs_prefix_scan_noalloc(const uint32_t *cell_counts, uint32_t *cell_starts,
+                           uint32_t total_cells, uint32_t *device_status,
+                           void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
