@@ -73,6 +73,12 @@ struct DevState {
   float *sdf;
   uint32_t *mask_words;            // per-particle hit bitmasks (see sph_kernels.cu)
   uint32_t *mask_off;              // word offset of each sorted slot's mask
+  uint32_t *mask_hits;             // set bits in each sorted slot's mask
+  uint32_t *warp_order;            // neighbour-pass task order (warp ids, heaviest first)
+  uint32_t *task_counters;         // one task counter per neighbour-pass launch
+  uint8_t *warp_bucket;            // work bucket of each warp of sorted slots
+  uint32_t *order_hist;            // bucket counts, then bucket cursors
+  int sm_count;                    // streaming multiprocessors of the device
   unsigned long long *mask_alloc;  // bump allocator of mask words
   unsigned long long mask_cap;     // mask capacity in words
   float4 *dir_tab;  // close-pair fallback directions for slot differences
@@ -106,6 +112,8 @@ cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_dir_table(const DevState &d, cudaStream_t st);
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st);
+constexpr int TASK_COUNTERS = 16;
+cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last,

@@ -140,6 +140,11 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.mask_cap = std::max<size_t>(size_t(1) << 22, 128 * M);
   d.mask_words = c.take<uint32_t>(d.mask_cap);
   d.mask_off = c.take<uint32_t>(M);
+  d.mask_hits = c.take<uint32_t>(M);
+  d.warp_order = c.take<uint32_t>((M + 31) / 32);
+  d.task_counters = c.take<uint32_t>(TASK_COUNTERS);
+  d.warp_bucket = c.take<uint8_t>((M + 31) / 32);
+  d.order_hist = c.take<uint32_t>(2 * 33);
   d.mask_alloc = c.take<unsigned long long>(1);
   d.dir_half = int(std::min<size_t>(M, size_t(1) << 20));
   d.dir_tab = c.take<float4>(2 * size_t(d.dir_half) + 1);
@@ -232,6 +237,7 @@ int enqueue_step(FsSim *s, bool timed) {
   FS_CUDA(launch_scatter(d, n, st), "reorder (scatter)");
   FS_CUDA(launch_sort_gather(d, n, st), "reorder (sort/gather)");
   if ((rc = mark(4))) return rc;
+  FS_CUDA(launch_order_warps(d, n, st), "neighbour-pass work order");
   FS_CUDA(launch_density(d, n, st), "density");
   if ((rc = mark(5))) return rc;
   FS_CUDA(launch_xsph(d, n, st), "xsph");
@@ -350,6 +356,12 @@ int fs_create(const SphParticle3D *particles, uint32_t num_particles, const GpuS
     if (e != cudaSuccess) return bail(cuda_fail(e, "create event"));
   }
   carve(s, nullptr, &s->arena_bytes);
+  {
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "query SM count"));
+    s->d.sm_count = sms;
+  }
   e = cudaMalloc(&s->arena, s->arena_bytes);
   if (e != cudaSuccess) return bail(cuda_fail(e, "allocate device arena"));
   carve(s, static_cast<char *>(s->arena), &s->arena_bytes);

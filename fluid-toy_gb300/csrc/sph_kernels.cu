@@ -270,13 +270,13 @@ __device__ __forceinline__ float boundary_gamma(const GpuContainerGeometry &c, f
 // sph_density_3d_grid.wgsl:111-194 (writes the sorted copy only). Besides the
 // density it records each particle's hit mask (1e-12 < r^2 < h^2, the XSPH and
 // force criterion) for the later passes.
-__global__ void __launch_bounds__(128)
-    k_density(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+__device__ __forceinline__ void density_one(
+    uint32_t s, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
               const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
               float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
               uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
-              unsigned long long *__restrict__ mask_alloc, unsigned long long mask_cap) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+              uint32_t *__restrict__ mask_hits, unsigned long long *__restrict__ mask_alloc,
+              unsigned long long mask_cap) {
   const bool active = s < U->n;
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
@@ -329,6 +329,7 @@ __global__ void __launch_bounds__(128)
       }
     }
     if (bit && off != MASK_NONE) words[widx] = word;
+    mask_hits[s] = uint32_t(nonself);
     const float gamma = boundary_gamma(U->geom, h, pos_i);
     density = density / gamma;
     const float h8 = P.kernel_radius_pow6 * h * h;
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(128)
 // ---- XSPH -------------------------------------------------------------------
 // xsph.wgsl:81-138; the result is the post-XSPH velocity in sorted order (the
 // reference scatters it to the canonical array).
-__global__ void __launch_bounds__(128) k_xsph(const DevUniforms *__restrict__ U,
+__device__ __forceinline__ void xsph_one(uint32_t s, const DevUniforms *__restrict__ U,
                                               const float4 *__restrict__ s_pos,
                                               const float4 *__restrict__ s_vel,
                                               const float2 *__restrict__ s_dens,
@@ -358,7 +359,6 @@ __global__ void __launch_bounds__(128) k_xsph(const DevUniforms *__restrict__ U,
                                               const uint32_t *__restrict__ mask_words,
                                               const uint32_t *__restrict__ mask_off,
                                               float4 *__restrict__ vel_x) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= U->n) return;
   const GpuSphParams3D &P = U->sph;
   const float4 vi4 = s_vel[s];
@@ -402,15 +402,14 @@ __global__ void __launch_bounds__(128) k_xsph(const DevUniforms *__restrict__ U,
 // ---- force + PCISPH predict ---------------------------------------------------
 // sph_force_3d_grid.wgsl:105-227, then pcisph_predict.wgsl:61-72 for the same
 // particle (sorted order).
-__global__ void __launch_bounds__(128, 4)
-    k_force_predict(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+__device__ __forceinline__ void force_predict_one(
+    uint32_t s, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
                     const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
                     const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
                     const uint32_t *__restrict__ mask_off, float4 *__restrict__ anp,
                     float4 *__restrict__ pred_xp, float *__restrict__ pred_rho) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= U->n) return;
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
@@ -513,15 +512,14 @@ __global__ void __launch_bounds__(128, 4)
 // bit-identical results. The last iteration only produces the corrected
 // velocity.
 template <bool HAS_PRESSURE, bool LAST>
-__global__ void __launch_bounds__(128)
-    k_solve(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+__device__ __forceinline__ void solve_one(
+    uint32_t s, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
             const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
             const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float4 *__restrict__ v_out,
             unsigned long long *__restrict__ stats) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = s < U->n;
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
@@ -605,6 +603,126 @@ __global__ void __launch_bounds__(128)
     atomicAdd(stats + STAT_CAND_SOLVE, cand);
     atomicAdd(stats + STAT_HIT_SOLVE, hits);
   }
+}
+
+// ---- work ordering -------------------------------------------------------------
+// The neighbour passes' cost per warp (32 consecutive sorted slots) ranges over
+// two orders of magnitude: the clumps carry most of the pairs. Launched in slot
+// order, the heaviest blocks form a tail. Instead, persistent warps pull
+// 32-slot tasks from a queue ordered heaviest first (longest-processing-time
+// scheduling); which warp computes a particle does not change its result.
+struct TaskQueue {
+  const uint32_t *order;  // task t -> warp index (32 slots)
+  uint32_t *counter;      // next task, zeroed before each launch
+  uint32_t nwarps;
+};
+
+template <class F>
+__device__ __forceinline__ void for_warp_tasks(const TaskQueue &q, F &&f) {
+  const unsigned lane = threadIdx.x & 31u;
+  while (true) {
+    uint32_t t = 0u;
+    if (lane == 0u) t = atomicAdd(q.counter, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= q.nwarps) break;
+    f(__ldg(q.order + t) * 32u + lane);
+  }
+}
+
+// Task order, heaviest first: k_warp_work puts every warp (32 sorted slots)
+// in a bucket floor(log2(max candidates of its particles)) + 1 and counts the
+// buckets; k_scatter_order writes the warps bucket by bucket, heaviest bucket
+// first (the order inside a bucket is immaterial).
+constexpr int ORDER_BUCKETS = 33;
+__global__ void __launch_bounds__(256)
+    k_warp_work(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+                const uint32_t *__restrict__ begin, uint8_t *__restrict__ warp_bucket,
+                uint32_t *__restrict__ hist) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t total = 0u;
+  if (s < U->n) {
+    Runs R;
+    neighbor_runs(xyz(s_pos[s]), U->grid, begin, R);
+    total = R.total;
+  }
+  const uint32_t m = __reduce_max_sync(0xffffffffu, total);
+  if ((threadIdx.x & 31u) == 0u && s < U->n) {
+    const uint32_t b = 32u - uint32_t(__clz(m));
+    warp_bucket[s >> 5] = uint8_t(b);
+    atomicAdd(&hist[b], 1u);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_scatter_order(const DevUniforms *__restrict__ U, const uint8_t *__restrict__ warp_bucket,
+                    const uint32_t *__restrict__ hist, uint32_t *__restrict__ cursor,
+                    uint32_t *__restrict__ order) {
+  __shared__ uint32_t base[ORDER_BUCKETS];
+  if (threadIdx.x == 0) {
+    uint32_t acc = 0u;
+    for (int b = ORDER_BUCKETS - 1; b >= 0; b--) {
+      base[b] = acc;
+      acc += hist[b];
+    }
+  }
+  __syncthreads();
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= (U->n + 31u) / 32u) return;
+  const uint32_t b = warp_bucket[w];
+  order[base[b] + atomicAdd(&cursor[b], 1u)] = w;
+}
+
+__global__ void __launch_bounds__(128)
+    k_density(TaskQueue q, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+              const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
+              float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
+              uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
+              uint32_t *__restrict__ mask_hits, unsigned long long *__restrict__ mask_alloc,
+              unsigned long long mask_cap) {
+  for_warp_tasks(q, [&](uint32_t s) {
+    density_one(s, U, s_pos, begin, s_dens, s_nrm, stats, mask_words, mask_off, mask_hits,
+                mask_alloc, mask_cap);
+  });
+}
+
+__global__ void __launch_bounds__(128)
+    k_xsph(TaskQueue q, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+           const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
+           const uint32_t *__restrict__ begin, const uint32_t *__restrict__ mask_words,
+           const uint32_t *__restrict__ mask_off, float4 *__restrict__ vel_x) {
+  for_warp_tasks(q, [&](uint32_t s) {
+    xsph_one(s, U, s_pos, s_vel, s_dens, begin, mask_words, mask_off, vel_x);
+  });
+}
+
+__global__ void __launch_bounds__(128, 4)
+    k_force_predict(TaskQueue q, const DevUniforms *__restrict__ U,
+                    const float4 *__restrict__ s_pos, const float4 *__restrict__ s_vel,
+                    const float2 *__restrict__ s_dens, const float4 *__restrict__ s_nrm,
+                    const float4 *__restrict__ vel_x, const uint32_t *__restrict__ begin,
+                    const float4 *__restrict__ dir_tab, int dir_half,
+                    const uint32_t *__restrict__ mask_words, const uint32_t *__restrict__ mask_off,
+                    float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
+                    float *__restrict__ pred_rho) {
+  for_warp_tasks(q, [&](uint32_t s) {
+    force_predict_one(s, U, s_pos, s_vel, s_dens, s_nrm, vel_x, begin, dir_tab, dir_half,
+                      mask_words, mask_off, anp, pred_xp, pred_rho);
+  });
+}
+
+template <bool HAS_PRESSURE, bool LAST>
+__global__ void __launch_bounds__(128)
+    k_solve(TaskQueue q, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+            const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
+            const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
+            const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
+            const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
+            float *__restrict__ rho_out, float4 *__restrict__ v_out,
+            unsigned long long *__restrict__ stats) {
+  for_warp_tasks(q, [&](uint32_t s) {
+    solve_one<HAS_PRESSURE, LAST>(s, U, s_pos, vel_x, anp, begin, xp_in, rho_in, mask_words,
+                                  mask_off, xp_out, rho_out, v_out, stats);
+  });
 }
 
 // ---- finalize + integrate ----------------------------------------------------
@@ -857,39 +975,93 @@ cudaError_t launch_dir_table(const DevState &d, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+namespace {
+// Persistent grid: as many resident blocks as the kernel's occupancy allows.
+template <class K>
+unsigned persistent_blocks(K kernel, int sm_count) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return unsigned(per_sm * sm_count);
+}
+
+cudaError_t prepare_queue(const DevState &d, uint32_t n, int slot, cudaStream_t st, TaskQueue *q) {
+  q->order = d.warp_order;
+  q->counter = d.task_counters + slot;
+  q->nwarps = (n + 31u) / 32u;
+  return cudaMemsetAsync(q->counter, 0, sizeof(uint32_t), st);
+}
+}  // namespace
+
+cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d.order_hist, 0, sizeof(uint32_t) * 2 * ORDER_BUCKETS, st);
+  if (e != cudaSuccess) return e;
+  k_warp_work<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.s_pos, d.cell_begin, d.warp_bucket,
+                                                  d.order_hist);
+  const uint32_t nwarps = (n + 31u) / 32u;
+  k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(d.u, d.warp_bucket, d.order_hist,
+                                                           d.order_hist + ORDER_BUCKETS,
+                                                           d.warp_order);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d.mask_alloc, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_density<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.cell_begin, d.s_dens, d.s_nrm,
-                                                d.stats, d.mask_words, d.mask_off, d.mask_alloc,
-                                                d.mask_cap);
+  TaskQueue q;
+  e = prepare_queue(d, n, TASK_COUNTERS - 1, st, &q);
+  if (e != cudaSuccess) return e;
+  static unsigned blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_density, d.sm_count);
+  k_density<<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.cell_begin, d.s_dens, d.s_nrm, d.stats,
+                                    d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc,
+                                    d.mask_cap);
   return cudaGetLastError();
 }
 
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_xsph<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.s_dens, d.cell_begin,
-                                             d.mask_words, d.mask_off, d.vel_x);
+  TaskQueue q;
+  cudaError_t e = prepare_queue(d, n, 0, st, &q);
+  if (e != cudaSuccess) return e;
+  static unsigned blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_xsph, d.sm_count);
+  k_xsph<<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.s_vel, d.s_dens, d.cell_begin, d.mask_words,
+                                 d.mask_off, d.vel_x);
   return cudaGetLastError();
 }
 
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_force_predict<<<blocks_for(n, 128), 128, 0, st>>>(
-      d.u, d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x, d.cell_begin, d.dir_tab, d.dir_half,
-      d.mask_words, d.mask_off, d.anp, d.pred_xp[0], d.pred_rho[0]);
+  TaskQueue q;
+  cudaError_t e = prepare_queue(d, n, 1, st, &q);
+  if (e != cudaSuccess) return e;
+  static unsigned blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count);
+  k_force_predict<<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x,
+                                          d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
+                                          d.mask_off, d.anp, d.pred_xp[0], d.pred_rho[0]);
   return cudaGetLastError();
 }
 
 cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int in = iter & 1, out = in ^ 1;
-  const unsigned g = blocks_for(n, 128);
-#define FS_SOLVE(P_, L_)                                                                     \
-  k_solve<P_, L_><<<g, 128, 0, st>>>(d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,            \
-                                     d.pred_xp[in], d.pred_rho[in], d.mask_words, d.mask_off, \
-                                     d.pred_xp[out], d.pred_rho[out], d.pred_v, d.stats)
+  TaskQueue q;
+  cudaError_t e = prepare_queue(d, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
+  if (e != cudaSuccess) return e;
+#define FS_SOLVE(P_, L_)                                                                      \
+  do {                                                                                        \
+    static unsigned blocks = 0;                                                               \
+    if (!blocks) blocks = persistent_blocks(k_solve<P_, L_>, d.sm_count);                    \
+    k_solve<P_, L_><<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,    \
+                                            d.pred_xp[in], d.pred_rho[in], d.mask_words,      \
+                                            d.mask_off, d.pred_xp[out], d.pred_rho[out],      \
+                                            d.pred_v, d.stats);                               \
+  } while (0)
   if (iter == 0 && last) FS_SOLVE(false, true);
   else if (iter == 0) FS_SOLVE(false, false);
   else if (last) FS_SOLVE(true, true);
