@@ -180,7 +180,7 @@ def measured_peaks() -> dict:
 
 def profile_traffic(kernel: str) -> float | None:
     """dram bytes per launch of `kernel` from the committed ncu summary."""
-    for f in (ROOT / "profiles").glob("*.md"):
+    for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
             if line.startswith(f"traffic_bytes_per_launch[{kernel}]"):
                 try:
