@@ -230,6 +230,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     stream = torch.cuda.Stream(device=dev)  # events and steps on one stream
     sim.set_stream(stream.cuda_stream)
     sim.step(W)
+    sim.prepare_steps(K)  # capture the step graphs outside the timed region
     sim.sync()
     state_after_warmup = sim.particles() if dist.rank == 0 and not args.no_cpu else None
     sim.neighbor_stats(reset=True)
@@ -366,6 +367,98 @@ def run_ours(args, dist: Dist) -> dict | None:
     return out
 
 
+def run_batch(args, dist: Dist) -> dict | None:
+    """The batched ensemble: all scenes in one launch per stage, K steps from
+    graphs, against looping the plain simulation over the same scenes (one
+    stream, each scene's steps graph-replayed)."""
+    import torch
+    from fluidsph import scenes as S
+    from fluidsph.sim import SphBatch3DGrid, SphSimulation3DGrid
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    scenes = S.config2()
+    counts = np.array([s.n for s in scenes])
+    total = int(counts.sum())
+    K, W = args.steps, args.warmup
+    stream = torch.cuda.Stream(device=dev)
+
+    b = SphBatch3DGrid([s.particles for s in scenes], [s.sph for s in scenes],
+                       [s.geom for s in scenes], device=dev)
+    for k, s in enumerate(scenes):
+        b.update_scene(k, gravity=s.gravity)
+    b.set_pcisph_iterations(scenes[0].iterations)
+    b.set_stream(stream.cuda_stream)
+    b.step(W)
+    t0 = time.perf_counter()
+    b.prepare_steps(K)
+    capture_s = time.perf_counter() - t0
+    b.sync()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(K)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    dist.barrier()
+    clk = clocks.stop()
+    secs = e0.elapsed_time(e1) / 1e3
+    value, secs_max = aggregate(total * K, secs, dist)
+    b.enable_stage_timing(True)
+    b.stage_times(reset=True)
+    b.step(min(K, 20))
+    stages, timed = b.stage_times(reset=True)
+    b.close()
+
+    # looped plain: the same scenes one after another on one stream, each for
+    # k_loop graph-replayed steps after W warm-up steps
+    k_loop = max(1, min(K, args.loop_steps))
+    sims = []
+    for s in scenes:
+        sim = SphSimulation3DGrid(s.particles, s.sph, s.geom, device=dev)
+        sim.update_gravity(s.gravity)
+        sim.set_pcisph_iterations(s.iterations)
+        sim.set_stream(stream.cuda_stream)
+        sim.step(W)
+        sim.prepare_steps(k_loop)
+        sims.append(sim)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for sim in sims:
+        sim.step(k_loop)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    loop_secs = e0.elapsed_time(e1) / 1e3
+    loop_value, _ = aggregate(total * k_loop, loop_secs, dist)
+    for sim in sims:
+        sim.close()
+    if dist.rank != 0:
+        return None
+    per_step_ms = {k: round(v / max(timed, 1), 4) for k, v in stages.items()}
+    return {
+        "metric": METRIC, "value": round(value, 1), "unit": METRIC, "n_gpus": dist.world,
+        "steps": K, "warmup": W, "ms_per_step": round(secs_max / K * 1e3, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded SplitMix64 scene draws and lattice jitter)",
+        "config": {"workload": f"batched_ensemble_{len(scenes)}_scenes", "scenes": len(scenes),
+                   "particles": total, "count_range": [int(counts.min()), int(counts.max())],
+                   "steps_timed": f"{W + 1}..{W + K}", "graph_capture_s": round(capture_s, 3),
+                   "l2": "state > 1 GB exceeds the 129 MB L2 (no flush)"},
+        "stages_ms_per_step": per_step_ms,
+        "looped_plain": {"value": round(loop_value, 1), "unit": METRIC, "steps": k_loop,
+                         "ms_per_step": round(loop_secs / k_loop * 1e3, 4),
+                         "pattern": "one SphSimulation3DGrid per scene on one stream, "
+                                    "each fs_step(k) graph-replayed, scene after scene"},
+        "batched_over_looped": round(value / loop_value, 3) if loop_value else None,
+        "gpu_launches": K * (8 + scenes[0].iterations),
+        "clocks": clk,
+    }
+
+
 def run_reference(args, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
@@ -404,6 +497,8 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--loop-steps", type=int, default=20,
+                    help="steps per scene of the looped-plain comparison (--config 2)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps")
@@ -417,7 +512,7 @@ def main():
             if dist.local_rank == 0:
                 build_library()
             dist.barrier()
-            out = run_ours(args, dist)
+            out = run_batch(args, dist) if args.config == 2 else run_ours(args, dist)
         if out is not None:
             print(json.dumps(out), flush=True)
     finally:

@@ -14,6 +14,7 @@ namespace fs {
 // orders them before later steps exactly like the reference's
 // queue.write_buffer uploads (sph_3d_grid.rs:1446-1473), and lets captured
 // step graphs stay valid across parameter changes.
+// One block per scene: a simulation holds one scene, a batch many.
 struct DevUniforms {
   GpuSphParams3D sph;
   GpuGridParams grid;
@@ -21,9 +22,28 @@ struct DevUniforms {
   GpuGravity gravity;
   GpuMouseForce mouse;
   GpuRigidBody rigid;
-  uint32_t n;        // effective particle count for every stage
-  uint32_t sdf_res;  // SDF texture edge length (1 = the reference's dummy)
-  uint32_t pad[2];
+  uint32_t n;         // effective particle count of the scene for every stage
+  uint32_t sdf_res;   // SDF texture edge length (1 = the reference's dummy)
+  uint32_t p_offset;  // first canonical particle of the scene
+  uint32_t c_offset;  // first cell of the scene in the global cell arrays
+  uint32_t s_offset;  // first sorted slot of the scene
+  uint32_t pad[3];
+};
+
+// Counts over all scenes of a simulation (device copy).
+struct DevBatch {
+  uint32_t n_scenes;
+  uint32_t n_canon;      // canonical particles in the buffer
+  uint32_t n_sorted;     // hashed particles (sum of the scenes' effective counts)
+  uint32_t cells_total;  // sum of the scenes' cell counts
+};
+
+// What a kernel needs to find the scene of a particle or sorted slot.
+struct SceneView {
+  const DevUniforms *u;         // [n_scenes]
+  const DevBatch *b;
+  const uint16_t *scene_of;     // canonical particle -> scene
+  const uint16_t *scene_of_slot;  // sorted slot -> scene
 };
 
 // Neighbour-statistics counters written by the density and solve kernels.
@@ -83,10 +103,14 @@ struct DevState {
   unsigned long long mask_cap;     // mask capacity in words
   float4 *dir_tab;  // close-pair fallback directions for slot differences
   int dir_half;     // table covers d in [-dir_half, dir_half]
-  GpuRigidBodyAccum *accum;
+  GpuRigidBodyAccum *accum;  // [n_scenes]
   uint32_t *err;
   unsigned long long *stats;
-  DevUniforms *u;
+  DevUniforms *u;           // [n_scenes]
+  DevBatch *b;
+  uint16_t *scene_of;       // canonical particle -> scene
+  uint16_t *scene_of_slot;  // sorted slot -> scene
+  SceneView view() const { return SceneView{u, b, scene_of, scene_of_slot}; }
 };
 
 // Set the thread-local text fs_last_error() returns (sim.cu).
@@ -101,15 +125,16 @@ inline uint32_t scan_tiles(uint32_t total_cells) {
   return (total_cells + SCAN_TILE - 1) / SCAN_TILE;
 }
 
-cudaError_t launch_hash(const DevState &d, uint32_t n, cudaStream_t st);
+// n_canon: canonical particles of all scenes; n_sorted: hashed particles.
+cudaError_t launch_hash(const DevState &d, uint32_t n_canon, cudaStream_t st);
 cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st);
 // The scan kernel on caller-provided scratch: tile_status holds
 // scan_tiles(total_cells) descriptors followed by the ticket word, all zero.
 cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uint32_t total_cells,
                                      unsigned long long *tile_status, uint32_t *err,
                                      cudaStream_t st);
-cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st);
-cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_scatter(const DevState &d, uint32_t n_canon, cudaStream_t st);
+cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_t st);
 cudaError_t launch_dir_table(const DevState &d, cudaStream_t st);
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st);
 constexpr int TASK_COUNTERS = 16;

@@ -39,16 +39,20 @@ __device__ __forceinline__ uint32_t hash_cell(float4 p, const GpuGridParams &g) 
 // Hash + count with warp-aggregated atomics: lanes holding the same cell
 // (found with __match_any_sync) elect one leader that adds the group's size;
 // every lane keeps its arrival rank (leader's old count + rank among peers).
-__global__ void __launch_bounds__(256) k_hash(const float4 *__restrict__ pos,
-                                              const DevUniforms *__restrict__ U,
+// Each scene owns a block of the global cell arrays (c_offset), so one pass
+// hashes every scene; particles beyond a scene's effective count stay out.
+__global__ void __launch_bounds__(256) k_hash(const float4 *__restrict__ pos, SceneView v,
                                               uint32_t *__restrict__ cell_of,
                                               uint32_t *__restrict__ rank_of,
                                               uint32_t *__restrict__ counts) {
-  const uint32_t n = U->n;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = i < n;
+  bool active = i < v.b->n_canon;
   uint32_t cell = 0;
-  if (active) cell = hash_cell(pos[i], U->grid);
+  if (active) {
+    const DevUniforms *U = v.u + v.scene_of[i];
+    active = i - U->p_offset < U->n;
+    if (active) cell = U->c_offset + hash_cell(pos[i], U->grid);
+  }
   const unsigned act = __ballot_sync(0xffffffffu, active);
   if (!active) return;
   const unsigned lane = threadIdx.x & 31u;
@@ -201,30 +205,32 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 #undef PAD
 }
 
-// Scatter every particle to its unsorted slot: begin[cell] + arrival rank.
-__global__ void __launch_bounds__(256) k_scatter(const DevUniforms *__restrict__ U,
-                                                 const uint32_t *__restrict__ cell_of,
+// Scatter every hashed particle to its unsorted slot: begin[cell] + arrival rank.
+__global__ void __launch_bounds__(256) k_scatter(SceneView v, const uint32_t *__restrict__ cell_of,
                                                  const uint32_t *__restrict__ rank_of,
                                                  const uint32_t *__restrict__ begin,
                                                  uint32_t *__restrict__ t_tmp) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= U->n) return;
+  if (i >= v.b->n_canon) return;
+  const DevUniforms *U = v.u + v.scene_of[i];
+  if (i - U->p_offset >= U->n) return;
   t_tmp[begin[cell_of[i]] + rank_of[i]] = i;
 }
 
 // Stable counting sort, second half: slot s of the unsorted order holds
 // particle v; its final slot is begin[cell] + #{particles of the cell with a
 // smaller index}. The record is gathered into grid order (grid_reorder.wgsl:
-// 54-62) and both index maps are written.
+// 54-62) and both index maps and the slot's scene are written.
 __global__ void __launch_bounds__(256)
-    k_sort_gather(const DevUniforms *__restrict__ U, const uint32_t *__restrict__ t_tmp,
+    k_sort_gather(SceneView sv, const uint32_t *__restrict__ t_tmp,
                   const uint32_t *__restrict__ cell_of, const uint32_t *__restrict__ begin,
                   const float4 *__restrict__ p_pos, const float4 *__restrict__ p_vel,
                   const float4 *__restrict__ p_force, float4 *__restrict__ s_pos,
                   float4 *__restrict__ s_vel, float4 *__restrict__ s_frc,
-                  uint32_t *__restrict__ s2o, uint32_t *__restrict__ cidx) {
+                  uint32_t *__restrict__ s2o, uint32_t *__restrict__ cidx,
+                  uint16_t *__restrict__ scene_of_slot) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= U->n) return;
+  if (s >= sv.b->n_sorted) return;
   const uint32_t v = t_tmp[s];
   const uint32_t c = cell_of[v];
   const uint32_t b = begin[c], e = begin[c + 1];
@@ -233,6 +239,7 @@ __global__ void __launch_bounds__(256)
   const uint32_t d = b + rank;
   s2o[d] = v;
   cidx[v] = d;
+  scene_of_slot[d] = sv.scene_of[v];
   s_pos[d] = p_pos[v];
   s_vel[d] = p_vel[v];
   s_frc[d] = p_force[v];
@@ -245,9 +252,10 @@ inline unsigned blocks_for(uint32_t n, unsigned threads) {
 }  // namespace
 
 // counts must be zeroed by the caller (the grid_clear stage).
-cudaError_t launch_hash(const DevState &d, uint32_t n, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_hash<<<blocks_for(n, 256), 256, 0, st>>>(d.p_pos, d.u, d.cell_of, d.rank_of, d.counts);
+cudaError_t launch_hash(const DevState &d, uint32_t n_canon, cudaStream_t st) {
+  if (n_canon == 0) return cudaSuccess;
+  k_hash<<<blocks_for(n_canon, 256), 256, 0, st>>>(d.p_pos, d.view(), d.cell_of, d.rank_of,
+                                                   d.counts);
   return cudaGetLastError();
 }
 
@@ -272,18 +280,18 @@ cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uin
   return cudaGetLastError();
 }
 
-cudaError_t launch_scatter(const DevState &d, uint32_t n, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.cell_of, d.rank_of, d.cell_begin,
-                                                d.t_tmp);
+cudaError_t launch_scatter(const DevState &d, uint32_t n_canon, cudaStream_t st) {
+  if (n_canon == 0) return cudaSuccess;
+  k_scatter<<<blocks_for(n_canon, 256), 256, 0, st>>>(d.view(), d.cell_of, d.rank_of,
+                                                      d.cell_begin, d.t_tmp);
   return cudaGetLastError();
 }
 
-cudaError_t launch_sort_gather(const DevState &d, uint32_t n, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_sort_gather<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.t_tmp, d.cell_of, d.cell_begin,
-                                                    d.p_pos, d.p_vel, d.p_force, d.s_pos,
-                                                    d.s_vel, d.s_frc, d.s2o, d.cidx);
+cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_t st) {
+  if (n_sorted == 0) return cudaSuccess;
+  k_sort_gather<<<blocks_for(n_sorted, 256), 256, 0, st>>>(
+      d.view(), d.t_tmp, d.cell_of, d.cell_begin, d.p_pos, d.p_vel, d.p_force, d.s_pos, d.s_vel,
+      d.s_frc, d.s2o, d.cidx, d.scene_of_slot);
   return cudaGetLastError();
 }
 

@@ -5,6 +5,13 @@
 // (:1261-1444), parameter uploads (:1446-1477), rigid-body accumulator
 // clear/readback (:1479-1498), buffer getters (:1500-1530) and spawning
 // (:1534-1569). All device memory lives in one arena allocated at creation.
+//
+// A simulation holds one or more scenes. fs_create makes one; fs_batch_create
+// makes many independent scenes stepped together, every stage one launch over
+// all of them. Scene k owns canonical particles [p_offset, p_offset + n_k),
+// cells [c_offset, c_offset + G_k) of the global cell arrays and sorted slots
+// [s_offset, s_offset + active_k), so the global prefix scan over all cells is
+// every scene's own scan shifted by s_offset.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -56,35 +63,49 @@ static_assert(offsetof(SphParticle3D, density) == 44, "density offset");
 static_assert(offsetof(SphParticle3D, normal) == 52, "normal offset");
 static_assert(offsetof(GpuContainerGeometry, wall_stiffness) == 112, "geometry offset");
 static_assert(offsetof(GpuRigidBody, rot_row0) == 48, "rigid offset");
+static_assert(sizeof(FsSceneInfo) == 80, "FsSceneInfo layout");
+static_assert(FS_BATCH_MAX_SCENES <= 65535u, "scene ids are 16-bit");
 
 }  // namespace
 
 void fs::set_last_error(const char *msg) { g_last_error = msg; }
 
+// Step graphs: one captured graph per step count, a few kept.
+constexpr uint32_t kMaxGraphSteps = 256;
+constexpr int kGraphSlots = 4;
+
+struct StepGraph {
+  cudaGraphExec_t exec = nullptr;
+  uint32_t steps = 0, n_canon = 0, n_sorted = 0, iters = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t last_use = 0;
+};
+
 struct FsSim {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
-  uint32_t n = 0;      // particles in the canonical buffer (num_particles())
-  uint32_t max_n = 0;  // capacity
+  bool batch = false;       // made by fs_batch_create
+  uint32_t max_n = 0;       // canonical capacity
   uint32_t iterations = 5;  // sph_3d_grid.rs:1253 default
   uint32_t sdf_res = 1;
-  GpuGridParams grid{};
-  DevUniforms host_u{};  // host mirror of the device parameter block
+  std::vector<uint32_t> scene_n;  // canonical particles of each scene
+  std::vector<DevUniforms> hu;    // host mirror of the per-scene parameter blocks
+  DevBatch hb{};                  // host mirror of the batch header
+  uint32_t cells_total = 0;
   DevState d{};
   void *arena = nullptr;
   size_t arena_bytes = 0;
-  // CUDA graph of one step (replayed for nsteps > 1)
-  cudaGraphExec_t graph_exec = nullptr;
-  uint32_t graph_n = 0, graph_iters = 0;
-  cudaStream_t graph_stream = nullptr;
+  StepGraph graphs[kGraphSlots];
+  uint64_t graph_clock = 0;
   // stage timing
   bool timing = false;
   cudaEvent_t ev[FS_STAGE_COUNT + 1] = {};
   double stage_ms[FS_STAGE_COUNT] = {};
   uint32_t timed_steps = 0;
 
-  uint32_t effective_n() const { return std::min(host_u.sph.num_particles, n); }
+  uint32_t scenes() const { return uint32_t(scene_n.size()); }
+  uint32_t active(uint32_t k) const { return std::min(hu[k].sph.num_particles, scene_n[k]); }
 };
 
 namespace {
@@ -106,7 +127,7 @@ struct Carver {
 void carve(FsSim *s, char *base, size_t *bytes) {
   Carver c{base};
   const size_t M = s->max_n;
-  const size_t G = s->grid.total_cells;
+  const size_t G = s->cells_total;
   DevState &d = s->d;
   d.p_pos = c.take<float4>(M);
   d.p_vel = c.take<float4>(M);
@@ -148,26 +169,66 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.mask_alloc = c.take<unsigned long long>(1);
   d.dir_half = int(std::min<size_t>(M, size_t(1) << 20));
   d.dir_tab = c.take<float4>(2 * size_t(d.dir_half) + 1);
-  d.accum = c.take<GpuRigidBodyAccum>(1);
+  const size_t S = s->scenes();
+  d.accum = c.take<GpuRigidBodyAccum>(S);
   d.err = c.take<uint32_t>(4);
   d.stats = c.take<unsigned long long>(STAT_COUNT);
-  d.u = c.take<DevUniforms>(1);
+  d.u = c.take<DevUniforms>(S);
+  d.b = c.take<DevBatch>(1);
+  d.scene_of = c.take<uint16_t>(M);
+  d.scene_of_slot = c.take<uint16_t>(M);
   *bytes = c.off;
 }
 
-void destroy_graph(FsSim *s) {
-  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
-  s->graph_exec = nullptr;
+void destroy_graphs(FsSim *s) {
+  for (StepGraph &g : s->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = StepGraph{};
+  }
 }
 
+// Offsets and counts of every scene from the scene sizes and the current
+// num_particles parameters.
+void layout(FsSim *s) {
+  uint32_t p = 0, c = 0, so = 0;
+  for (uint32_t k = 0; k < s->scenes(); k++) {
+    DevUniforms &u = s->hu[k];
+    u.n = s->active(k);
+    u.grid.num_particles = u.n;
+    u.sdf_res = s->sdf_res;
+    u.p_offset = p;
+    u.c_offset = c;
+    u.s_offset = so;
+    p += s->scene_n[k];
+    c += u.grid.total_cells;
+    so += u.n;
+  }
+  s->hb.n_scenes = s->scenes();
+  s->hb.n_canon = p;
+  s->hb.n_sorted = so;
+  s->hb.cells_total = c;
+}
+
+// Upload every scene's parameter block and the batch header.
 int upload_uniforms(FsSim *s) {
-  s->host_u.n = s->effective_n();
-  s->host_u.grid = s->grid;
-  s->host_u.grid.num_particles = s->host_u.n;
-  s->host_u.sdf_res = s->sdf_res;
-  FS_CUDA(cudaMemcpyAsync(s->d.u, &s->host_u, sizeof(DevUniforms), cudaMemcpyHostToDevice,
-                          s->stream),
+  layout(s);
+  FS_CUDA(cudaMemcpyAsync(s->d.u, s->hu.data(), sizeof(DevUniforms) * s->scenes(),
+                          cudaMemcpyHostToDevice, s->stream),
           "upload parameters");
+  FS_CUDA(cudaMemcpyAsync(s->d.b, &s->hb, sizeof(DevBatch), cudaMemcpyHostToDevice, s->stream),
+          "upload batch header");
+  return FS_OK;
+}
+
+// Upload scene k's block after a change to it; a change of its active count
+// moves the later scenes' slots, so then every block goes up.
+int upload_scene(FsSim *s, uint32_t k) {
+  const uint32_t before = s->hb.n_sorted;
+  layout(s);
+  if (s->hb.n_sorted != before) return upload_uniforms(s);
+  FS_CUDA(cudaMemcpyAsync(s->d.u + k, &s->hu[k], sizeof(DevUniforms), cudaMemcpyHostToDevice,
+                          s->stream),
+          "upload scene parameters");
   return FS_OK;
 }
 
@@ -216,10 +277,12 @@ int write_particles(FsSim *s, const SphParticle3D *parts, uint32_t offset, uint3
   return FS_OK;
 }
 
-// One step: the stage sequence of step(), sph_3d_grid.rs:1261-1444.
+// One step: the stage sequence of step(), sph_3d_grid.rs:1261-1444, over all
+// scenes at once.
 int enqueue_step(FsSim *s, bool timed) {
-  const uint32_t n = s->effective_n();
-  const uint32_t G = s->grid.total_cells;
+  const uint32_t n = s->hb.n_sorted;
+  const uint32_t n_canon = s->hb.n_canon;
+  const uint32_t G = s->cells_total;
   cudaStream_t st = s->stream;
   const DevState &d = s->d;
   auto mark = [&](int i) -> int {
@@ -230,11 +293,11 @@ int enqueue_step(FsSim *s, bool timed) {
   if ((rc = mark(0))) return rc;
   FS_CUDA(cudaMemsetAsync(d.counts, 0, sizeof(uint32_t) * G, st), "grid clear");
   if ((rc = mark(1))) return rc;
-  FS_CUDA(launch_hash(d, n, st), "grid build (hash)");
+  FS_CUDA(launch_hash(d, n_canon, st), "grid build (hash)");
   if ((rc = mark(2))) return rc;
   FS_CUDA(launch_scan(d, G, st), "prefix scan");
   if ((rc = mark(3))) return rc;
-  FS_CUDA(launch_scatter(d, n, st), "reorder (scatter)");
+  FS_CUDA(launch_scatter(d, n_canon, st), "reorder (scatter)");
   FS_CUDA(launch_sort_gather(d, n, st), "reorder (sort/gather)");
   if ((rc = mark(4))) return rc;
   FS_CUDA(launch_order_warps(d, n, st), "neighbour-pass work order");
@@ -252,30 +315,49 @@ int enqueue_step(FsSim *s, bool timed) {
   return FS_OK;
 }
 
-int ensure_graph(FsSim *s) {
-  const uint32_t n = s->effective_n();
-  if (s->graph_exec && s->graph_n == n && s->graph_iters == s->iterations &&
-      s->graph_stream == s->stream)
-    return FS_OK;
-  destroy_graph(s);
+// The graph of `steps` back-to-back steps for the current counts, captured
+// on first use (least recently used slot replaced).
+int graph_for(FsSim *s, uint32_t steps, cudaGraphExec_t *out) {
+  StepGraph *slot = nullptr;
+  for (StepGraph &g : s->graphs) {
+    if (g.exec && g.steps == steps && g.n_canon == s->hb.n_canon &&
+        g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream) {
+      g.last_use = ++s->graph_clock;
+      *out = g.exec;
+      return FS_OK;
+    }
+  }
+  for (StepGraph &g : s->graphs) {  // an empty slot, else the least recently used
+    if (!g.exec) {
+      slot = &g;
+      break;
+    }
+    if (!slot || g.last_use < slot->last_use) slot = &g;
+  }
+  if (slot->exec) cudaGraphExecDestroy(slot->exec);
+  *slot = StepGraph{};
   cudaGraph_t g = nullptr;
   FS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-  int rc = enqueue_step(s, false);
+  int rc = FS_OK;
+  for (uint32_t k = 0; k < steps && rc == FS_OK; k++) rc = enqueue_step(s, false);
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   if (rc != FS_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
   }
   if (e != cudaSuccess) return cuda_fail(e, "end capture");
-  e = cudaGraphInstantiate(&s->graph_exec, g, 0);
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
-  if (e != cudaSuccess) {
-    s->graph_exec = nullptr;
-    return cuda_fail(e, "instantiate step graph");
-  }
-  s->graph_n = n;
-  s->graph_iters = s->iterations;
-  s->graph_stream = s->stream;
+  if (e != cudaSuccess) return cuda_fail(e, "instantiate step graph");
+  slot->exec = exec;
+  slot->steps = steps;
+  slot->n_canon = s->hb.n_canon;
+  slot->n_sorted = s->hb.n_sorted;
+  slot->iters = s->iterations;
+  slot->stream = s->stream;
+  slot->last_use = ++s->graph_clock;
+  *out = exec;
   return FS_OK;
 }
 
@@ -287,57 +369,88 @@ int set_device(FsSim *s) {
   return FS_OK;
 }
 
-}  // namespace
+// Plain entry points act on a simulation's single scene.
+#define CHECK_PLAIN(s)                                                                        \
+  if ((s)->scenes() != 1)                                                                    \
+  return fail(FS_E_STATE, "%s: the simulation holds %u scenes (use the fs_batch_* calls)", \
+              __func__, (s)->scenes())
 
-extern "C" {
+#define CHECK_SCENE(s, k)                                                              \
+  if ((k) >= (s)->scenes())                                                           \
+  return fail(FS_E_INVALID_ARGUMENT, "%s: scene %u of %u", __func__, unsigned(k),     \
+              (s)->scenes())
 
-const char *fs_last_error(void) { return g_last_error.c_str(); }
-uint32_t fs_abi_version(void) { return FS_ABI_VERSION; }
+// Initial uniforms of SphSimulation3DGrid::new (sph_3d_grid.rs:257-300).
+void default_scene(DevUniforms &u, const GpuSphParams3D &params, const GpuContainerGeometry &geom) {
+  std::memset(&u, 0, sizeof(u));
+  u.sph = params;
+  u.geom = geom;
+  u.gravity = GpuGravity{{0.0f, -9.8f, 0.0f}, 0.0f};
+  u.mouse = GpuMouseForce{{0.0f, 0.0f, 0.0f}, 0.5f, 30.0f, 0u, 0u, 0.0f, {0.0f, 0.0f, -1.0f}, 0.0f};
+  u.rigid = GpuRigidBody{{0.0f, 0.0f, 0.0f}, 0.15f, {0.0f, 0.0f, 0.0f}, 0u, 200.0f, 0u, 0.0f, 0.0f,
+                         {1.0f, 0.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 1.0f, 0.0f}};
+}
 
-int fs_create(const SphParticle3D *particles, uint32_t num_particles, const GpuSphParams3D *params,
-              const GpuContainerGeometry *geom, uint32_t max_particles, const float *sdf,
-              uint32_t sdf_res, int device, uint32_t abi_version, FsSim **out) {
-  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_create: out is null");
+// Shared body of fs_create and fs_batch_create.
+int create_sim(const char *who, const SphParticle3D *particles, const uint32_t *counts,
+               uint32_t num_scenes, const GpuSphParams3D *params, const GpuContainerGeometry *geoms,
+               uint32_t max_particles, const float *sdf, uint32_t sdf_res, int device,
+               uint32_t abi_version, bool batch, FsSim **out) {
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "%s: out is null", who);
   *out = nullptr;
   if (abi_version != FS_ABI_VERSION)
-    return fail(FS_E_ABI_MISMATCH, "fs_create: caller ABI 0x%08x, library ABI 0x%08x", abi_version,
+    return fail(FS_E_ABI_MISMATCH, "%s: caller ABI 0x%08x, library ABI 0x%08x", who, abi_version,
                 FS_ABI_VERSION);
-  if (!params || !geom) return fail(FS_E_INVALID_ARGUMENT, "fs_create: params/geometry is null");
-  if (num_particles > 0 && !particles)
-    return fail(FS_E_INVALID_ARGUMENT, "fs_create: particles is null");
+  if (!params || !geoms) return fail(FS_E_INVALID_ARGUMENT, "%s: params/geometry is null", who);
+  if (num_scenes == 0 || num_scenes > FS_BATCH_MAX_SCENES)
+    return fail(FS_E_INVALID_ARGUMENT, "%s: %u scenes outside [1, %u]", who, num_scenes,
+                FS_BATCH_MAX_SCENES);
+  uint64_t total = 0;
+  for (uint32_t k = 0; k < num_scenes; k++) total += counts[k];
+  if (total > 0 && !particles) return fail(FS_E_INVALID_ARGUMENT, "%s: particles is null", who);
   if (sdf && (sdf_res == 0 || sdf_res > 512))
-    return fail(FS_E_INVALID_ARGUMENT, "fs_create: sdf_res %u outside [1, 512]", sdf_res);
-  const float h = params->kernel_radius;
-  if (!(h > 0.0f) || !std::isfinite(h))
-    return fail(FS_E_INVALID_ARGUMENT, "fs_create: kernel_radius must be finite and > 0");
-  const uint32_t max_n = std::max(max_particles, num_particles);
-  if (max_n > (1u << 30)) return fail(FS_E_CAPACITY, "fs_create: max_particles %u > 2^30", max_n);
+    return fail(FS_E_INVALID_ARGUMENT, "%s: sdf_res %u outside [1, 512]", who, sdf_res);
+  for (uint32_t k = 0; k < num_scenes; k++) {
+    const float h = params[k].kernel_radius;
+    if (!(h > 0.0f) || !std::isfinite(h))
+      return fail(FS_E_INVALID_ARGUMENT, "%s: scene %u kernel_radius must be finite and > 0", who, k);
+  }
+  const uint64_t max_n = std::max<uint64_t>(max_particles, total);
+  if (max_n > (1u << 30))
+    return fail(FS_E_CAPACITY, "%s: %llu particles > 2^30", who, (unsigned long long)max_n);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-    return fail(FS_E_NO_DEVICE, "fs_create: no CUDA device");
+    return fail(FS_E_NO_DEVICE, "%s: no CUDA device", who);
   if (device < 0 || device >= ndev)
-    return fail(FS_E_INVALID_ARGUMENT, "fs_create: device %d of %d", device, ndev);
+    return fail(FS_E_INVALID_ARGUMENT, "%s: device %d of %d", who, device, ndev);
 
   FsSim *s = new (std::nothrow) FsSim();
-  if (!s) return fail(FS_E_CAPACITY, "fs_create: out of host memory");
+  if (!s) return fail(FS_E_CAPACITY, "%s: out of host memory", who);
   s->device = device;
-  s->n = num_particles;
-  s->max_n = max_n;
-  GpuGridParams grid;
-  int rc = fs_grid_params_for(h, num_particles, &grid);
-  if (rc != FS_OK) {
-    delete s;
-    return fail(rc, "fs_create: grid for kernel_radius %g does not fit", double(h));
-  }
-  s->grid = grid;
+  s->batch = batch;
+  s->max_n = uint32_t(max_n);
   s->sdf_res = sdf ? sdf_res : 1u;
-  s->host_u.sph = *params;
-  s->host_u.geom = *geom;
-  // initial uniforms of SphSimulation3DGrid::new (sph_3d_grid.rs:257-300)
-  s->host_u.gravity = GpuGravity{{0.0f, -9.8f, 0.0f}, 0.0f};
-  s->host_u.mouse = GpuMouseForce{{0.0f, 0.0f, 0.0f}, 0.5f, 30.0f, 0u, 0u, 0.0f, {0.0f, 0.0f, -1.0f}, 0.0f};
-  s->host_u.rigid = GpuRigidBody{{0.0f, 0.0f, 0.0f}, 0.15f, {0.0f, 0.0f, 0.0f}, 0u, 200.0f, 0u, 0.0f, 0.0f,
-                                 {1.0f, 0.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 1.0f, 0.0f}};
+  s->scene_n.assign(counts, counts + num_scenes);
+  s->hu.resize(num_scenes);
+  uint64_t cells = 0;
+  for (uint32_t k = 0; k < num_scenes; k++) {
+    default_scene(s->hu[k], params[k], geoms[k]);
+    GpuGridParams grid;
+    int rc = fs_grid_params_for(params[k].kernel_radius, counts[k], &grid);
+    if (rc != FS_OK) {
+      delete s;
+      return fail(rc, "%s: scene %u grid for kernel_radius %g does not fit", who, k,
+                  double(params[k].kernel_radius));
+    }
+    s->hu[k].grid = grid;
+    cells += grid.total_cells;
+  }
+  if (cells >= (uint64_t(1) << 32) - 1) {
+    delete s;
+    return fail(FS_E_CAPACITY, "%s: %llu cells over all scenes", who, (unsigned long long)cells);
+  }
+  s->cells_total = uint32_t(cells);
+  layout(s);
 
   auto bail = [&](int code) {
     if (s->arena) cudaFree(s->arena);
@@ -347,6 +460,7 @@ int fs_create(const SphParticle3D *particles, uint32_t num_particles, const GpuS
     delete s;
     return code;
   };
+  int rc;
   if ((rc = set_device(s))) return bail(rc);
   cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(cuda_fail(e, "create stream"));
@@ -372,21 +486,125 @@ int fs_create(const SphParticle3D *particles, uint32_t num_particles, const GpuS
                       sizeof(float) * size_t(s->sdf_res) * s->sdf_res * s->sdf_res,
                       cudaMemcpyHostToDevice, s->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "upload SDF"));
+  if (num_scenes > 1) {  // scene ids of the canonical particles (a single scene is all zero)
+    std::vector<uint16_t> ids(s->hb.n_canon);
+    for (uint32_t k = 0; k < num_scenes; k++)
+      std::fill(ids.begin() + s->hu[k].p_offset, ids.begin() + s->hu[k].p_offset + counts[k],
+                uint16_t(k));
+    e = cudaMemcpyAsync(s->d.scene_of, ids.data(), sizeof(uint16_t) * ids.size(),
+                        cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "upload scene ids"));
+  }
   if ((rc = upload_uniforms(s))) return bail(rc);
   e = launch_dir_table(s->d, s->stream);
   if (e != cudaSuccess) return bail(cuda_fail(e, "close-pair direction table"));
-  if ((rc = write_particles(s, particles, 0, num_particles))) return bail(rc);
+  if ((rc = write_particles(s, particles, 0, uint32_t(total)))) return bail(rc);
   e = cudaStreamSynchronize(s->stream);
-  if (e != cudaSuccess) return bail(cuda_fail(e, "fs_create"));
+  if (e != cudaSuccess) return bail(cuda_fail(e, who));
   *out = s;
   return FS_OK;
+}
+
+// Scene k's canonical records [first, first + count) as 64-byte AoS.
+int read_canonical(FsSim *s, uint32_t first, SphParticle3D *out, uint32_t count) {
+  std::vector<float4> pos(count), vel(count), frc(count), aux(2 * size_t(count));
+  const size_t b = sizeof(float4) * count;
+  if (count) {
+    FS_CUDA(cudaMemcpyAsync(pos.data(), s->d.p_pos + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(vel.data(), s->d.p_vel + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(frc.data(), s->d.p_force + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(aux.data(), s->d.p_aux + 2 * size_t(first), 2 * b, cudaMemcpyDeviceToHost, s->stream), "download");
+  }
+  int rc;
+  if ((rc = check_device_error(s))) return rc;
+  for (uint32_t i = 0; i < count; i++) {
+    SphParticle3D &p = out[i];
+    p.position[0] = pos[i].x; p.position[1] = pos[i].y; p.position[2] = pos[i].z; p._pad0 = pos[i].w;
+    p.velocity[0] = vel[i].x; p.velocity[1] = vel[i].y; p.velocity[2] = vel[i].z; p._pad1 = vel[i].w;
+    p.force[0] = frc[i].x; p.force[1] = frc[i].y; p.force[2] = frc[i].z;
+    const float4 a0 = aux[2 * size_t(i)], a1 = aux[2 * size_t(i) + 1];
+    p.density = a0.x; p.near_density = a0.y;
+    p.normal[0] = a0.z; p.normal[1] = a0.w; p.normal[2] = a1.x;
+  }
+  return FS_OK;
+}
+
+// Sorted slots [first, first + count) as 64-byte AoS.
+int read_sorted(FsSim *s, uint32_t first, SphParticle3D *out, uint32_t count) {
+  std::vector<float4> pos(count), vel(count), frc(count), nrm(count);
+  std::vector<float2> dens(count);
+  const size_t b = sizeof(float4) * count;
+  if (count) {
+    FS_CUDA(cudaMemcpyAsync(pos.data(), s->d.s_pos + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(vel.data(), s->d.s_vel + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(frc.data(), s->d.s_frc + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(nrm.data(), s->d.s_nrm + first, b, cudaMemcpyDeviceToHost, s->stream), "download");
+    FS_CUDA(cudaMemcpyAsync(dens.data(), s->d.s_dens + first, sizeof(float2) * count, cudaMemcpyDeviceToHost, s->stream), "download");
+  }
+  int rc;
+  if ((rc = check_device_error(s))) return rc;
+  for (uint32_t i = 0; i < count; i++) {
+    SphParticle3D &p = out[i];
+    p.position[0] = pos[i].x; p.position[1] = pos[i].y; p.position[2] = pos[i].z; p._pad0 = pos[i].w;
+    p.velocity[0] = vel[i].x; p.velocity[1] = vel[i].y; p.velocity[2] = vel[i].z; p._pad1 = vel[i].w;
+    p.force[0] = frc[i].x; p.force[1] = frc[i].y; p.force[2] = frc[i].z;
+    p.density = dens[i].x; p.near_density = dens[i].y;
+    p.normal[0] = nrm[i].x; p.normal[1] = nrm[i].y; p.normal[2] = nrm[i].z;
+  }
+  return FS_OK;
+}
+
+// Scene k's cell counts and inclusive ends, relative to the scene's first slot.
+int read_cells(FsSim *s, uint32_t k, uint32_t *counts, uint32_t *starts) {
+  const DevUniforms &u = s->hu[k];
+  const uint32_t G = u.grid.total_cells;
+  const size_t b = sizeof(uint32_t) * G;
+  if (counts) FS_CUDA(cudaMemcpyAsync(counts, s->d.counts + u.c_offset, b, cudaMemcpyDeviceToHost, s->stream), "download counts");
+  if (starts) FS_CUDA(cudaMemcpyAsync(starts, s->d.cell_begin + 1 + u.c_offset, b, cudaMemcpyDeviceToHost, s->stream), "download starts");
+  int rc;
+  if ((rc = check_device_error(s))) return rc;
+  if (starts && u.s_offset)
+    for (uint32_t c = 0; c < G; c++) starts[c] -= u.s_offset;
+  return FS_OK;
+}
+
+// Scene k's index maps in scene-local numbering: particle -> slot for its
+// first `count` particles, slot -> particle for its first `count` slots.
+int read_index_maps(FsSim *s, uint32_t k, uint32_t *cell_indices, uint32_t *sorted_to_orig,
+                    uint32_t count) {
+  const DevUniforms &u = s->hu[k];
+  const size_t b = sizeof(uint32_t) * count;
+  if (cell_indices && count) FS_CUDA(cudaMemcpyAsync(cell_indices, s->d.cidx + u.p_offset, b, cudaMemcpyDeviceToHost, s->stream), "download cell indices");
+  if (sorted_to_orig && count) FS_CUDA(cudaMemcpyAsync(sorted_to_orig, s->d.s2o + u.s_offset, b, cudaMemcpyDeviceToHost, s->stream), "download sorted_to_orig");
+  int rc;
+  if ((rc = check_device_error(s))) return rc;
+  for (uint32_t i = 0; i < count; i++) {
+    if (cell_indices) cell_indices[i] -= u.s_offset;
+    if (sorted_to_orig) sorted_to_orig[i] -= u.p_offset;
+  }
+  return FS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *fs_last_error(void) { return g_last_error.c_str(); }
+uint32_t fs_abi_version(void) { return FS_ABI_VERSION; }
+
+int fs_create(const SphParticle3D *particles, uint32_t num_particles, const GpuSphParams3D *params,
+              const GpuContainerGeometry *geom, uint32_t max_particles, const float *sdf,
+              uint32_t sdf_res, int device, uint32_t abi_version, FsSim **out) {
+  return create_sim("fs_create", particles, &num_particles, 1, params, geom, max_particles, sdf,
+                    sdf_res, device, abi_version, false, out);
 }
 
 int fs_destroy(FsSim *s) {
   if (!s) return FS_OK;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  destroy_graph(s);
+  destroy_graphs(s);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
   if (s->arena) cudaFree(s->arena);
@@ -417,51 +635,59 @@ int fs_step(FsSim *s, uint32_t nsteps) {
     return FS_OK;
   }
   if (nsteps == 1) return enqueue_step(s, false);
-  if ((rc = ensure_graph(s))) return rc;
-  for (uint32_t k = 0; k < nsteps; k++)
-    FS_CUDA(cudaGraphLaunch(s->graph_exec, s->stream), "launch step graph");
+  // nsteps = chunks * chunk + rest: a graph of `chunk` steps (at most
+  // kMaxGraphSteps) replayed, then single-step graphs for the rest
+  const uint32_t chunks = (nsteps + kMaxGraphSteps - 1) / kMaxGraphSteps;
+  const uint32_t chunk = nsteps / chunks;
+  const uint32_t rest = nsteps - chunks * chunk;
+  cudaGraphExec_t g = nullptr;
+  if ((rc = graph_for(s, chunk, &g))) return rc;
+  for (uint32_t k = 0; k < chunks; k++)
+    FS_CUDA(cudaGraphLaunch(g, s->stream), "launch step graph");
+  if (rest) {
+    if ((rc = graph_for(s, 1, &g))) return rc;
+    for (uint32_t k = 0; k < rest; k++) FS_CUDA(cudaGraphLaunch(g, s->stream), "launch step graph");
+  }
+  return FS_OK;
+}
+
+int fs_prepare_steps(FsSim *s, uint32_t nsteps) {
+  CHECK_SIM(s);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (nsteps < 2 || s->timing) return FS_OK;
+  const uint32_t chunks = (nsteps + kMaxGraphSteps - 1) / kMaxGraphSteps;
+  const uint32_t chunk = nsteps / chunks;
+  cudaGraphExec_t g = nullptr;
+  if ((rc = graph_for(s, chunk, &g))) return rc;
+  if (nsteps != chunks * chunk && (rc = graph_for(s, 1, &g))) return rc;
   return FS_OK;
 }
 
 int fs_update_sph_params(FsSim *s, const GpuSphParams3D *p) {
   CHECK_SIM(s);
-  if (!p) return fail(FS_E_INVALID_ARGUMENT, "fs_update_sph_params: null params");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  s->host_u.sph = *p;
-  return upload_uniforms(s);
+  CHECK_PLAIN(s);
+  return fs_batch_update_scene(s, 0, p, nullptr, nullptr, nullptr, nullptr);
 }
 int fs_update_container_geometry(FsSim *s, const GpuContainerGeometry *g) {
   CHECK_SIM(s);
-  if (!g) return fail(FS_E_INVALID_ARGUMENT, "fs_update_container_geometry: null geometry");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  s->host_u.geom = *g;
-  return upload_uniforms(s);
+  CHECK_PLAIN(s);
+  return fs_batch_update_scene(s, 0, nullptr, g, nullptr, nullptr, nullptr);
 }
 int fs_update_mouse_force(FsSim *s, const GpuMouseForce *m) {
   CHECK_SIM(s);
-  if (!m) return fail(FS_E_INVALID_ARGUMENT, "fs_update_mouse_force: null mouse force");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  s->host_u.mouse = *m;
-  return upload_uniforms(s);
+  CHECK_PLAIN(s);
+  return fs_batch_update_scene(s, 0, nullptr, nullptr, nullptr, m, nullptr);
 }
 int fs_update_gravity(FsSim *s, const GpuGravity *g) {
   CHECK_SIM(s);
-  if (!g) return fail(FS_E_INVALID_ARGUMENT, "fs_update_gravity: null gravity");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  s->host_u.gravity = *g;
-  return upload_uniforms(s);
+  CHECK_PLAIN(s);
+  return fs_batch_update_scene(s, 0, nullptr, nullptr, g, nullptr, nullptr);
 }
 int fs_update_rigid_body(FsSim *s, const GpuRigidBody *b) {
   CHECK_SIM(s);
-  if (!b) return fail(FS_E_INVALID_ARGUMENT, "fs_update_rigid_body: null rigid body");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  s->host_u.rigid = *b;
-  return upload_uniforms(s);
+  CHECK_PLAIN(s);
+  return fs_batch_update_scene(s, 0, nullptr, nullptr, nullptr, nullptr, b);
 }
 int fs_set_pcisph_iterations(FsSim *s, uint32_t iterations) {
   CHECK_SIM(s);
@@ -473,41 +699,39 @@ int fs_clear_rigid_body_accum(FsSim *s) {
   CHECK_SIM(s);
   int rc;
   if ((rc = set_device(s))) return rc;
-  FS_CUDA(cudaMemsetAsync(s->d.accum, 0, sizeof(GpuRigidBodyAccum), s->stream), "clear accumulator");
+  FS_CUDA(cudaMemsetAsync(s->d.accum, 0, sizeof(GpuRigidBodyAccum) * s->scenes(), s->stream),
+          "clear accumulator");
   return FS_OK;
 }
 int fs_read_rigid_body_accum(FsSim *s, GpuRigidBodyAccum *out) {
   CHECK_SIM(s);
-  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_read_rigid_body_accum: null out");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  FS_CUDA(cudaMemcpyAsync(out, s->d.accum, sizeof(GpuRigidBodyAccum), cudaMemcpyDeviceToHost,
-                          s->stream),
-          "read accumulator");
-  return check_device_error(s);
+  CHECK_PLAIN(s);
+  return fs_batch_read_rigid_body_accum(s, out, 1);
 }
 
 int fs_num_particles(const FsSim *s, uint32_t *out) {
   CHECK_SIM(s);
   if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_num_particles: null out");
-  *out = s->n;
+  *out = s->hb.n_canon;
   return FS_OK;
 }
 
 int fs_grid_params(const FsSim *s, GpuGridParams *out) {
   CHECK_SIM(s);
+  CHECK_PLAIN(s);
   if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_grid_params: null out");
-  *out = s->grid;
-  out->num_particles = std::min(s->host_u.sph.num_particles, s->n);
+  *out = s->hu[0].grid;
   return FS_OK;
 }
 
 int fs_spawn_particles(FsSim *s, const float position[3], uint32_t count, float spread,
                        uint32_t *spawned) {
   CHECK_SIM(s);
+  CHECK_PLAIN(s);
   if (!position || !spawned) return fail(FS_E_INVALID_ARGUMENT, "fs_spawn_particles: null argument");
   *spawned = 0;
-  const uint32_t available = s->max_n - s->n;
+  const uint32_t n = s->scene_n[0];
+  const uint32_t available = s->max_n - n;
   const uint32_t spawn = std::min(count, available);
   if (spawn == 0) return FS_OK;
   int rc;
@@ -523,8 +747,8 @@ int fs_spawn_particles(FsSim *s, const float position[3], uint32_t count, float 
     np[i].position[1] = position[1] + float(layer) * spread * 0.3f;
     np[i].position[2] = position[2] + r * std::sin(angle);
   }
-  if ((rc = write_particles(s, np.data(), s->n, spawn))) return rc;
-  s->n += spawn;
+  if ((rc = write_particles(s, np.data(), n, spawn))) return rc;
+  s->scene_n[0] = n + spawn;
   if ((rc = upload_uniforms(s))) return rc;
   *spawned = spawn;
   return FS_OK;
@@ -532,90 +756,40 @@ int fs_spawn_particles(FsSim *s, const float position[3], uint32_t count, float 
 
 int fs_download_particles(FsSim *s, SphParticle3D *out, uint32_t count) {
   CHECK_SIM(s);
-  if (count > s->n) return fail(FS_E_CAPACITY, "fs_download_particles: %u > %u particles", count, s->n);
-  if (count && !out) return fail(FS_E_INVALID_ARGUMENT, "fs_download_particles: null out");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  std::vector<float4> pos(count), vel(count), frc(count), aux(2 * size_t(count));
-  const size_t b = sizeof(float4) * count;
-  if (count) {
-    FS_CUDA(cudaMemcpyAsync(pos.data(), s->d.p_pos, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(vel.data(), s->d.p_vel, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(frc.data(), s->d.p_force, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(aux.data(), s->d.p_aux, 2 * b, cudaMemcpyDeviceToHost, s->stream), "download");
-  }
-  if ((rc = check_device_error(s))) return rc;
-  for (uint32_t i = 0; i < count; i++) {
-    SphParticle3D &p = out[i];
-    p.position[0] = pos[i].x; p.position[1] = pos[i].y; p.position[2] = pos[i].z; p._pad0 = pos[i].w;
-    p.velocity[0] = vel[i].x; p.velocity[1] = vel[i].y; p.velocity[2] = vel[i].z; p._pad1 = vel[i].w;
-    p.force[0] = frc[i].x; p.force[1] = frc[i].y; p.force[2] = frc[i].z;
-    const float4 a0 = aux[2 * size_t(i)], a1 = aux[2 * size_t(i) + 1];
-    p.density = a0.x; p.near_density = a0.y;
-    p.normal[0] = a0.z; p.normal[1] = a0.w; p.normal[2] = a1.x;
-  }
-  return FS_OK;
+  CHECK_PLAIN(s);
+  return fs_batch_download_scene(s, 0, out, count);
 }
 
 int fs_download_sorted(FsSim *s, SphParticle3D *out, uint32_t count) {
   CHECK_SIM(s);
-  if (count > s->n) return fail(FS_E_CAPACITY, "fs_download_sorted: %u > %u particles", count, s->n);
+  CHECK_PLAIN(s);
+  if (count > s->scene_n[0])
+    return fail(FS_E_CAPACITY, "fs_download_sorted: %u > %u particles", count, s->scene_n[0]);
   if (count && !out) return fail(FS_E_INVALID_ARGUMENT, "fs_download_sorted: null out");
   int rc;
   if ((rc = set_device(s))) return rc;
-  std::vector<float4> pos(count), vel(count), frc(count), nrm(count);
-  std::vector<float2> dens(count);
-  const size_t b = sizeof(float4) * count;
-  if (count) {
-    FS_CUDA(cudaMemcpyAsync(pos.data(), s->d.s_pos, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(vel.data(), s->d.s_vel, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(frc.data(), s->d.s_frc, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(nrm.data(), s->d.s_nrm, b, cudaMemcpyDeviceToHost, s->stream), "download");
-    FS_CUDA(cudaMemcpyAsync(dens.data(), s->d.s_dens, sizeof(float2) * count, cudaMemcpyDeviceToHost, s->stream), "download");
-  }
-  if ((rc = check_device_error(s))) return rc;
-  for (uint32_t i = 0; i < count; i++) {
-    SphParticle3D &p = out[i];
-    p.position[0] = pos[i].x; p.position[1] = pos[i].y; p.position[2] = pos[i].z; p._pad0 = pos[i].w;
-    p.velocity[0] = vel[i].x; p.velocity[1] = vel[i].y; p.velocity[2] = vel[i].z; p._pad1 = vel[i].w;
-    p.force[0] = frc[i].x; p.force[1] = frc[i].y; p.force[2] = frc[i].z;
-    p.density = dens[i].x; p.near_density = dens[i].y;
-    p.normal[0] = nrm[i].x; p.normal[1] = nrm[i].y; p.normal[2] = nrm[i].z;
-  }
-  return FS_OK;
+  return read_sorted(s, 0, out, count);
 }
 
 int fs_download_cells(FsSim *s, uint32_t *counts, uint32_t *starts, uint32_t total_cells) {
   CHECK_SIM(s);
-  if (total_cells != s->grid.total_cells)
-    return fail(FS_E_INVALID_ARGUMENT, "fs_download_cells: total_cells %u != grid %u", total_cells,
-                s->grid.total_cells);
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  const size_t b = sizeof(uint32_t) * total_cells;
-  if (counts) FS_CUDA(cudaMemcpyAsync(counts, s->d.counts, b, cudaMemcpyDeviceToHost, s->stream), "download counts");
-  if (starts) FS_CUDA(cudaMemcpyAsync(starts, s->d.cell_begin + 1, b, cudaMemcpyDeviceToHost, s->stream), "download starts");
-  return check_device_error(s);
+  CHECK_PLAIN(s);
+  return fs_batch_download_scene_cells(s, 0, counts, starts, total_cells);
 }
 
 int fs_download_index_maps(FsSim *s, uint32_t *cell_indices, uint32_t *sorted_to_orig, uint32_t count) {
   CHECK_SIM(s);
-  if (count > s->n) return fail(FS_E_CAPACITY, "fs_download_index_maps: %u > %u", count, s->n);
+  CHECK_PLAIN(s);
+  if (count > s->scene_n[0]) return fail(FS_E_CAPACITY, "fs_download_index_maps: %u > %u", count, s->scene_n[0]);
   int rc;
   if ((rc = set_device(s))) return rc;
-  const size_t b = sizeof(uint32_t) * count;
-  if (cell_indices && count) FS_CUDA(cudaMemcpyAsync(cell_indices, s->d.cidx, b, cudaMemcpyDeviceToHost, s->stream), "download cell indices");
-  if (sorted_to_orig && count) FS_CUDA(cudaMemcpyAsync(sorted_to_orig, s->d.s2o, b, cudaMemcpyDeviceToHost, s->stream), "download sorted_to_orig");
-  return check_device_error(s);
+  return read_index_maps(s, 0, cell_indices, sorted_to_orig, count);
 }
 
 int fs_upload_particles(FsSim *s, const SphParticle3D *particles, uint32_t count) {
   CHECK_SIM(s);
-  if (count > s->n) return fail(FS_E_CAPACITY, "fs_upload_particles: %u > %u particles", count, s->n);
-  if (count && !particles) return fail(FS_E_INVALID_ARGUMENT, "fs_upload_particles: null particles");
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  return write_particles(s, particles, 0, count);
+  CHECK_PLAIN(s);
+  return fs_batch_upload_scene(s, 0, particles, count);
 }
 
 int fs_device_pointers(FsSim *s, FsDevicePointers *out) {
@@ -685,6 +859,130 @@ int fs_neighbor_stats(FsSim *s, uint64_t out[FS_STAT_COUNT], int reset) {
   for (int i = 0; i < FS_STAT_COUNT; i++) out[i] = v[i];
   if (reset) FS_CUDA(cudaMemset(s->d.stats, 0, sizeof(v)), "reset stats");
   return FS_OK;
+}
+
+// ---- batched form ---------------------------------------------------------------
+
+int fs_batch_create(const SphParticle3D *particles, const uint32_t *scene_counts,
+                    uint32_t num_scenes, const GpuSphParams3D *params,
+                    const GpuContainerGeometry *geoms, const float *sdf, uint32_t sdf_res,
+                    int device, uint32_t abi_version, FsSim **out) {
+  if (!scene_counts) return fail(FS_E_INVALID_ARGUMENT, "fs_batch_create: scene_counts is null");
+  return create_sim("fs_batch_create", particles, scene_counts, num_scenes, params, geoms, 0, sdf,
+                    sdf_res, device, abi_version, true, out);
+}
+
+int fs_batch_num_scenes(const FsSim *s, uint32_t *out) {
+  CHECK_SIM(s);
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_batch_num_scenes: null out");
+  *out = s->scenes();
+  return FS_OK;
+}
+
+int fs_batch_scene_info(const FsSim *s, uint32_t scene, FsSceneInfo *out) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_batch_scene_info: null out");
+  const DevUniforms &u = s->hu[scene];
+  std::memset(out, 0, sizeof(*out));
+  out->particle_offset = u.p_offset;
+  out->num_particles = s->scene_n[scene];
+  out->active_particles = u.n;
+  out->sorted_offset = u.s_offset;
+  out->cell_offset = u.c_offset;
+  out->total_cells = u.grid.total_cells;
+  out->grid = u.grid;
+  return FS_OK;
+}
+
+int fs_batch_update_scene(FsSim *s, uint32_t scene, const GpuSphParams3D *params,
+                          const GpuContainerGeometry *geom, const GpuGravity *gravity,
+                          const GpuMouseForce *mouse, const GpuRigidBody *body) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (!params && !geom && !gravity && !mouse && !body)
+    return fail(FS_E_INVALID_ARGUMENT, "%s: nothing to update", __func__);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  DevUniforms &u = s->hu[scene];
+  if (params) u.sph = *params;
+  if (geom) u.geom = *geom;
+  if (gravity) u.gravity = *gravity;
+  if (mouse) u.mouse = *mouse;
+  if (body) u.rigid = *body;
+  return upload_scene(s, scene);
+}
+
+int fs_batch_read_rigid_body_accum(FsSim *s, GpuRigidBodyAccum *out, uint32_t num_scenes) {
+  CHECK_SIM(s);
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_batch_read_rigid_body_accum: null out");
+  if (num_scenes > s->scenes())
+    return fail(FS_E_INVALID_ARGUMENT, "fs_batch_read_rigid_body_accum: %u > %u scenes",
+                num_scenes, s->scenes());
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (num_scenes)
+    FS_CUDA(cudaMemcpyAsync(out, s->d.accum, sizeof(GpuRigidBodyAccum) * num_scenes,
+                            cudaMemcpyDeviceToHost, s->stream),
+            "read accumulators");
+  return check_device_error(s);
+}
+
+int fs_batch_download_scene(FsSim *s, uint32_t scene, SphParticle3D *out, uint32_t count) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (count > s->scene_n[scene])
+    return fail(FS_E_CAPACITY, "%s: %u > %u particles", __func__, count, s->scene_n[scene]);
+  if (count && !out) return fail(FS_E_INVALID_ARGUMENT, "%s: null out", __func__);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  return read_canonical(s, s->hu[scene].p_offset, out, count);
+}
+
+int fs_batch_download_scene_sorted(FsSim *s, uint32_t scene, SphParticle3D *out, uint32_t count) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (count > s->hu[scene].n)
+    return fail(FS_E_CAPACITY, "%s: %u > %u active particles", __func__, count, s->hu[scene].n);
+  if (count && !out) return fail(FS_E_INVALID_ARGUMENT, "%s: null out", __func__);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  return read_sorted(s, s->hu[scene].s_offset, out, count);
+}
+
+int fs_batch_download_scene_cells(FsSim *s, uint32_t scene, uint32_t *counts, uint32_t *starts,
+                                  uint32_t total_cells) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (total_cells != s->hu[scene].grid.total_cells)
+    return fail(FS_E_INVALID_ARGUMENT, "%s: total_cells %u != grid %u", __func__, total_cells,
+                s->hu[scene].grid.total_cells);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  return read_cells(s, scene, counts, starts);
+}
+
+int fs_batch_download_scene_index_maps(FsSim *s, uint32_t scene, uint32_t *cell_indices,
+                                       uint32_t *sorted_to_orig, uint32_t count) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (count > s->hu[scene].n)
+    return fail(FS_E_CAPACITY, "%s: %u > %u active particles", __func__, count, s->hu[scene].n);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  return read_index_maps(s, scene, cell_indices, sorted_to_orig, count);
+}
+
+int fs_batch_upload_scene(FsSim *s, uint32_t scene, const SphParticle3D *particles,
+                          uint32_t count) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (count > s->scene_n[scene])
+    return fail(FS_E_CAPACITY, "%s: %u > %u particles", __func__, count, s->scene_n[scene]);
+  if (count && !particles) return fail(FS_E_INVALID_ARGUMENT, "%s: null particles", __func__);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  return write_particles(s, particles, s->hu[scene].p_offset, count);
 }
 
 }  // extern "C"

@@ -271,13 +271,14 @@ __device__ __forceinline__ float boundary_gamma(const GpuContainerGeometry &c, f
 // density it records each particle's hit mask (1e-12 < r^2 < h^2, the XSPH and
 // force criterion) for the later passes.
 __device__ __forceinline__ void density_one(
-    uint32_t s, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
               const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
               float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
               uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
               uint32_t *__restrict__ mask_hits, unsigned long long *__restrict__ mask_alloc,
               unsigned long long mask_cap) {
-  const bool active = s < U->n;
+  const bool active = s < v.b->n_sorted;
+  const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
@@ -290,7 +291,7 @@ __device__ __forceinline__ void density_one(
   R.total = 0;
   if (active) {
     pos_i = xyz(s_pos[s]);
-    neighbor_runs(pos_i, U->grid, begin, R);
+    neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   }
   const uint32_t off = alloc_mask(active, (R.total + 31u) >> 5, mask_alloc, mask_cap);
   if (active) {
@@ -351,7 +352,7 @@ __device__ __forceinline__ void density_one(
 // ---- XSPH -------------------------------------------------------------------
 // xsph.wgsl:81-138; the result is the post-XSPH velocity in sorted order (the
 // reference scatters it to the canonical array).
-__device__ __forceinline__ void xsph_one(uint32_t s, const DevUniforms *__restrict__ U,
+__device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
                                               const float4 *__restrict__ s_pos,
                                               const float4 *__restrict__ s_vel,
                                               const float2 *__restrict__ s_dens,
@@ -359,7 +360,8 @@ __device__ __forceinline__ void xsph_one(uint32_t s, const DevUniforms *__restri
                                               const uint32_t *__restrict__ mask_words,
                                               const uint32_t *__restrict__ mask_off,
                                               float4 *__restrict__ vel_x) {
-  if (s >= U->n) return;
+  if (s >= v.b->n_sorted) return;
+  const DevUniforms *U = v.u + v.scene_of_slot[s];
   const GpuSphParams3D &P = U->sph;
   const float4 vi4 = s_vel[s];
   const float eps = P.xsph_epsilon;
@@ -372,7 +374,7 @@ __device__ __forceinline__ void xsph_one(uint32_t s, const DevUniforms *__restri
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
   const float3 pos_i = xyz(s_pos[s]);
   Runs R;
-  neighbor_runs(pos_i, U->grid, begin, R);
+  neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   float3 corr = f3(0.f, 0.f, 0.f);
   auto body = [&](uint32_t j, float r_sq) {
     const float density_j = fmaxf(__ldg(&s_dens[j].x), 1.0f);
@@ -395,22 +397,23 @@ __device__ __forceinline__ void xsph_one(uint32_t s, const DevUniforms *__restri
         R, [&](uint32_t j) { r_sq = dist2(j); return r_sq < h2 && r_sq > 1e-12f; },
         [&](uint32_t j) { body(j, r_sq); });
   }
-  const float3 v = vel_i + eps * corr;
-  vel_x[s] = make_float4(v.x, v.y, v.z, vi4.w);
+  const float3 vn = vel_i + eps * corr;
+  vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
 }
 
 // ---- force + PCISPH predict ---------------------------------------------------
 // sph_force_3d_grid.wgsl:105-227, then pcisph_predict.wgsl:61-72 for the same
 // particle (sorted order).
 __device__ __forceinline__ void force_predict_one(
-    uint32_t s, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
                     const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
                     const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
                     const uint32_t *__restrict__ mask_off, float4 *__restrict__ anp,
                     float4 *__restrict__ pred_xp, float *__restrict__ pred_rho) {
-  if (s >= U->n) return;
+  if (s >= v.b->n_sorted) return;
+  const DevUniforms *U = v.u + v.scene_of_slot[s];
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
@@ -427,7 +430,7 @@ __device__ __forceinline__ void force_predict_one(
   const float near_pressure_i = near_k * near_density_i;
   float3 a_p = f3(0.f, 0.f, 0.f), a_v = f3(0.f, 0.f, 0.f), a_c = f3(0.f, 0.f, 0.f);
   Runs R;
-  neighbor_runs(pos_i, U->grid, begin, R);
+  neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   // Every arm of the shader's branches is evaluated and the accumulators are
   // updated with selects (x = c ? x + t : x), which leaves their bits exactly
   // as the branches would: lanes of a warp then never split inside the body.
@@ -450,7 +453,8 @@ __device__ __forceinline__ void force_predict_one(
     const int d = int(s) - int(j);
     const bool tabulated = d >= -dir_half && d <= dir_half;
     float3 dir_close = tabulated ? xyz(__ldg(dir_tab + (tabulated ? d + dir_half : 0))) : dir_far;
-    if (close && !tabulated) dir_close = fallback_dir_eval(float(s) - float(j));
+    if (close && !tabulated)
+      dir_close = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
     const float3 dir = close ? dir_close : dir_far;
     const float density_j = fmaxf(dj.x, 1.0f);
     const float near_density_j = fmaxf(dj.y, 1.0f);
@@ -513,14 +517,15 @@ __device__ __forceinline__ void force_predict_one(
 // velocity.
 template <bool HAS_PRESSURE, bool LAST>
 __device__ __forceinline__ void solve_one(
-    uint32_t s, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
             const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
             const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float4 *__restrict__ v_out,
             unsigned long long *__restrict__ stats) {
-  const bool active = s < U->n;
+  const bool active = s < v.b->n_sorted;
+  const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
@@ -535,7 +540,7 @@ __device__ __forceinline__ void solve_one(
     const float old_p = self_xp.w;
     const float sd = fmaxf(rho_in[s], 1.0f);
     const float3 pos_i = xyz(s_pos[s]);  // current position decides the cells
-    neighbor_runs(pos_i, U->grid, begin, R);
+    neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
     float pred_density = 0.0f;
     float3 a_p = f3(0.f, 0.f, 0.f);
     const float self_term = old_p / (sd * sd);
@@ -635,18 +640,20 @@ __device__ __forceinline__ void for_warp_tasks(const TaskQueue &q, F &&f) {
 // first (the order inside a bucket is immaterial).
 constexpr int ORDER_BUCKETS = 33;
 __global__ void __launch_bounds__(256)
-    k_warp_work(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    k_warp_work(SceneView v, const float4 *__restrict__ s_pos,
                 const uint32_t *__restrict__ begin, uint8_t *__restrict__ warp_bucket,
                 uint32_t *__restrict__ hist) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t total = 0u;
-  if (s < U->n) {
+  const bool active = s < v.b->n_sorted;
+  if (active) {
+    const DevUniforms *U = v.u + v.scene_of_slot[s];
     Runs R;
-    neighbor_runs(xyz(s_pos[s]), U->grid, begin, R);
+    neighbor_runs(xyz(s_pos[s]), U->grid, begin + U->c_offset, R);
     total = R.total;
   }
   const uint32_t m = __reduce_max_sync(0xffffffffu, total);
-  if ((threadIdx.x & 31u) == 0u && s < U->n) {
+  if ((threadIdx.x & 31u) == 0u && active) {
     const uint32_t b = 32u - uint32_t(__clz(m));
     warp_bucket[s >> 5] = uint8_t(b);
     atomicAdd(&hist[b], 1u);
@@ -654,7 +661,7 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void __launch_bounds__(256)
-    k_scatter_order(const DevUniforms *__restrict__ U, const uint8_t *__restrict__ warp_bucket,
+    k_scatter_order(SceneView v, const uint8_t *__restrict__ warp_bucket,
                     const uint32_t *__restrict__ hist, uint32_t *__restrict__ cursor,
                     uint32_t *__restrict__ order) {
   __shared__ uint32_t base[ORDER_BUCKETS];
@@ -667,36 +674,36 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= (U->n + 31u) / 32u) return;
+  if (w >= (v.b->n_sorted + 31u) / 32u) return;
   const uint32_t b = warp_bucket[w];
   order[base[b] + atomicAdd(&cursor[b], 1u)] = w;
 }
 
 __global__ void __launch_bounds__(128)
-    k_density(TaskQueue q, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    k_density(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
               const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
               float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
               uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
               uint32_t *__restrict__ mask_hits, unsigned long long *__restrict__ mask_alloc,
               unsigned long long mask_cap) {
   for_warp_tasks(q, [&](uint32_t s) {
-    density_one(s, U, s_pos, begin, s_dens, s_nrm, stats, mask_words, mask_off, mask_hits,
+    density_one(s, v, s_pos, begin, s_dens, s_nrm, stats, mask_words, mask_off, mask_hits,
                 mask_alloc, mask_cap);
   });
 }
 
 __global__ void __launch_bounds__(128)
-    k_xsph(TaskQueue q, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    k_xsph(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
            const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
            const uint32_t *__restrict__ begin, const uint32_t *__restrict__ mask_words,
            const uint32_t *__restrict__ mask_off, float4 *__restrict__ vel_x) {
   for_warp_tasks(q, [&](uint32_t s) {
-    xsph_one(s, U, s_pos, s_vel, s_dens, begin, mask_words, mask_off, vel_x);
+    xsph_one(s, v, s_pos, s_vel, s_dens, begin, mask_words, mask_off, vel_x);
   });
 }
 
 __global__ void __launch_bounds__(128, 4)
-    k_force_predict(TaskQueue q, const DevUniforms *__restrict__ U,
+    k_force_predict(TaskQueue q, SceneView v,
                     const float4 *__restrict__ s_pos, const float4 *__restrict__ s_vel,
                     const float2 *__restrict__ s_dens, const float4 *__restrict__ s_nrm,
                     const float4 *__restrict__ vel_x, const uint32_t *__restrict__ begin,
@@ -705,14 +712,14 @@ __global__ void __launch_bounds__(128, 4)
                     float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
                     float *__restrict__ pred_rho) {
   for_warp_tasks(q, [&](uint32_t s) {
-    force_predict_one(s, U, s_pos, s_vel, s_dens, s_nrm, vel_x, begin, dir_tab, dir_half,
+    force_predict_one(s, v, s_pos, s_vel, s_dens, s_nrm, vel_x, begin, dir_tab, dir_half,
                       mask_words, mask_off, anp, pred_xp, pred_rho);
   });
 }
 
 template <bool HAS_PRESSURE, bool LAST>
 __global__ void __launch_bounds__(128)
-    k_solve(TaskQueue q, const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
             const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
@@ -720,7 +727,7 @@ __global__ void __launch_bounds__(128)
             float *__restrict__ rho_out, float4 *__restrict__ v_out,
             unsigned long long *__restrict__ stats) {
   for_warp_tasks(q, [&](uint32_t s) {
-    solve_one<HAS_PRESSURE, LAST>(s, U, s_pos, vel_x, anp, begin, xp_in, rho_in, mask_words,
+    solve_one<HAS_PRESSURE, LAST>(s, v, s_pos, vel_x, anp, begin, xp_in, rho_in, mask_words,
                                   mask_off, xp_out, rho_out, v_out, stats);
   });
 }
@@ -756,7 +763,7 @@ __device__ __forceinline__ float sample_sdf(const float *__restrict__ sdf, int r
 __device__ __forceinline__ int f2i_rz(float x) { return __float2int_rz(x); }  // saturating, NaN -> 0
 
 __global__ void __launch_bounds__(128)
-    k_finalize_integrate(const DevUniforms *__restrict__ U, const float4 *__restrict__ s_pos,
+    k_finalize_integrate(SceneView v, const float4 *__restrict__ s_pos,
                          const float4 *__restrict__ s_vel, const float4 *__restrict__ vel_x,
                          const float4 *__restrict__ v_fin, const uint32_t *__restrict__ s2o,
                          const float *__restrict__ sdf, float4 *__restrict__ p_pos,
@@ -765,7 +772,10 @@ __global__ void __launch_bounds__(128)
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   int32_t rfx = 0, rfy = 0, rfz = 0, rtx = 0, rty = 0, rtz = 0;
   uint32_t contact = 0;
-  if (s < U->n) {
+  const bool active = s < v.b->n_sorted;
+  const uint32_t scene = active ? v.scene_of_slot[s] : 0u;
+  if (active) {
+    const DevUniforms *U = v.u + scene;
     const GpuSphParams3D &P = U->sph;
     const GpuContainerGeometry &c = U->geom;
     const uint32_t orig = s2o[s];
@@ -939,26 +949,41 @@ __global__ void __launch_bounds__(128)
     p_vel[orig] = make_float4(vw.x, vw.y, vw.z, s_vel[s].w);
   }
   // rigid-body reaction: integer sums are order independent, so reduce in
-  // the warp and add once per warp (sph_integrate_3d.wgsl:328-339)
+  // the warp and add once per warp (sph_integrate_3d.wgsl:328-339). A warp
+  // whose contacts span two scenes (a scene boundary inside the warp) adds
+  // lane by lane into each scene's accumulator instead.
   const unsigned any = __ballot_sync(0xffffffffu, contact != 0u);
   if (any) {
+    const uint32_t s0 = __shfl_sync(0xffffffffu, scene, __ffs(any) - 1);
+    if (__all_sync(0xffffffffu, contact == 0u || scene == s0)) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      rfx += __shfl_xor_sync(0xffffffffu, rfx, o);
-      rfy += __shfl_xor_sync(0xffffffffu, rfy, o);
-      rfz += __shfl_xor_sync(0xffffffffu, rfz, o);
-      rtx += __shfl_xor_sync(0xffffffffu, rtx, o);
-      rty += __shfl_xor_sync(0xffffffffu, rty, o);
-      rtz += __shfl_xor_sync(0xffffffffu, rtz, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      atomicAdd(&accum->force_x, rfx);
-      atomicAdd(&accum->force_y, rfy);
-      atomicAdd(&accum->force_z, rfz);
-      atomicAdd(&accum->contact_count, uint32_t(__popc(any)));
-      atomicAdd(&accum->torque_x, rtx);
-      atomicAdd(&accum->torque_y, rty);
-      atomicAdd(&accum->torque_z, rtz);
+      for (int o = 16; o > 0; o >>= 1) {
+        rfx += __shfl_xor_sync(0xffffffffu, rfx, o);
+        rfy += __shfl_xor_sync(0xffffffffu, rfy, o);
+        rfz += __shfl_xor_sync(0xffffffffu, rfz, o);
+        rtx += __shfl_xor_sync(0xffffffffu, rtx, o);
+        rty += __shfl_xor_sync(0xffffffffu, rty, o);
+        rtz += __shfl_xor_sync(0xffffffffu, rtz, o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        GpuRigidBodyAccum *a = accum + s0;
+        atomicAdd(&a->force_x, rfx);
+        atomicAdd(&a->force_y, rfy);
+        atomicAdd(&a->force_z, rfz);
+        atomicAdd(&a->contact_count, uint32_t(__popc(any)));
+        atomicAdd(&a->torque_x, rtx);
+        atomicAdd(&a->torque_y, rty);
+        atomicAdd(&a->torque_z, rtz);
+      }
+    } else if (contact) {
+      GpuRigidBodyAccum *a = accum + scene;
+      atomicAdd(&a->force_x, rfx);
+      atomicAdd(&a->force_y, rfy);
+      atomicAdd(&a->force_z, rfz);
+      atomicAdd(&a->contact_count, 1u);
+      atomicAdd(&a->torque_x, rtx);
+      atomicAdd(&a->torque_y, rty);
+      atomicAdd(&a->torque_z, rtz);
     }
   }
 }
@@ -998,10 +1023,10 @@ cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d.order_hist, 0, sizeof(uint32_t) * 2 * ORDER_BUCKETS, st);
   if (e != cudaSuccess) return e;
-  k_warp_work<<<blocks_for(n, 256), 256, 0, st>>>(d.u, d.s_pos, d.cell_begin, d.warp_bucket,
+  k_warp_work<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.cell_begin, d.warp_bucket,
                                                   d.order_hist);
   const uint32_t nwarps = (n + 31u) / 32u;
-  k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(d.u, d.warp_bucket, d.order_hist,
+  k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(d.view(), d.warp_bucket, d.order_hist,
                                                            d.order_hist + ORDER_BUCKETS,
                                                            d.warp_order);
   return cudaGetLastError();
@@ -1016,7 +1041,7 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_density, d.sm_count);
-  k_density<<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.cell_begin, d.s_dens, d.s_nrm, d.stats,
+  k_density<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.cell_begin, d.s_dens, d.s_nrm, d.stats,
                                     d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc,
                                     d.mask_cap);
   return cudaGetLastError();
@@ -1029,7 +1054,7 @@ cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_xsph, d.sm_count);
-  k_xsph<<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.s_vel, d.s_dens, d.cell_begin, d.mask_words,
+  k_xsph<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.s_dens, d.cell_begin, d.mask_words,
                                  d.mask_off, d.vel_x);
   return cudaGetLastError();
 }
@@ -1041,7 +1066,7 @@ cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st)
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count);
-  k_force_predict<<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x,
+  k_force_predict<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x,
                                           d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
                                           d.mask_off, d.anp, d.pred_xp[0], d.pred_rho[0]);
   return cudaGetLastError();
@@ -1057,7 +1082,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   do {                                                                                        \
     static unsigned blocks = 0;                                                               \
     if (!blocks) blocks = persistent_blocks(k_solve<P_, L_>, d.sm_count);                    \
-    k_solve<P_, L_><<<blocks, 128, 0, st>>>(q, d.u, d.s_pos, d.vel_x, d.anp, d.cell_begin,    \
+    k_solve<P_, L_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp, d.cell_begin,    \
                                             d.pred_xp[in], d.pred_rho[in], d.mask_words,      \
                                             d.mask_off, d.pred_xp[out], d.pred_rho[out],      \
                                             d.pred_v, d.stats);                               \
@@ -1073,7 +1098,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
 cudaError_t launch_finalize_integrate(const DevState &d, uint32_t n, int /*final_buf*/,
                                       cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_finalize_integrate<<<blocks_for(n, 128), 128, 0, st>>>(d.u, d.s_pos, d.s_vel, d.vel_x,
+  k_finalize_integrate<<<blocks_for(n, 128), 128, 0, st>>>(d.view(), d.s_pos, d.s_vel, d.vel_x,
                                                            d.pred_v, d.s2o, d.sdf, d.p_pos,
                                                            d.p_vel, d.p_force, d.accum);
   return cudaGetLastError();

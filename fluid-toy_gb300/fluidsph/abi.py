@@ -15,7 +15,7 @@ import numpy as np
 
 from .build import LIB_PATH
 
-FS_ABI_VERSION = 0x00010040
+FS_ABI_VERSION = 0x00010050
 FS_OK = 0
 FS_STAGE_COUNT = 10
 FS_STAT_COUNT = 5
@@ -98,9 +98,16 @@ class FsDevicePointers(C.Structure):
         "stream")]
 
 
+class FsSceneInfo(C.Structure):
+    _fields_ = [("particle_offset", C.c_uint32), ("num_particles", C.c_uint32),
+                ("active_particles", C.c_uint32), ("sorted_offset", C.c_uint32),
+                ("cell_offset", C.c_uint32), ("total_cells", C.c_uint32),
+                ("_pad", C.c_uint32 * 2), ("grid", GpuGridParams)]
+
+
 STRUCT_SIZES = {
     GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
-    GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48,
+    GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48, FsSceneInfo: 80,
 }
 for _t, _n in STRUCT_SIZES.items():
     assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))
@@ -126,6 +133,7 @@ SIGNATURES = {
                             _vp, _u32, C.c_int, _u32, _P(_vp)]),
     "fs_destroy": (C.c_int, [_vp]),
     "fs_step": (C.c_int, [_vp, _u32]),
+    "fs_prepare_steps": (C.c_int, [_vp, _u32]),
     "fs_update_sph_params": (C.c_int, [_vp, _P(GpuSphParams3D)]),
     "fs_update_container_geometry": (C.c_int, [_vp, _P(GpuContainerGeometry)]),
     "fs_update_mouse_force": (C.c_int, [_vp, _P(GpuMouseForce)]),
@@ -149,7 +157,20 @@ SIGNATURES = {
     "fs_stage_times": (C.c_int, [_vp, _P(C.c_double), _P(_u32), C.c_int]),
     "fs_neighbor_stats": (C.c_int, [_vp, _P(C.c_uint64), C.c_int]),
     "fs_prefix_scan_noalloc": (C.c_int, [_vp, _vp, _u32, _vp, _vp]),
+    "fs_batch_create": (C.c_int, [_vp, _P(_u32), _u32, _vp, _vp, _vp, _u32, C.c_int, _u32,
+                                  _P(_vp)]),
+    "fs_batch_num_scenes": (C.c_int, [_vp, _P(_u32)]),
+    "fs_batch_scene_info": (C.c_int, [_vp, _u32, _P(FsSceneInfo)]),
+    "fs_batch_update_scene": (C.c_int, [_vp, _u32, _P(GpuSphParams3D), _P(GpuContainerGeometry),
+                                        _P(GpuGravity), _P(GpuMouseForce), _P(GpuRigidBody)]),
+    "fs_batch_read_rigid_body_accum": (C.c_int, [_vp, _vp, _u32]),
+    "fs_batch_download_scene": (C.c_int, [_vp, _u32, _vp, _u32]),
+    "fs_batch_download_scene_sorted": (C.c_int, [_vp, _u32, _vp, _u32]),
+    "fs_batch_download_scene_cells": (C.c_int, [_vp, _u32, _vp, _vp, _u32]),
+    "fs_batch_download_scene_index_maps": (C.c_int, [_vp, _u32, _vp, _vp, _u32]),
+    "fs_batch_upload_scene": (C.c_int, [_vp, _u32, _vp, _u32]),
 }
+FS_BATCH_MAX_SCENES = 65535
 FS_NOALLOC_SCAN_MAX_CELLS = 1 << 26
 
 _lib = None

@@ -160,4 +160,77 @@ def config3(seed: int = 0) -> Scene:
     return make_scene("rollout_32768", parts, box, steps=200)
 
 
+def _to_container(parts: np.ndarray, geom: GpuContainerGeometry) -> np.ndarray:
+    """Map positions given in the untilted container frame through the
+    container's rotation about its centre (the local_to_world transform of
+    container_common.wgsl), so a block at the local min corner stays inside a
+    tilted box."""
+    rows = np.array([list(geom.forward_row0)[:3], list(geom.forward_row1)[:3],
+                     list(geom.forward_row2)[:3]], np.float64)
+    local = parts[:, COL_POS].astype(np.float64)
+    local[:, 1] -= geom.center_y
+    world = local @ rows.T
+    world[:, 1] += geom.center_y
+    out = parts.copy()
+    out[:, COL_POS] = world.astype(np.float32)
+    return out
+
+
+def batch_scene(k: int, seed: int = 0, lo: int = 2048, hi: int = 65536,
+                steps: int = 200) -> Scene:
+    """Scene k of the batched ensemble.
+
+    count log-uniform in [lo, hi]; fill f ~ U[0.3, 0.6]; side lengths
+    U[0.8, 2.0] rescaled so that count * 0.02^3 / V = f, redrawn (up to 32
+    times) while a side leaves [0.8, 2.0], else clamped into it (small counts
+    cannot reach the fill inside a 0.8 box: their effective fill is lower and
+    is recorded in ``info``); viscosity U[5, 25], stiffness U[20, 50],
+    surface_tension U[3, 10], tilt_x and tilt_z U[-15, 15] degrees. The block
+    is a dam-break lattice at the box's min corner whose footprint covers
+    f^(1/3) of the floor along x and z, filled x, z, then y up to `count`
+    particles, then rotated with the container."""
+    u = uniform01(seed * 1_000_003 + 7919 * (k + 1), 128)
+    count = int(round(np.exp(np.log(lo) + u[0] * (np.log(hi) - np.log(lo)))))
+    count = min(max(count, lo), hi)
+    fill = 0.3 + 0.3 * u[1]
+    target_v = count * 0.02 ** 3 / fill
+    sides = None
+    for a in range(32):
+        L = 0.8 + 1.2 * u[2 + 3 * a: 5 + 3 * a]
+        L = L * (target_v / np.prod(L)) ** (1.0 / 3.0)
+        if np.all((L >= 0.8) & (L <= 2.0)):
+            sides = L
+            break
+    clamped = sides is None
+    if clamped:
+        sides = np.clip(L, 0.8, 2.0)
+    Lx, Ly, Lz = (float(np.float32(v)) for v in sides)
+    eff_fill = count * 0.02 ** 3 / (Lx * Ly * Lz)
+    g = min(eff_fill, 1.0) ** (1.0 / 3.0)
+    max_x, max_z = int(Lx / 0.02) - 2, int(Lz / 0.02) - 2
+    nx = min(max(int(g * Lx / 0.02), 1), max_x)
+    nz = min(max(int(g * Lz / 0.02), 1), max_z)
+    ny = -(-count // (nx * nz))
+    if (ny + 1) * 0.02 > Ly - 0.02:
+        nx, nz = max_x, max_z
+        ny = -(-count // (nx * nz))
+    c = Common(viscosity=float(5.0 + 20.0 * u[100]), stiffness=float(20.0 + 30.0 * u[101]),
+               surface_tension=float(3.0 + 7.0 * u[102]))
+    tilt_x = float(np.radians(-15.0 + 30.0 * u[103]))
+    tilt_z = float(np.radians(-15.0 + 30.0 * u[104]))
+    box = (Lx, Ly, Lz)
+    parts = lattice_block(nx, ny, nz, box, seed=seed * 1_000_003 + 7919 * (k + 1) + 1)[:count]
+    sc = make_scene(f"batch{k}_{count}", parts, box, c, steps=steps, tilt_x=tilt_x,
+                    tilt_z=tilt_z, info={"fill": fill, "effective_fill": eff_fill,
+                                         "clamped": clamped, "block": (nx, ny, nz)})
+    sc.particles = _to_container(parts, sc.geom)
+    return sc
+
+
+def config2(seed: int = 0, num_scenes: int = 256, lo: int = 2048, hi: int = 65536,
+            steps: int = 200) -> list:
+    """Batched ensemble: `num_scenes` independent scenes (batch_scene)."""
+    return [batch_scene(k, seed, lo, hi, steps) for k in range(num_scenes)]
+
+
 CONFIGS = {0: config0, 1: config1, 3: config3}

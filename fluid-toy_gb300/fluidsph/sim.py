@@ -15,9 +15,9 @@ import ctypes as C
 import numpy as np
 
 from . import abi
-from .abi import (FS_ABI_VERSION, FS_STAGE_COUNT, FS_STAT_COUNT, GpuContainerGeometry,
-                  GpuGravity, GpuGridParams, GpuMouseForce, GpuRigidBody, GpuRigidBodyAccum,
-                  GpuSphParams3D, check)
+from .abi import (FS_ABI_VERSION, FS_STAGE_COUNT, FS_STAT_COUNT, FsSceneInfo,
+                  GpuContainerGeometry, GpuGravity, GpuGridParams, GpuMouseForce, GpuRigidBody,
+                  GpuRigidBodyAccum, GpuSphParams3D, check)
 
 
 class SphSimulation3DGrid:
@@ -64,6 +64,10 @@ class SphSimulation3DGrid:
     # -- step and parameter uploads (sph_3d_grid.rs:1261-1477) --------------------
     def step(self, nsteps: int = 1) -> None:
         check(self._lib.fs_step(self._h, int(nsteps)))
+
+    def prepare_steps(self, nsteps: int) -> None:
+        """Capture the step graphs ``step(nsteps)`` will replay."""
+        check(self._lib.fs_prepare_steps(self._h, int(nsteps)))
 
     def update_sph_params(self, params: GpuSphParams3D) -> None:
         check(self._lib.fs_update_sph_params(self._h, C.byref(params)))
@@ -168,3 +172,94 @@ class SphSimulation3DGrid:
         check(self._lib.fs_neighbor_stats(self._h, out, 1 if reset else 0))
         keys = ("cand_density", "hits_density", "hits_nonself", "cand_solve", "hits_solve")
         return {k: int(out[i]) for i, k in enumerate(keys)}
+
+
+class SphBatch3DGrid(SphSimulation3DGrid):
+    """Independent scenes stepped together (fs_batch_*): every stage is one
+    launch over all scenes, and scene k evolves bit for bit like a
+    ``SphSimulation3DGrid`` built from the same inputs. The simulation-wide
+    methods (``step``, ``set_pcisph_iterations``, timing, statistics) are
+    inherited; per-scene state goes through the ``*_scene`` methods."""
+
+    def __init__(self, scenes_particles, sph_params, container_geoms, sdf=None, device: int = 0):
+        self._lib = abi.load()
+        counts = [len(p) for p in scenes_particles]
+        if not counts:
+            raise ValueError("a batch needs at least one scene")
+        if not (len(sph_params) == len(container_geoms) == len(counts)):
+            raise ValueError("one particle array, SphParams and geometry per scene")
+        parts = np.concatenate([abi.as_particles(p) if len(p) else np.zeros((0, 16), np.float32)
+                                for p in scenes_particles])
+        self._parts_keep = parts
+        c_counts = (C.c_uint32 * len(counts))(*counts)
+        c_params = (GpuSphParams3D * len(counts))(*sph_params)
+        c_geoms = (GpuContainerGeometry * len(counts))(*container_geoms)
+        sdf_ptr, sdf_res = None, 0
+        if sdf is not None:
+            sdf = np.ascontiguousarray(sdf, dtype=np.float32)
+            sdf_res = int(round(sdf.size ** (1.0 / 3.0)))
+            if sdf_res ** 3 != sdf.size:
+                raise ValueError("sdf must hold res^3 values")
+            sdf_ptr = sdf.ctypes.data
+        h = C.c_void_p()
+        check(self._lib.fs_batch_create(parts.ctypes.data if len(parts) else None, c_counts,
+                                        len(counts), C.cast(c_params, C.c_void_p),
+                                        C.cast(c_geoms, C.c_void_p), sdf_ptr, sdf_res,
+                                        int(device), FS_ABI_VERSION, C.byref(h)))
+        self._h = h
+        self.counts = counts
+
+    def num_scenes(self) -> int:
+        v = C.c_uint32()
+        check(self._lib.fs_batch_num_scenes(self._h, C.byref(v)))
+        return v.value
+
+    def scene_info(self, scene: int) -> FsSceneInfo:
+        out = FsSceneInfo()
+        check(self._lib.fs_batch_scene_info(self._h, int(scene), C.byref(out)))
+        return out
+
+    def update_scene(self, scene: int, sph_params=None, container_geom=None, gravity=None,
+                     mouse=None, rigid_body=None) -> None:
+        ref = lambda x: C.byref(x) if x is not None else None
+        check(self._lib.fs_batch_update_scene(self._h, int(scene), ref(sph_params),
+                                              ref(container_geom), ref(gravity), ref(mouse),
+                                              ref(rigid_body)))
+
+    def read_rigid_body_accums(self) -> list:
+        n = self.num_scenes()
+        out = (GpuRigidBodyAccum * n)()
+        check(self._lib.fs_batch_read_rigid_body_accum(self._h, C.cast(out, C.c_void_p), n))
+        return list(out)
+
+    def scene_particles(self, scene: int, count: int | None = None) -> np.ndarray:
+        n = self.scene_info(scene).num_particles if count is None else int(count)
+        out = np.empty((n, 16), np.float32)
+        check(self._lib.fs_batch_download_scene(self._h, int(scene), out.ctypes.data, n))
+        return out
+
+    def scene_sorted_particles(self, scene: int, count: int | None = None) -> np.ndarray:
+        n = self.scene_info(scene).active_particles if count is None else int(count)
+        out = np.empty((n, 16), np.float32)
+        check(self._lib.fs_batch_download_scene_sorted(self._h, int(scene), out.ctypes.data, n))
+        return out
+
+    def scene_cells(self, scene: int) -> tuple[np.ndarray, np.ndarray]:
+        g = self.scene_info(scene).total_cells
+        counts = np.empty(g, np.uint32)
+        starts = np.empty(g, np.uint32)
+        check(self._lib.fs_batch_download_scene_cells(self._h, int(scene), counts.ctypes.data,
+                                                      starts.ctypes.data, g))
+        return counts, starts
+
+    def scene_index_maps(self, scene: int) -> tuple[np.ndarray, np.ndarray]:
+        n = self.scene_info(scene).active_particles
+        ci = np.empty(n, np.uint32)
+        so = np.empty(n, np.uint32)
+        check(self._lib.fs_batch_download_scene_index_maps(self._h, int(scene), ci.ctypes.data,
+                                                           so.ctypes.data, n))
+        return ci, so
+
+    def upload_scene_particles(self, scene: int, particles: np.ndarray) -> None:
+        p = abi.as_particles(particles)
+        check(self._lib.fs_batch_upload_scene(self._h, int(scene), p.ctypes.data, len(p)))

@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010040u
+#define FS_ABI_VERSION 0x00010050u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -233,9 +233,15 @@ int fs_create(const SphParticle3D *particles, uint32_t num_particles,
 int fs_destroy(FsSim *sim);
 
 /* step(), sph_3d_grid.rs:1261-1444, run `nsteps` times back to back on the
- * simulation's stream. With nsteps > 1 the step sequence is replayed from a
- * captured CUDA graph. Asynchronous. */
+ * simulation's stream. With nsteps > 1 the steps run from captured CUDA
+ * graphs: one graph of up to 256 whole steps, replayed, plus one-step
+ * replays for a remainder. A graph is captured on first use for its step
+ * count and the current particle counts and iteration count (a few are
+ * kept). Asynchronous. */
 int fs_step(FsSim *sim, uint32_t nsteps);
+/* No counterpart in the reference. Capture now the graphs a later
+ * fs_step(sim, nsteps) uses, so that call only launches. */
+int fs_prepare_steps(FsSim *sim, uint32_t nsteps);
 
 /* update_* uploads, sph_3d_grid.rs:1446-1473. Ordered before later steps. */
 int fs_update_sph_params(FsSim *sim, const GpuSphParams3D *params);
@@ -309,6 +315,69 @@ int fs_stage_times(FsSim *sim, double ms[FS_STAGE_COUNT], uint32_t *steps,
  * PCISPH solve iterations, out[4] solve pairs with r^2 < h^2. Synchronises. */
 #define FS_STAT_COUNT 5
 int fs_neighbor_stats(FsSim *sim, uint64_t out[FS_STAT_COUNT], int reset);
+
+/* ---- batched form ----------------------------------------------------------- */
+
+/* No counterpart in the reference, whose App owns one SphSimulation3DGrid
+ * (src/app.rs:253). A batch is a simulation holding independent scenes, each
+ * with its own particles, SphParams, container (box, tilt), gravity, mouse
+ * force, rigid body and grid (fs_grid_params_for of its kernel radius and
+ * count), stepped together: every stage is one launch over all scenes, and
+ * scene k's results are bit for bit those of fs_create on the same inputs.
+ * The simulation-wide calls (fs_step, fs_prepare_steps, fs_set_pcisph_iterations,
+ * fs_clear_rigid_body_accum (all scenes), fs_num_particles (all scenes),
+ * fs_device_pointers, fs_set_stream, fs_sync, the timing and statistics
+ * calls, fs_destroy) take a batch; the per-scene plain calls return
+ * FS_E_STATE on a batch of more than one scene, and fs_spawn_particles is
+ * not available for batches. */
+#define FS_BATCH_MAX_SCENES 65535u
+
+/* Where scene k lives in the batch's device arrays (fs_device_pointers):
+ * canonical particles [particle_offset, particle_offset + num_particles),
+ * sorted slots [sorted_offset, sorted_offset + active_particles), cells
+ * [cell_offset, cell_offset + total_cells); the cell_starts/cell_begin
+ * entries of its cells count slots from 0, not from sorted_offset. */
+typedef struct FsSceneInfo {
+    uint32_t particle_offset;
+    uint32_t num_particles;
+    uint32_t active_particles; /* min(params.num_particles, num_particles) */
+    uint32_t sorted_offset;
+    uint32_t cell_offset;
+    uint32_t total_cells;
+    uint32_t _pad[2];
+    GpuGridParams grid;        /* the scene's grid (num_particles = active) */
+} FsSceneInfo;
+
+/* particles: all scenes' records, scene after scene; scene_counts,
+ * params and geoms: one entry per scene. Each scene starts with the
+ * defaults of fs_create (gravity (0,-9.8,0), mouse force and rigid body
+ * inactive). The SDF is shared by all scenes. */
+int fs_batch_create(const SphParticle3D *particles, const uint32_t *scene_counts,
+                    uint32_t num_scenes, const GpuSphParams3D *params,
+                    const GpuContainerGeometry *geoms, const float *sdf,
+                    uint32_t sdf_res, int device, uint32_t abi_version,
+                    FsSim **out);
+int fs_batch_num_scenes(const FsSim *sim, uint32_t *out);
+int fs_batch_scene_info(const FsSim *sim, uint32_t scene, FsSceneInfo *out);
+/* The update_* uploads for one scene; NULL arguments keep their value. */
+int fs_batch_update_scene(FsSim *sim, uint32_t scene, const GpuSphParams3D *params,
+                          const GpuContainerGeometry *geom, const GpuGravity *gravity,
+                          const GpuMouseForce *mouse, const GpuRigidBody *body);
+/* Accumulators of scenes [0, num_scenes); synchronises. */
+int fs_batch_read_rigid_body_accum(FsSim *sim, GpuRigidBodyAccum *out,
+                                   uint32_t num_scenes);
+/* Per-scene read-outs and upload, in scene-local numbering (synchronising). */
+int fs_batch_download_scene(FsSim *sim, uint32_t scene, SphParticle3D *out,
+                            uint32_t count);
+int fs_batch_download_scene_sorted(FsSim *sim, uint32_t scene, SphParticle3D *out,
+                                   uint32_t count);
+int fs_batch_download_scene_cells(FsSim *sim, uint32_t scene, uint32_t *counts,
+                                  uint32_t *starts, uint32_t total_cells);
+int fs_batch_download_scene_index_maps(FsSim *sim, uint32_t scene,
+                                       uint32_t *cell_indices,
+                                       uint32_t *sorted_to_orig, uint32_t count);
+int fs_batch_upload_scene(FsSim *sim, uint32_t scene, const SphParticle3D *particles,
+                          uint32_t count);
 
 /* ---- prefix scan without allocation -------------------------------------- */
 
