@@ -116,6 +116,24 @@ struct DevState {
 // Set the thread-local text fs_last_error() returns (sim.cu).
 void set_last_error(const char *msg);
 
+// x^n for an integral n >= 1: binary exponentiation in double, rounded once
+// to float (host_params.cpp). The library's value of WGSL pow(x, n.0).
+float pow_int_f32(float x, unsigned n);
+
+// The MC density pass (splat_kernels.cu). begin: the scene's cell_begin
+// (global slot numbers), s_pos: the sorted positions of all scenes.
+struct SplatArgs {
+  GpuMcGridParams mc;
+  GpuContainerGeometry geom;
+  GpuGridParams sph;
+  float coeff;      // 315 / (64 pi pow(h, 9))
+  int cell_radius;  // ceil(h * sph.inv_cell_size)
+};
+SplatArgs make_splat_args(const GpuMcGridParams &mc, const GpuContainerGeometry &geom,
+                          const GpuGridParams &sph);
+cudaError_t launch_density_splat(const SplatArgs &a, const float4 *s_pos, const uint32_t *begin,
+                                 float *out, cudaStream_t st);
+
 // ---- kernel launchers (grid_kernels.cu / sph_kernels.cu) --------------------
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;

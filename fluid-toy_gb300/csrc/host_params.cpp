@@ -7,6 +7,7 @@
 //   rotation_matrices + to_gpu_geometry  src/state/simulation.rs:139-184
 //   quat_to_rotation_rows     src/state/rigid_body.rs:188-205
 //   grid sizing               src/simulation/sph_3d_grid.rs:121-143
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -182,4 +183,38 @@ int fs_grid_params_for(float kernel_radius, uint32_t num_particles, GpuGridParam
   return FS_OK;
 }
 
+int fs_mc_grid_params(const float grid_min[3], const float grid_max[3], uint32_t grid_size,
+                      float kernel_radius, float iso_value, uint32_t num_particles,
+                      GpuMcGridParams *out) {
+  if (!out || !grid_min || !grid_max || grid_size == 0) return FS_E_INVALID_ARGUMENT;
+  const float ex = grid_max[0] - grid_min[0];
+  const float ey = grid_max[1] - grid_min[1];
+  const float ez = grid_max[2] - grid_min[2];
+  GpuMcGridParams p;
+  std::memset(&p, 0, sizeof(p));
+  std::memcpy(p.grid_min, grid_min, 12);
+  std::memcpy(p.grid_max, grid_max, 12);
+  p.grid_size = grid_size;
+  p.cell_size = std::max(std::max(ex, ey), ez) / float(grid_size);
+  p.kernel_radius = kernel_radius;
+  p.iso_value = iso_value;
+  p.num_particles = num_particles;
+  p.max_vertices = 4000000u;
+  *out = p;
+  return FS_OK;
+}
+
 }  // extern "C"
+
+namespace fs {
+float pow_int_f32(float x, unsigned n);
+}
+
+float fs::pow_int_f32(float x, unsigned n) {
+  double r = 1.0, b = double(x);
+  for (; n; n >>= 1) {
+    if (n & 1u) r *= b;
+    b *= b;
+  }
+  return float(r);
+}

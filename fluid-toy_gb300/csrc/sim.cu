@@ -64,6 +64,7 @@ static_assert(offsetof(SphParticle3D, normal) == 52, "normal offset");
 static_assert(offsetof(GpuContainerGeometry, wall_stiffness) == 112, "geometry offset");
 static_assert(offsetof(GpuRigidBody, rot_row0) == 48, "rigid offset");
 static_assert(sizeof(FsSceneInfo) == 80, "FsSceneInfo layout");
+static_assert(sizeof(GpuMcGridParams) == 48, "GpuMcGridParams layout");
 static_assert(FS_BATCH_MAX_SCENES <= 65535u, "scene ids are 16-bit");
 
 }  // namespace
@@ -98,6 +99,8 @@ struct FsSim {
   size_t arena_bytes = 0;
   StepGraph graphs[kGraphSlots];
   uint64_t graph_clock = 0;
+  float *splat_buf = nullptr;  // device staging of host-bound density fields
+  size_t splat_cap = 0;
   // stage timing
   bool timing = false;
   cudaEvent_t ev[FS_STAGE_COUNT + 1] = {};
@@ -607,6 +610,7 @@ int fs_destroy(FsSim *s) {
   destroy_graphs(s);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
+  if (s->splat_buf) cudaFree(s->splat_buf);
   if (s->arena) cudaFree(s->arena);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
@@ -790,6 +794,48 @@ int fs_upload_particles(FsSim *s, const SphParticle3D *particles, uint32_t count
   CHECK_SIM(s);
   CHECK_PLAIN(s);
   return fs_batch_upload_scene(s, 0, particles, count);
+}
+
+int fs_density_splat(FsSim *s, uint32_t scene, const GpuMcGridParams *grid,
+                     const GpuContainerGeometry *geom, float *density, int density_on_device) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (!grid || !geom || !density)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_density_splat: null argument");
+  if (grid->grid_size == 0 || grid->grid_size > 1024)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_density_splat: grid_size %u outside [1, 1024]",
+                grid->grid_size);
+  if (!(grid->kernel_radius > 0.0f) || !std::isfinite(grid->kernel_radius) ||
+      !(grid->cell_size > 0.0f) || !std::isfinite(grid->cell_size))
+    return fail(FS_E_INVALID_ARGUMENT, "fs_density_splat: kernel_radius and cell_size must be "
+                                       "finite and > 0");
+  const SplatArgs a = make_splat_args(*grid, *geom, s->hu[scene].grid);
+  if (a.cell_radius < 1 || a.cell_radius > 8)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_density_splat: splat radius spans %d SPH cells (1..8)",
+                a.cell_radius);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  const size_t voxels = size_t(grid->grid_size) * grid->grid_size * grid->grid_size;
+  const uint32_t *begin = s->d.cell_begin + s->hu[scene].c_offset;
+  if (density_on_device) {
+    FS_CUDA(launch_density_splat(a, s->d.s_pos, begin, density, s->stream), "density splat");
+    return FS_OK;
+  }
+  if (s->splat_cap < voxels) {
+    if (s->splat_buf) {
+      FS_CUDA(cudaStreamSynchronize(s->stream), "density splat");
+      cudaFree(s->splat_buf);
+      s->splat_buf = nullptr;
+      s->splat_cap = 0;
+    }
+    FS_CUDA(cudaMalloc(&s->splat_buf, sizeof(float) * voxels), "allocate density field");
+    s->splat_cap = voxels;
+  }
+  FS_CUDA(launch_density_splat(a, s->d.s_pos, begin, s->splat_buf, s->stream), "density splat");
+  FS_CUDA(cudaMemcpyAsync(density, s->splat_buf, sizeof(float) * voxels, cudaMemcpyDeviceToHost,
+                          s->stream),
+          "download density field");
+  return check_device_error(s);
 }
 
 int fs_device_pointers(FsSim *s, FsDevicePointers *out) {

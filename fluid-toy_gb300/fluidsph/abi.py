@@ -91,6 +91,13 @@ class GpuGridParams(C.Structure):
                 ("_padding", C.c_uint32 * 2)]
 
 
+class GpuMcGridParams(C.Structure):
+    _fields_ = [("grid_min", C.c_float * 3), ("grid_size", C.c_uint32),
+                ("grid_max", C.c_float * 3), ("cell_size", C.c_float),
+                ("kernel_radius", C.c_float), ("iso_value", C.c_float),
+                ("num_particles", C.c_uint32), ("max_vertices", C.c_uint32)]
+
+
 class FsDevicePointers(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in (
         "pos", "vel", "force", "sorted_pos", "sorted_vel", "sorted_density", "sorted_normal",
@@ -108,6 +115,7 @@ class FsSceneInfo(C.Structure):
 STRUCT_SIZES = {
     GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
     GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48, FsSceneInfo: 80,
+    GpuMcGridParams: 48,
 }
 for _t, _n in STRUCT_SIZES.items():
     assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))
@@ -129,6 +137,7 @@ SIGNATURES = {
                                         _P(GpuContainerGeometry)]),
     "fs_quat_to_rotation_rows": (C.c_int, [_P(_f), _P(_f)]),
     "fs_grid_params_for": (C.c_int, [_f, _u32, _P(GpuGridParams)]),
+    "fs_mc_grid_params": (C.c_int, [_P(_f), _P(_f), _u32, _f, _f, _u32, _P(GpuMcGridParams)]),
     "fs_create": (C.c_int, [_vp, _u32, _P(GpuSphParams3D), _P(GpuContainerGeometry), _u32,
                             _vp, _u32, C.c_int, _u32, _P(_vp)]),
     "fs_destroy": (C.c_int, [_vp]),
@@ -150,6 +159,8 @@ SIGNATURES = {
     "fs_download_cells": (C.c_int, [_vp, _vp, _vp, _u32]),
     "fs_download_index_maps": (C.c_int, [_vp, _vp, _vp, _u32]),
     "fs_upload_particles": (C.c_int, [_vp, _vp, _u32]),
+    "fs_density_splat": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),
+                                   _vp, C.c_int]),
     "fs_device_pointers": (C.c_int, [_vp, _P(FsDevicePointers)]),
     "fs_set_stream": (C.c_int, [_vp, _vp]),
     "fs_sync": (C.c_int, [_vp]),

@@ -91,3 +91,15 @@ def grid_params_for(kernel_radius: float, num_particles: int) -> GpuGridParams:
     g = GpuGridParams()
     check(abi.load().fs_grid_params_for(kernel_radius, int(num_particles), C.byref(g)))
     return g
+
+
+def mc_grid_params(grid_min, grid_max, grid_size: int, kernel_radius: float,
+                   iso_value: float = 0.0, num_particles: int = 0):
+    """MarchingCubesRenderer::update_params (marching_cubes.rs:2099-2113)."""
+    from .abi import GpuMcGridParams
+    out = GpuMcGridParams()
+    lo = (C.c_float * 3)(*[float(v) for v in grid_min])
+    hi = (C.c_float * 3)(*[float(v) for v in grid_max])
+    check(abi.load().fs_mc_grid_params(lo, hi, int(grid_size), float(kernel_radius),
+                                       float(iso_value), int(num_particles), C.byref(out)))
+    return out

@@ -152,6 +152,21 @@ class SphSimulation3DGrid:
         check(self._lib.fs_download_index_maps(self._h, ci.ctypes.data, so.ctypes.data, n))
         return ci, so
 
+    def density_splat(self, mc_params, container_geom, scene: int = 0,
+                      out_device_ptr: int | None = None):
+        """The MC density pass (mc_density.wgsl) over the last step's sorted
+        positions: a (gs, gs, gs) float32 array indexed [z, y, x], or, with
+        ``out_device_ptr``, written to that device memory asynchronously."""
+        gs = int(mc_params.grid_size)
+        if out_device_ptr is not None:
+            check(self._lib.fs_density_splat(self._h, int(scene), C.byref(mc_params),
+                                             C.byref(container_geom), int(out_device_ptr), 1))
+            return None
+        out = np.empty((gs, gs, gs), np.float32)
+        check(self._lib.fs_density_splat(self._h, int(scene), C.byref(mc_params),
+                                         C.byref(container_geom), out.ctypes.data, 0))
+        return out
+
     def device_pointers(self) -> abi.FsDevicePointers:
         p = abi.FsDevicePointers()
         check(self._lib.fs_device_pointers(self._h, C.byref(p)))

@@ -164,6 +164,20 @@ typedef struct GpuGridParams {
     uint32_t _padding[2];
 } GpuGridParams;
 
+/* GpuGridParams of the marching-cubes renderer, src/render/marching_cubes.rs:
+ * 56-66 — 48 bytes. Named GpuMcGridParams here because the SPH grid struct
+ * above carries the same name in the reference. */
+typedef struct GpuMcGridParams {
+    float grid_min[3];
+    uint32_t grid_size;      /* voxels per dimension */
+    float grid_max[3];
+    float cell_size;         /* voxel edge length */
+    float kernel_radius;     /* splat radius (sim h * mc_density_radius_scale) */
+    float iso_value;
+    uint32_t num_particles;
+    uint32_t max_vertices;
+} GpuMcGridParams;
+
 /* Device pointers of a simulation, the analogue of the reference's buffer
  * getters (sph_3d_grid.rs:1500-1530). The library keeps particles as
  * structure-of-arrays float4 records (one coalesced 16-byte load per field),
@@ -217,6 +231,13 @@ int fs_quat_to_rotation_rows(const float q[4], float rows[12]);
 /* Grid sizing of SphSimulation3DGrid::new, sph_3d_grid.rs:121-143. */
 int fs_grid_params_for(float kernel_radius, uint32_t num_particles,
                        GpuGridParams *out);
+
+/* MarchingCubesRenderer::update_params, src/render/marching_cubes.rs:
+ * 2099-2113: cell_size = largest extent of [grid_min, grid_max] / grid_size,
+ * max_vertices = 4,000,000 (marching_cubes.rs:20). */
+int fs_mc_grid_params(const float grid_min[3], const float grid_max[3], uint32_t grid_size,
+                      float kernel_radius, float iso_value, uint32_t num_particles,
+                      GpuMcGridParams *out);
 
 /* ---- SphSimulation3DGrid ------------------------------------------------- */
 
@@ -286,6 +307,23 @@ int fs_download_index_maps(FsSim *sim, uint32_t *cell_indices,
 /* Overwrite the canonical particle records (all fields) of [0, count). */
 int fs_upload_particles(FsSim *sim, const SphParticle3D *particles,
                         uint32_t count);
+
+/* The marching-cubes density pass, mc_density.wgsl:130-231 (dispatched at
+ * src/render/marching_cubes.rs:2462-2468), in its isotropic form (anisotropy
+ * off): the poly6 density (no mass factor) at the centres of grid_size^3
+ * voxels, x fastest, summed over the particles of the SPH cells within
+ * ceil(kernel_radius / cell) of the voxel's cell, from the grid-sorted
+ * positions and cell tables of the scene's last step (the buffers the
+ * reference binds). With geom->clip_enabled, voxels outside the box hold -1;
+ * the others are divided by the five-wall boundary gamma (floor 0.15).
+ * pow(h, 9) is binary exponentiation in double rounded once to float (WGSL
+ * leaves pow's precision to the implementation). `density` receives the
+ * field: host memory (synchronises) or, with density_on_device != 0, device
+ * memory (asynchronous on the simulation's stream). grid_size <= 1024.
+ * `scene` is 0 for a plain simulation. */
+int fs_density_splat(FsSim *sim, uint32_t scene, const GpuMcGridParams *grid,
+                     const GpuContainerGeometry *geom, float *density,
+                     int density_on_device);
 
 /* Borrow device memory zero-copy (buffer getters). */
 int fs_device_pointers(FsSim *sim, FsDevicePointers *out);

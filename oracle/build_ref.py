@@ -34,6 +34,8 @@ SHADERS = [
     ("pcisph_solve", "pcisph_solve.wgsl", False),
     ("pcisph_finalize", "pcisph_finalize.wgsl", False),
     ("sph_integrate", "sph_integrate_3d.wgsl", True),
+    # the MC density splat (marching_cubes.rs:663-669 prepends container_common)
+    ("mc_density", "mc_density.wgsl", True),
 ]
 
 CXXFLAGS = ["-std=c++20", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing",

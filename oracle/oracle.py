@@ -92,6 +92,7 @@ def _bind(lib):
         lib.or_get_predicted.argtypes = [vp, C.c_int, vp, u32]
         lib.or_sincos_f32.argtypes = [vp, vp, vp, u32]
         lib.or_set_threads.argtypes = [C.c_int]
+        lib.or_density_splat.argtypes = [vp, vp, vp, vp]
         lib.or_max_threads.restype = C.c_int
     return lib
 
@@ -211,6 +212,16 @@ class OracleSim:
         so = np.empty(self._n, np.uint32)
         self._lib.or_get_index_maps(self._h, ci.ctypes.data, so.ctypes.data, self._n)
         return ci, so
+
+    def density_splat(self, mc_params, container_geom) -> np.ndarray:
+        """The MC density field (mc_density.wgsl) of the last step's sorted
+        positions, shape (gs, gs, gs) indexed [z, y, x]; float64 (the FP32
+        path's values are exact in it)."""
+        gs = int(mc_params.grid_size)
+        out = np.empty((gs, gs, gs), np.float64)
+        self._lib.or_density_splat(self._h, C.addressof(mc_params), C.addressof(container_geom),
+                                   out.ctypes.data)
+        return out
 
     def predicted(self, which: int) -> np.ndarray:
         out = np.empty((self._n, 8), np.float32)

@@ -315,4 +315,25 @@ void or_get_predicted(void *, int, float *, uint32_t) {}
 void or_get_grid(void *h, void *out) { std::memcpy(out, ((RefSim *)h)->grid, 48); }
 void or_sincos_f32(const float *, float *, float *, uint32_t) {}
 
+// The MC density pass exactly as mc_density.wgsl runs it, on the sorted
+// buffer and cell tables of the last step (bindings of marching_cubes.rs).
+void or_density_splat(void *hv, const void *mc, const void *geom, double *out) {
+  auto *h = (RefSim *)hv;
+  static_assert(sizeof(mc_density::GridParams) == 48, "MC GridParams");
+  std::memcpy(&mc_density::params, mc, 48);
+  std::memcpy(&mc_density::container, geom, 128);
+  std::memcpy(&mc_density::sph_grid, h->grid, 48);
+  mc_density::sorted_particles = as<mc_density::SphParticle3D>(h->S.data());
+  mc_density::cell_starts = h->starts.data();
+  mc_density::cell_counts = h->counts.data();
+  mc_density::aniso_params = mc_density::AnisoParams{};  // enabled = 0
+  const u32 gs = mc_density::params.grid_size;
+  std::vector<float> field(size_t(gs) * gs * gs);
+  mc_density::density_field.data = field.data();
+  mc_density::density_field.dim = gs;
+  const u32 groups = (gs + 3u) / 4u;
+  mc_density::dispatch_main(groups, groups, groups);
+  for (size_t i = 0; i < field.size(); i++) out[i] = field[i];
+}
+
 }  // extern "C"

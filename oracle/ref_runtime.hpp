@@ -170,6 +170,22 @@ inline f32 cos(f32 x) {
 inline f32 abs(f32 x) { return std::fabs(x); }
 inline vec3<f32> abs(vec3<f32> v) { return vec3<f32>(std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)); }
 inline f32 floor(f32 x) { return std::floor(x); }
+inline f32 ceil(f32 x) { return std::ceil(x); }
+// pow: WGSL leaves its precision to the implementation. A positive integral
+// exponent up to 64 is evaluated as binary exponentiation in double, rounded
+// once to f32 (the library's own definition, fs_pow_f32); other exponents use
+// std::pow in double.
+inline f32 pow(f32 x, f32 y) {
+  if (y >= 1.0f && y <= 64.0f && y == std::floor(y)) {
+    double r = 1.0, b = double(x);
+    for (unsigned n = unsigned(y); n; n >>= 1) {
+      if (n & 1u) r *= b;
+      b *= b;
+    }
+    return f32(r);
+  }
+  return f32(std::pow(double(x), double(y)));
+}
 inline vec3<f32> floor(vec3<f32> v) { return vec3<f32>(std::floor(v.x), std::floor(v.y), std::floor(v.z)); }
 inline f32 max(f32 a, f32 b) { return std::fmax(a, b); }
 inline f32 min(f32 a, f32 b) { return std::fmin(a, b); }
@@ -204,6 +220,14 @@ struct texture_3d {
   int res = 1;
 };
 struct sampler {};
+// write-only r32float storage volume, dim^3 texels, x fastest
+struct texture_storage_3d_r32f {
+  float *data = nullptr;
+  u32 dim = 0;
+};
+inline void textureStore(texture_storage_3d_r32f &t, vec3<i32> c, vec4<f32> v) {
+  t.data[size_t(c.x) + size_t(t.dim) * (size_t(c.y) + size_t(t.dim) * size_t(c.z))] = v.x;
+}
 struct vec4r {
   float r;
 };
@@ -240,6 +264,19 @@ inline void dispatch_sequential(u32 groups, u32 wg_size,
                                 const std::function<void(uvec3, uvec3, uvec3)> &fn) {
   for (u32 g = 0; g < groups; g++)
     for (u32 l = 0; l < wg_size; l++) fn(uvec3(g * wg_size + l, 0u, 0u), uvec3(l, 0u, 0u), uvec3(g, 0u, 0u));
+}
+
+// 3-D dispatch, invocations one at a time (no barriers in the shader).
+inline void dispatch_sequential_3d(u32 gx, u32 gy, u32 gz, uvec3 wg,
+                                   const std::function<void(uvec3, uvec3, uvec3)> &fn) {
+  for (u32 z = 0; z < gz; z++)
+    for (u32 y = 0; y < gy; y++)
+      for (u32 x = 0; x < gx; x++)
+        for (u32 lz = 0; lz < wg.z; lz++)
+          for (u32 ly = 0; ly < wg.y; ly++)
+            for (u32 lx = 0; lx < wg.x; lx++)
+              fn(uvec3(x * wg.x + lx, y * wg.y + ly, z * wg.z + lz), uvec3(lx, ly, lz),
+                 uvec3(x, y, z));
 }
 
 // Shaders with workgroupBarrier(): every function that reaches a barrier is

@@ -91,6 +91,25 @@ static_assert(sizeof(MouseF) == 48, "mouse");
 static_assert(sizeof(RigidF) == 96, "rigid");
 static_assert(sizeof(AccumI) == 32, "accum");
 static_assert(sizeof(GridF) == 48, "grid");
+struct McGridF {  // GpuGridParams of the MC renderer, src/render/marching_cubes.rs:56-66
+  float grid_min[3];
+  uint32_t grid_size;
+  float grid_max[3];
+  float cell_size, kernel_radius, iso_value;
+  uint32_t num_particles, max_vertices;
+};
+static_assert(sizeof(McGridF) == 48, "mc grid");
+
+// WGSL pow(x, n.0) for an integral n >= 1: binary exponentiation in double,
+// rounded once (the library's definition; WGSL leaves pow's precision open).
+inline double pow_int_d(double x, unsigned n) {
+  double r = 1.0, b = x;
+  for (; n; n >>= 1) {
+    if (n & 1u) r *= b;
+    b *= b;
+  }
+  return r;
+}
 
 // ---- small vector type: every operator is one IEEE op per component --------
 template <class R>
@@ -805,6 +824,85 @@ struct Oracle {
     p.st = R(q.surface_tension); p.delta = R(q.pcisph_delta); p.xsph_eps = R(q.xsph_epsilon);
     grid.num_particles = p.n;  // update_sph_params keeps both counts in sync
   }
+  // mc_density.wgsl:130-231, isotropic path (anisotropy off): the poly6
+  // density of the sorted positions S at the centres of gs^3 voxels (x
+  // fastest), over the SPH cells within ceil(h / cell) of the voxel's
+  // unclamped cell in dz, dy, dx, slot order; -1 outside the box when
+  // clipping; else divided by the five-wall gamma (mc_density.wgsl:110-128).
+  // The cell radius is an index quantity and is taken in f32 at any R.
+  void density_splat(const McGridF &mc, const GeomF &cgf, double *out) const {
+    Geom<R> cg;
+    cg.hw = R(cgf.half_width); cg.hh = R(cgf.half_height); cg.hd = R(cgf.half_depth);
+    cg.cy = R(cgf.center_y);
+    cg.i0 = from4<R>(cgf.i0); cg.i1 = from4<R>(cgf.i1); cg.i2 = from4<R>(cgf.i2);
+    const uint32_t gs = mc.grid_size;
+    const R h = R(mc.kernel_radius);
+    const R h_sq = h * h;
+    const R pow9 = sizeof(R) == 4 ? R(float(pow_int_d(double(mc.kernel_radius), 9)))
+                                  : R(pow_int_d(double(mc.kernel_radius), 9));
+    const R coeff = R(315) / (R(64) * R(PI_F) * pow9);
+    const int32_t cr = f2i_sat(double(std::ceil(mc.kernel_radius * grid.inv_cell_size)));
+    const R cs = R(mc.cell_size);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t zi = 0; zi < int64_t(gs); zi++) {
+      const uint32_t z = uint32_t(zi);
+      for (uint32_t y = 0; y < gs; y++)
+        for (uint32_t x = 0; x < gs; x++) {
+          const V3<R> wp{R(mc.grid_min[0]) + (R(float(x)) + R(0.5f)) * cs,
+                         R(mc.grid_min[1]) + (R(float(y)) + R(0.5f)) * cs,
+                         R(mc.grid_min[2]) + (R(float(z)) + R(0.5f)) * cs};
+          int32_t c[3];
+          position_to_cell(wp, c);
+          R density = R(0);
+          for (int32_t dz = -cr; dz <= cr; dz++)
+            for (int32_t dy = -cr; dy <= cr; dy++)
+              for (int32_t dx = -cr; dx <= cr; dx++) {
+                const int64_t nx = int64_t(c[0]) + dx, ny = int64_t(c[1]) + dy,
+                              nz = int64_t(c[2]) + dz;
+                if (nx < 0 || nx >= int64_t(grid.gx) || ny < 0 || ny >= int64_t(grid.gy) ||
+                    nz < 0 || nz >= int64_t(grid.gz))
+                  continue;
+                const uint32_t idx = uint32_t(nx) + uint32_t(ny) * grid.gx +
+                                     uint32_t(nz) * grid.gx * grid.gy;
+                const uint32_t count = counts[idx];
+                const uint32_t start = starts[idx] - count;
+                for (uint32_t k = 0; k < count; k++) {
+                  const V3<R> d = wp - S[start + k].pos;
+                  const R r_sq = dot3(d, d);
+                  if (r_sq < h_sq) {
+                    const R diff = h_sq - r_sq;
+                    density += coeff * diff * diff * diff;
+                  }
+                }
+              }
+          const V3<R> q{wp.x, wp.y - cg.cy, wp.z};
+          const V3<R> l{dot3(cg.i0, q), dot3(cg.i1, q), dot3(cg.i2, q)};
+          double &o = out[size_t(x) + size_t(gs) * (size_t(y) + size_t(gs) * z)];
+          if (cgf.clip_enabled != 0u &&
+              !(l.x >= -cg.hw && l.x <= cg.hw && l.y >= -cg.hh && l.y <= cg.hh &&
+                l.z >= -cg.hd && l.z <= cg.hd)) {
+            o = -1.0;
+            continue;
+          }
+          R gamma = R(1);
+          const R dnx = l.x + cg.hw, dpx = cg.hw - l.x, dfl = l.y + cg.hh;
+          const R dnz = l.z + cg.hd, dpz = cg.hd - l.z;
+          auto fac = [&](R dd) {
+            R t = dd / h;
+            t = std::min(std::max(t, R(0)), R(1));
+            return R(0.5f) + R(0.5f) * t;
+          };
+          if (dnx < h) gamma *= fac(dnx);
+          if (dpx < h) gamma *= fac(dpx);
+          if (dfl < h) gamma *= fac(dfl);
+          if (dnz < h) gamma *= fac(dnz);
+          if (dpz < h) gamma *= fac(dpz);
+          gamma = std::max(gamma, R(0.15f));
+          o = double(density / gamma);
+        }
+    }
+  }
+
   void set_geom(const GeomF &q) {
     geom.hw = R(q.half_width); geom.hh = R(q.half_height); geom.hd = R(q.half_depth);
     geom.cy = R(q.center_y);
@@ -1046,6 +1144,12 @@ void or_sincos_f32(const float *x, float *s, float *c, uint32_t n) {
 void or_get_grid(void *hv, void *out) {
   auto *h = (Handle *)hv;
   DISPATCH(h, std::memcpy(out, &o->grid, sizeof(GridF)));
+}
+
+// The MC density field of the last step's sorted positions (gs^3 doubles).
+void or_density_splat(void *hv, const void *mc, const void *geom, double *out) {
+  auto *h = (Handle *)hv;
+  DISPATCH(h, o->density_splat(*(const McGridF *)mc, *(const GeomF *)geom, out));
 }
 
 }  // extern "C"

@@ -143,6 +143,8 @@ class Translator:
             args = [self.type_text(a) for a in args]
             if name == "atomic":
                 return args[0]
+            if name == "texture_storage_3d":  # only r32float write volumes occur
+                return "texture_storage_3d_r32f"
             if name == "array":
                 if len(args) == 1:
                     return f"__runtime_array<{args[0]}>"
@@ -493,10 +495,11 @@ class Translator:
                 plist.append(f"{ptype} {pname}")
         fname = f"{name}"
         if is_entry:
-            wg = 1
+            wg = (1, 1, 1)
             for a, args in attrs:
                 if a == "@workgroup_size":
-                    wg = int(re.sub(r"[iu]$", "", args[0]))
+                    dims = [int(re.sub(r"[iu]$", "", x)) for x in args if x != ","]
+                    wg = tuple(dims + [1] * (3 - len(dims)))
             self.entries.append((name, wg))
             sig = f"void {fname}(uvec3 __gid, uvec3 __lid, uvec3 __wid)"
             prelude = []
@@ -520,7 +523,15 @@ class Translator:
     def render(self) -> str:
         out = [f"namespace {self.ns} {{", "using namespace wgsl;"]
         out += self.structs + self.consts + self.globals + self.fn_decls + self.fn_defs
-        for name, wg in self.entries:
+        for name, wg3 in self.entries:
+            if wg3[1] != 1 or wg3[2] != 1:
+                assert name not in self.coroutines, "3-D workgroups with barriers"
+                out.append(
+                    f"inline void dispatch_{name}(u32 gx, u32 gy, u32 gz) {{\n"
+                    f"  dispatch_sequential_3d(gx, gy, gz, uvec3({wg3[0]}u, {wg3[1]}u, {wg3[2]}u),\n"
+                    f"                         [](uvec3 g, uvec3 l, uvec3 w) {{ {name}(g, l, w); }});\n}}")
+                continue
+            wg = wg3[0]
             if name in self.coroutines:
                 resets = " ".join(f"{v} = {{}};" for v in self.workgroup_vars)
                 out.append(
