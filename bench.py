@@ -459,6 +459,85 @@ def run_batch(args, dist: Dist) -> dict | None:
     }
 
 
+def run_adjoint(args, dist: Dist) -> dict | None:
+    """The differentiable rollout: forward-only ms/step (graph-replayed steps)
+    against forward + reverse ms/step (fs_adj_forward with checkpoints every
+    20 steps, the density-splat loss, fs_adj_backward), same workload."""
+    import torch
+    from fluidsph import scenes as S
+    from fluidsph.adjoint import DifferentiableRollout
+    from fluidsph.sim import SphSimulation3DGrid
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    sc = S.config3()
+    T = args.steps
+    every = 20
+    mc = S.loss_grid(sc)
+
+    def fresh(sph=None):
+        sim = SphSimulation3DGrid(sc.particles, sph or sc.sph, sc.geom, device=dev)
+        sim.update_gravity(sc.gravity)
+        sim.set_pcisph_iterations(sc.iterations)
+        return sim
+
+    hidden_p = type(sc.sph).from_buffer_copy(sc.sph)
+    hidden_p.viscosity, hidden_p.stiffness = 12.0, 30.0
+    hidden = fresh(hidden_p)
+    hidden.step(T)
+    target = hidden.density_splat(mc, sc.geom)  # the hidden run's field
+    hidden.close()
+
+    stream = torch.cuda.Stream(device=dev)
+    sim = fresh()
+    sim.set_stream(stream.cuda_stream)
+    sim.prepare_steps(T)
+    sim.step(args.warmup)
+    sim.upload_particles(sc.particles)
+    sim.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    sim.step(T)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    fwd_ms = e0.elapsed_time(e1) / T
+
+    r = DifferentiableRollout(sim, every)
+    sim.upload_particles(sc.particles)
+    r.forward(T)  # warm-up of the recording path
+    r.splat_mse_loss(mc, sc.geom, target)
+    r.backward()
+    sim.upload_particles(sc.particles)
+    sim.sync()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    r.forward(T)
+    loss = r.splat_mse_loss(mc, sc.geom, target)
+    dpos, dvel, dpar = r.backward()
+    torch.cuda.synchronize(dev)
+    total_ms = (time.perf_counter() - t0) * 1e3 / T
+    finite = bool(np.isfinite(dvel).all() and np.isfinite(dpar).all())
+    r.close()
+    sim.close()
+    if dist.rank != 0:
+        return None
+    return {
+        "metric": "fwd+adjoint ms/step", "value": round(total_ms, 4), "unit": "ms/step",
+        "n_gpus": dist.world, "steps": T, "warmup": args.warmup, "ms_per_step": round(total_ms, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded lattice, 8-mode Fourier initial velocity)",
+        "config": {"workload": sc.name, "particles": sc.n, "steps": T, "checkpoint_every": every,
+                   "loss": "MSE of the 64^3 density splat against a hidden run "
+                           "(viscosity 12, stiffness 30)"},
+        "forward_ms_per_step": round(fwd_ms, 4),
+        "fwd_adjoint_over_forward": round(total_ms / fwd_ms, 3),
+        "loss": loss, "gradient_finite": finite,
+        "grad_params": {"viscosity": float(dpar[0, 0]), "stiffness": float(dpar[0, 1]),
+                        "surface_tension": float(dpar[0, 2])},
+    }
+
+
 def run_reference(args, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
@@ -512,7 +591,12 @@ def main():
             if dist.local_rank == 0:
                 build_library()
             dist.barrier()
-            out = run_batch(args, dist) if args.config == 2 else run_ours(args, dist)
+            if args.config == 2:
+                out = run_batch(args, dist)
+            elif args.config == 3:
+                out = run_adjoint(args, dist)
+            else:
+                out = run_ours(args, dist)
         if out is not None:
             print(json.dumps(out), flush=True)
     finally:

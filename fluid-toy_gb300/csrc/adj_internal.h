@@ -1,0 +1,49 @@
+// adj_internal.h — types shared by the reverse pass's host side (adjoint.cu)
+// and its kernels (adj_kernels.cu).
+#pragma once
+
+#include "fs_internal.h"
+
+namespace fs {
+
+constexpr int kMaxAdjIters = 16;  // PCISPH iterations a recorded step may hold
+
+// One recorded forward step, grid-sorted order (the buffers the step's
+// kernels wrote, see enqueue_step with a DevState override).
+struct TapeView {
+  const uint32_t *s2o;
+  const uint16_t *scene_of_slot;
+  const uint32_t *cell_begin;  // [cells + 1], global slot numbers
+  const float4 *pos, *vel, *nrm, *vhat, *anp, *vfin;
+  const float2 *dens;
+  const float4 *xp[kMaxAdjIters + 1];  // predicted (x*, p) per level
+  const float *rho[kMaxAdjIters + 1];  // predicted densities per level
+  const float4 *ap[kMaxAdjIters];      // pressure acceleration before the clamp
+};
+
+// Reverse accumulators, grid-sorted order.
+struct AdjView {
+  float4 *gx;     // d/d position
+  float4 *gvhat;  // d/d post-XSPH velocity
+  float4 *gv;     // d/d pre-XSPH velocity (the step's input velocity)
+  float4 *ga;     // d/d non-pressure acceleration
+  float4 *gn;     // d/d Akinci normal
+  float2 *grho;   // d/d density (raw, after the XSPH reverse), d/d near density
+  float *gp;      // d/d pressure carried between PCISPH levels
+  float4 *gu[2];  // per level: d/d pressure acceleration (pre-clamp), d/d next density
+  double *gparam; // [scenes][3]: viscosity, stiffness, surface_tension (FP64)
+  uint32_t *err;
+};
+
+cudaError_t launch_adj_step(const SceneView &v, const TapeView &t, const AdjView &a,
+                            const float4 *xbar_in, const float4 *vbar_in, float4 *xbar_out,
+                            float4 *vbar_out, const float4 *dir_tab, int dir_half, uint32_t n,
+                            int K, cudaStream_t st);
+cudaError_t launch_splat_mse(const SplatArgs &sa, const float *field, const float *target,
+                             float *gg, double *loss, cudaStream_t st);
+cudaError_t launch_rows_to_f4(uint32_t n, const float *rows, float4 *out, cudaStream_t st);
+cudaError_t launch_f4_to_rows(uint32_t n, const float4 *in, float *rows, cudaStream_t st);
+cudaError_t launch_splat_adjoint(const SplatArgs &sa, uint32_t n, const float4 *pos,
+                                 const float *gg, float4 *xbar, cudaStream_t st);
+
+}  // namespace fs

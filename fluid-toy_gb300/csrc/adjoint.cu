@@ -1,0 +1,461 @@
+// adjoint.cu — the differentiable rollout behind fs_adj_* (include/fluidsph.h).
+//
+// No counterpart in the reference: it differentiates SphSimulation3DGrid's
+// step (sph_3d_grid.rs:1261-1444) with respect to the initial state and the
+// viscosity / surface-tension parameters. Forward records: it runs the steps
+// on the simulation's graphs and keeps the canonical state (x, v) every
+// `checkpoint_every` steps. Backward consumes cotangents of the final state:
+// segment by segment from the last, it restores the segment's checkpoint,
+// re-runs its steps once more while recording each step's intermediates (the
+// sorted state, densities, normals, XSPH velocities, accelerations and every
+// PCISPH level) into a tape, then reverses the recorded steps one by one
+// with the kernels of adj_kernels.cu. Memory: the checkpoints, one segment of
+// tape and the reverse accumulators.
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "adj_internal.h"
+#include "fs_sim.h"
+
+using namespace fs;
+
+namespace {
+
+struct TapeSlot {
+  uint32_t *s2o;
+  uint16_t *sos;
+  uint32_t *cell_begin;
+  float4 *pos, *vel, *nrm, *vhat, *anp, *vfin;
+  float2 *dens;
+  float4 *xp[kMaxAdjIters + 1];
+  float *rho[kMaxAdjIters + 1];
+  float4 *ap[kMaxAdjIters];
+};
+
+size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Carve {
+  char *base;
+  size_t off = 0;
+  template <class T>
+  T *take(size_t count) {
+    T *p = reinterpret_cast<T *>(base ? base + off : nullptr);
+    off += a256(sizeof(T) * std::max<size_t>(count, 1));
+    return p;
+  }
+};
+
+}  // namespace
+
+struct FsAdj {
+  FsSim *sim = nullptr;
+  uint32_t every = 1;
+  // shape at recording
+  uint32_t K = 0, N = 0, G = 0, scenes = 0;
+  uint32_t steps = 0;
+  std::vector<DevUniforms> hu_snapshot;
+  // checkpoints [nck][2][N] and the final state [2][N]
+  float4 *ck = nullptr;
+  size_t ck_slots = 0;
+  float4 *final_state = nullptr;
+  // one segment of tape + reverse accumulators + cotangents
+  void *work = nullptr;
+  size_t work_bytes = 0;
+  uint32_t work_N = 0, work_G = 0, work_K = 0, work_every = 0, work_scenes = 0;
+  std::vector<TapeSlot> tape;
+  AdjView av{};
+  float4 *cot[2][2] = {};  // [buffer][0 = d/d pos, 1 = d/d vel], canonical
+  int cur = 0;
+  bool seeded = false;
+  // loss scratch
+  float *field = nullptr, *target = nullptr, *gg = nullptr;
+  double *loss = nullptr;
+  size_t vox_cap = 0;
+};
+
+namespace {
+
+void free_adj(FsAdj *a) {
+  if (a->ck) cudaFree(a->ck);
+  if (a->final_state) cudaFree(a->final_state);
+  if (a->work) cudaFree(a->work);
+  if (a->field) cudaFree(a->field);
+  a->ck = a->final_state = nullptr;
+  a->work = nullptr;
+  a->field = nullptr;
+}
+
+// Lay out (or size, when base == nullptr) the tape, accumulators and cotangents.
+void carve_work(FsAdj *a, char *base, size_t *bytes) {
+  Carve c{base};
+  const size_t N = a->N, G = a->G;
+  a->tape.assign(a->every, TapeSlot{});
+  for (TapeSlot &t : a->tape) {
+    t.s2o = c.take<uint32_t>(N);
+    t.sos = c.take<uint16_t>(N);
+    t.cell_begin = c.take<uint32_t>(G + 1);
+    t.pos = c.take<float4>(N);
+    t.vel = c.take<float4>(N);
+    t.nrm = c.take<float4>(N);
+    t.vhat = c.take<float4>(N);
+    t.anp = c.take<float4>(N);
+    t.vfin = c.take<float4>(N);
+    t.dens = c.take<float2>(N);
+    for (uint32_t k = 0; k <= a->K; k++) {
+      t.xp[k] = c.take<float4>(N);
+      t.rho[k] = c.take<float>(N);
+    }
+    for (uint32_t k = 0; k < a->K; k++) t.ap[k] = c.take<float4>(N);
+  }
+  AdjView &v = a->av;
+  v.gx = c.take<float4>(N);
+  v.gvhat = c.take<float4>(N);
+  v.gv = c.take<float4>(N);
+  v.ga = c.take<float4>(N);
+  v.gn = c.take<float4>(N);
+  v.grho = c.take<float2>(N);
+  v.gp = c.take<float>(N);
+  v.gu[0] = c.take<float4>(N);
+  v.gu[1] = c.take<float4>(N);
+  v.gparam = c.take<double>(3 * size_t(a->scenes));
+  for (auto &b : a->cot)
+    for (auto &p : b) p = c.take<float4>(N);
+  *bytes = c.off;
+}
+
+int ensure_work(FsAdj *a) {
+  if (a->work && a->work_N == a->N && a->work_G == a->G && a->work_K == a->K &&
+      a->work_every == a->every && a->work_scenes == a->scenes)
+    return FS_OK;
+  FsSim *s = a->sim;
+  if (a->work) {
+    FS_CUDA(cudaStreamSynchronize(s->stream), "adjoint workspace");
+    cudaFree(a->work);
+    a->work = nullptr;
+  }
+  carve_work(a, nullptr, &a->work_bytes);
+  FS_CUDA(cudaMalloc(&a->work, a->work_bytes), "allocate adjoint workspace");
+  carve_work(a, static_cast<char *>(a->work), &a->work_bytes);
+  // cell_begin[0] of every slot must read 0 (the scan writes from index 1)
+  FS_CUDA(cudaMemsetAsync(a->work, 0, a->work_bytes, s->stream), "clear adjoint workspace");
+  a->av.err = s->d.err;
+  a->work_N = a->N;
+  a->work_G = a->G;
+  a->work_K = a->K;
+  a->work_every = a->every;
+  a->work_scenes = a->scenes;
+  return FS_OK;
+}
+
+// The simulation's buffers with the step's outputs redirected into slot t.
+DevState recording_state(const FsAdj *a, const TapeSlot &t) {
+  DevState dv = a->sim->d;
+  dv.s2o = t.s2o;
+  dv.scene_of_slot = t.sos;
+  dv.cell_begin = t.cell_begin;
+  dv.s_pos = t.pos;
+  dv.s_vel = t.vel;
+  dv.s_nrm = t.nrm;
+  dv.s_dens = t.dens;
+  dv.vel_x = t.vhat;
+  dv.anp = t.anp;
+  dv.pred_v = t.vfin;
+  dv.rec_xp = t.xp;
+  dv.rec_rho = t.rho;
+  dv.rec_ap = t.ap;
+  return dv;
+}
+
+TapeView tape_view(const TapeSlot &t, uint32_t K) {
+  TapeView v{};
+  v.s2o = t.s2o;
+  v.scene_of_slot = t.sos;
+  v.cell_begin = t.cell_begin;
+  v.pos = t.pos;
+  v.vel = t.vel;
+  v.nrm = t.nrm;
+  v.vhat = t.vhat;
+  v.anp = t.anp;
+  v.vfin = t.vfin;
+  v.dens = t.dens;
+  for (uint32_t k = 0; k <= K; k++) {
+    v.xp[k] = t.xp[k];
+    v.rho[k] = t.rho[k];
+  }
+  for (uint32_t k = 0; k < K; k++) v.ap[k] = t.ap[k];
+  return v;
+}
+
+int copy_state(FsSim *s, float4 *dst_pos, float4 *dst_vel, const float4 *src_pos,
+               const float4 *src_vel, uint32_t n) {
+  FS_CUDA(cudaMemcpyAsync(dst_pos, src_pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice,
+                          s->stream),
+          "copy state");
+  FS_CUDA(cudaMemcpyAsync(dst_vel, src_vel, sizeof(float4) * n, cudaMemcpyDeviceToDevice,
+                          s->stream),
+          "copy state");
+  return FS_OK;
+}
+
+// What the reverse pass differentiates: every particle active, mouse force
+// and rigid body off, at most kMaxAdjIters PCISPH iterations.
+int check_supported(const char *who, FsSim *s) {
+  if (s->iterations > uint32_t(kMaxAdjIters))
+    return fail(FS_E_STATE, "%s: %u PCISPH iterations (at most %d are differentiated)", who,
+                s->iterations, kMaxAdjIters);
+  if (s->hb.n_sorted != s->hb.n_canon)
+    return fail(FS_E_STATE, "%s: every particle must be active (num_particles >= count)", who);
+  for (uint32_t k = 0; k < s->scenes(); k++) {
+    if (s->hu[k].mouse.is_active == 1u)
+      return fail(FS_E_STATE, "%s: scene %u: the mouse force is not differentiated", who, k);
+    if (s->hu[k].rigid.is_active != 0u)
+      return fail(FS_E_STATE, "%s: scene %u: the rigid-body coupling is not differentiated", who,
+                  k);
+  }
+  return FS_OK;
+}
+
+#define CHECK_ADJ(a) \
+  if (!(a) || !(a)->sim) return fail(FS_E_INVALID_ARGUMENT, "%s: null handle", __func__)
+
+}  // namespace
+
+extern "C" {
+
+int fs_adj_create(FsSim *sim, uint32_t checkpoint_every, FsAdj **out) {
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_adj_create: out is null");
+  *out = nullptr;
+  if (!sim) return fail(FS_E_INVALID_ARGUMENT, "fs_adj_create: null simulation");
+  if (checkpoint_every == 0 || checkpoint_every > 4096)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_create: checkpoint_every %u outside [1, 4096]",
+                checkpoint_every);
+  FsAdj *a = new (std::nothrow) FsAdj();
+  if (!a) return fail(FS_E_CAPACITY, "fs_adj_create: out of host memory");
+  a->sim = sim;
+  a->every = checkpoint_every;
+  *out = a;
+  return FS_OK;
+}
+
+int fs_adj_destroy(FsAdj *a) {
+  if (!a) return FS_OK;
+  if (a->sim) {
+    cudaSetDevice(a->sim->device);
+    cudaStreamSynchronize(a->sim->stream);
+  }
+  free_adj(a);
+  delete a;
+  return FS_OK;
+}
+
+int fs_adj_forward(FsAdj *a, uint32_t nsteps) {
+  CHECK_ADJ(a);
+  FsSim *s = a->sim;
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if ((rc = check_supported(__func__, s))) return rc;
+  a->K = s->iterations;
+  a->N = s->hb.n_canon;
+  a->G = s->cells_total;
+  a->scenes = s->scenes();
+  a->hu_snapshot = s->hu;
+  a->steps = 0;
+  a->seeded = false;
+  const uint32_t nck = (nsteps + a->every - 1) / a->every;
+  const size_t need = std::max<size_t>(nck, 1) * 2 * size_t(a->N);
+  if (a->ck_slots < need) {
+    if (a->ck) {
+      FS_CUDA(cudaStreamSynchronize(s->stream), "checkpoints");
+      cudaFree(a->ck);
+      a->ck = nullptr;
+    }
+    FS_CUDA(cudaMalloc(&a->ck, sizeof(float4) * need), "allocate checkpoints");
+    a->ck_slots = need;
+    if (a->final_state) cudaFree(a->final_state);
+    a->final_state = nullptr;
+  }
+  if (!a->final_state)
+    FS_CUDA(cudaMalloc(&a->final_state, sizeof(float4) * 2 * std::max<size_t>(a->N, 1)),
+            "allocate final state");
+  if ((rc = ensure_work(a))) return rc;
+  for (uint32_t c = 0; c < nck; c++) {
+    float4 *ck = a->ck + size_t(c) * 2 * a->N;
+    if ((rc = copy_state(s, ck, ck + a->N, s->d.p_pos, s->d.p_vel, a->N))) return rc;
+    const uint32_t len = std::min(a->every, nsteps - c * a->every);
+    if ((rc = fs_step(s, len))) return rc;
+  }
+  if ((rc = copy_state(s, a->final_state, a->final_state + a->N, s->d.p_pos, s->d.p_vel, a->N)))
+    return rc;
+  for (int b = 0; b < 2; b++)
+    FS_CUDA(cudaMemsetAsync(a->cot[a->cur][b], 0, sizeof(float4) * a->N, s->stream),
+            "clear cotangents");
+  a->steps = nsteps;
+  return FS_OK;
+}
+
+int fs_adj_set_cotangents(FsAdj *a, const float *dl_dpos, const float *dl_dvel, int on_device) {
+  CHECK_ADJ(a);
+  FsSim *s = a->sim;
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (!a->work) return fail(FS_E_STATE, "fs_adj_set_cotangents: no recorded rollout");
+  const float *src[2] = {dl_dpos, dl_dvel};
+  for (int b = 0; b < 2; b++) {
+    float4 *dst = a->cot[a->cur][b];
+    if (!src[b]) {
+      FS_CUDA(cudaMemsetAsync(dst, 0, sizeof(float4) * a->N, s->stream), "clear cotangent");
+    } else if (on_device) {
+      FS_CUDA(launch_rows_to_f4(a->N, src[b], dst, s->stream), "cotangent rows");
+    } else {
+      std::vector<float4> h(a->N);
+      for (uint32_t i = 0; i < a->N; i++)
+        h[i] = make_float4(src[b][3 * size_t(i)], src[b][3 * size_t(i) + 1],
+                           src[b][3 * size_t(i) + 2], 0.0f);
+      FS_CUDA(cudaMemcpyAsync(dst, h.data(), sizeof(float4) * a->N, cudaMemcpyHostToDevice,
+                              s->stream),
+              "upload cotangent");
+      FS_CUDA(cudaStreamSynchronize(s->stream), "upload cotangent");
+    }
+  }
+  a->seeded = true;
+  return FS_OK;
+}
+
+int fs_adj_splat_mse_loss(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
+                          const GpuContainerGeometry *geom, const float *target,
+                          int target_on_device, double *loss_out) {
+  CHECK_ADJ(a);
+  FsSim *s = a->sim;
+  if (!grid || !geom || !target || !loss_out)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: null argument");
+  if (scene >= s->scenes())
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: scene %u of %u", scene,
+                s->scenes());
+  if (!a->work) return fail(FS_E_STATE, "fs_adj_splat_mse_loss: no recorded rollout");
+  if (grid->grid_size == 0 || grid->grid_size > 1024)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: grid_size %u outside [1, 1024]",
+                grid->grid_size);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  const size_t vox = size_t(grid->grid_size) * grid->grid_size * grid->grid_size;
+  if (a->vox_cap < vox) {
+    FS_CUDA(cudaStreamSynchronize(s->stream), "loss scratch");
+    if (a->field) cudaFree(a->field);
+    a->field = nullptr;
+    const size_t bytes = a256(sizeof(float) * vox) * 3 + 256;
+    char *p = nullptr;
+    FS_CUDA(cudaMalloc(&p, bytes), "allocate loss scratch");
+    a->field = reinterpret_cast<float *>(p);
+    a->target = reinterpret_cast<float *>(p + a256(sizeof(float) * vox));
+    a->gg = reinterpret_cast<float *>(p + 2 * a256(sizeof(float) * vox));
+    a->loss = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox));
+    a->vox_cap = vox;
+  }
+  const DevUniforms &u = s->hu[scene];
+  const SplatArgs sa = make_splat_args(*grid, *geom, u.grid);
+  if (sa.cell_radius < 1 || sa.cell_radius > 8)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: splat radius spans %d cells",
+                sa.cell_radius);
+  // the final positions, grid-sorted, then the density pass
+  if ((rc = enqueue_grid_build(s))) return rc;
+  FS_CUDA(launch_density_splat(sa, s->d.s_pos, s->d.cell_begin + u.c_offset, a->field,
+                               s->stream),
+          "loss splat");
+  FS_CUDA(cudaMemcpyAsync(a->target, target, sizeof(float) * vox,
+                          target_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                          s->stream),
+          "upload target");
+  FS_CUDA(cudaMemsetAsync(a->loss, 0, sizeof(double), s->stream), "clear loss");
+  FS_CUDA(launch_splat_mse(sa, a->field, a->target, a->gg, a->loss, s->stream), "loss");
+  FS_CUDA(launch_splat_adjoint(sa, s->scene_n[scene], s->d.p_pos + u.p_offset, a->gg,
+                               a->cot[a->cur][0] + u.p_offset, s->stream),
+          "loss adjoint");
+  FS_CUDA(cudaMemsetAsync(a->cot[a->cur][1] + u.p_offset, 0, sizeof(float4) * s->scene_n[scene],
+                          s->stream),
+          "clear velocity cotangent");
+  FS_CUDA(cudaMemcpyAsync(loss_out, a->loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream),
+          "read loss");
+  if ((rc = check_device_error(s))) return rc;
+  a->seeded = true;
+  return FS_OK;
+}
+
+int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
+                    double *dl_dparams) {
+  CHECK_ADJ(a);
+  FsSim *s = a->sim;
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (!a->work) return fail(FS_E_STATE, "fs_adj_backward: no recorded rollout");
+  if (!a->seeded) return fail(FS_E_STATE, "fs_adj_backward: no cotangents (set them or a loss)");
+  if (s->iterations != a->K || s->hb.n_canon != a->N || s->scenes() != a->scenes ||
+      std::memcmp(s->hu.data(), a->hu_snapshot.data(), sizeof(DevUniforms) * a->scenes) != 0)
+    return fail(FS_E_STATE, "fs_adj_backward: parameters changed since fs_adj_forward");
+  const uint32_t N = a->N, K = a->K;
+  FS_CUDA(cudaMemsetAsync(a->av.gparam, 0, sizeof(double) * 3 * a->scenes, s->stream),
+          "clear parameter gradients");
+  const uint32_t nck = (a->steps + a->every - 1) / a->every;
+  const SceneView base = s->d.view();
+  for (uint32_t seg = nck; seg-- > 0;) {
+    const float4 *ck = a->ck + size_t(seg) * 2 * N;
+    if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, ck, ck + N, N))) return rc;
+    const uint32_t len = std::min(a->every, a->steps - seg * a->every);
+    for (uint32_t t = 0; t < len; t++) {
+      const DevState dv = recording_state(a, a->tape[t]);
+      if ((rc = enqueue_step(s, false, &dv))) return rc;
+    }
+    for (uint32_t t = len; t-- > 0;) {
+      const TapeSlot &slot = a->tape[t];
+      SceneView v = base;
+      v.scene_of_slot = slot.sos;
+      const int nxt = a->cur ^ 1;
+      FS_CUDA(launch_adj_step(v, tape_view(slot, K), a->av, a->cot[a->cur][0], a->cot[a->cur][1],
+                              a->cot[nxt][0], a->cot[nxt][1], s->d.dir_tab, s->d.dir_half, N,
+                              int(K), s->stream),
+              "reverse step");
+      a->cur = nxt;
+    }
+  }
+  // outputs
+  const float4 *g[2] = {a->cot[a->cur][0], a->cot[a->cur][1]};
+  float *outs[2] = {dl_dpos0, dl_dvel0};
+  std::vector<float4> host(N);
+  for (int b = 0; b < 2; b++) {
+    if (!outs[b]) continue;
+    if (on_device) {
+      FS_CUDA(launch_f4_to_rows(N, g[b], outs[b], s->stream), "gradient rows");
+    } else {
+      FS_CUDA(cudaMemcpyAsync(host.data(), g[b], sizeof(float4) * N, cudaMemcpyDeviceToHost,
+                              s->stream),
+              "download gradient");
+      FS_CUDA(cudaStreamSynchronize(s->stream), "download gradient");
+      for (uint32_t i = 0; i < N; i++) {
+        outs[b][3 * size_t(i)] = host[i].x;
+        outs[b][3 * size_t(i) + 1] = host[i].y;
+        outs[b][3 * size_t(i) + 2] = host[i].z;
+      }
+    }
+  }
+  if (dl_dparams)
+    FS_CUDA(cudaMemcpyAsync(dl_dparams, a->av.gparam, sizeof(double) * 3 * a->scenes,
+                            cudaMemcpyDeviceToHost, s->stream),
+            "download parameter gradients");
+  // leave the simulation at the rollout's final state
+  if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, a->final_state, a->final_state + N, N)))
+    return rc;
+  uint32_t err = 0;
+  FS_CUDA(cudaMemcpyAsync(&err, s->d.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream),
+          "read error word");
+  FS_CUDA(cudaStreamSynchronize(s->stream), "backward");
+  if (err & ERR_ADJ_OUTSIDE_GRID) {
+    FS_CUDA(cudaMemset(s->d.err, 0, sizeof(uint32_t)), "clear error word");
+    return fail(FS_E_STATE, "fs_adj_backward: a particle left the grid (neighbour sets are "
+                            "then not symmetric); the gradient is not valid");
+  }
+  if ((rc = check_device_error(s))) return rc;
+  a->seeded = false;
+  return FS_OK;
+}
+
+}  // extern "C"

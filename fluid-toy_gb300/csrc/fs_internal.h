@@ -58,7 +58,8 @@ enum StatIndex : int {
 
 // Device error word bits.
 enum ErrorBits : uint32_t {
-  ERR_SCAN_TIMEOUT = 1u,  // decoupled-lookback poll limit reached
+  ERR_SCAN_TIMEOUT = 1u,      // decoupled-lookback poll limit reached
+  ERR_ADJ_OUTSIDE_GRID = 2u,  // reverse pass: a particle's cell outside the grid
 };
 
 // Particle state in HBM: structure-of-arrays, one 16-byte record per particle
@@ -111,6 +112,12 @@ struct DevState {
   uint16_t *scene_of;       // canonical particle -> scene
   uint16_t *scene_of_slot;  // sorted slot -> scene
   SceneView view() const { return SceneView{u, b, scene_of, scene_of_slot}; }
+  // Recording of the PCISPH levels for the reverse pass; null = ping-pong in
+  // pred_xp/pred_rho. Host arrays of device pointers: level k holds the
+  // predicted (x*, p) and densities read by iteration k (level 0 = predict).
+  float4 *const *rec_xp = nullptr;   // [iterations + 1]
+  float *const *rec_rho = nullptr;   // [iterations + 1]
+  float4 *const *rec_ap = nullptr;   // [iterations] pressure acceleration before the clamp
 };
 
 // Set the thread-local text fs_last_error() returns (sim.cu).

@@ -1,0 +1,76 @@
+// fs_sim.h — the simulation object behind the C ABI (sim.cu) and the host
+// helpers shared with the reverse pass (adjoint.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "fs_internal.h"
+
+namespace fs {
+
+// Record fs_last_error's text and return `code`.
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define FS_CUDA(call, what)                                   \
+  do {                                                        \
+    cudaError_t e__ = (call);                                 \
+    if (e__ != cudaSuccess) return ::fs::cuda_fail(e__, what); \
+  } while (0)
+
+// Step graphs: one captured graph per step count, a few kept.
+constexpr uint32_t kMaxGraphSteps = 256;
+constexpr int kGraphSlots = 4;
+
+struct StepGraph {
+  cudaGraphExec_t exec = nullptr;
+  uint32_t steps = 0, n_canon = 0, n_sorted = 0, iters = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t last_use = 0;
+};
+
+}  // namespace fs
+
+struct FsSim {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  bool batch = false;       // made by fs_batch_create
+  uint32_t max_n = 0;       // canonical capacity
+  uint32_t iterations = 5;  // sph_3d_grid.rs:1253 default
+  uint32_t sdf_res = 1;
+  std::vector<uint32_t> scene_n;  // canonical particles of each scene
+  std::vector<fs::DevUniforms> hu;    // host mirror of the per-scene parameter blocks
+  fs::DevBatch hb{};                  // host mirror of the batch header
+  uint32_t cells_total = 0;
+  fs::DevState d{};
+  void *arena = nullptr;
+  size_t arena_bytes = 0;
+  fs::StepGraph graphs[fs::kGraphSlots];
+  uint64_t graph_clock = 0;
+  float *splat_buf = nullptr;  // device staging of host-bound density fields
+  size_t splat_cap = 0;
+  // stage timing
+  bool timing = false;
+  cudaEvent_t ev[FS_STAGE_COUNT + 1] = {};
+  double stage_ms[FS_STAGE_COUNT] = {};
+  uint32_t timed_steps = 0;
+
+  uint32_t scenes() const { return uint32_t(scene_n.size()); }
+  uint32_t active(uint32_t k) const { return std::min(hu[k].sph.num_particles, scene_n[k]); }
+};
+
+namespace fs {
+
+int set_device(FsSim *s);
+// Synchronise the stream and report a device-side error word, if set.
+int check_device_error(FsSim *s);
+// Enqueue one step on the simulation's stream (on `dv`'s buffers if given).
+int enqueue_step(FsSim *s, bool timed, const DevState *dv = nullptr);
+// Enqueue only the grid build (clear, hash, scan, reorder) of the current state.
+int enqueue_grid_build(FsSim *s);
+
+}  // namespace fs

@@ -23,15 +23,15 @@
 #include <string>
 #include <vector>
 
-#include "fs_internal.h"
+#include "fs_sim.h"
 
 using namespace fs;
 
 namespace {
-
 thread_local std::string g_last_error = "no error";
+}  // namespace
 
-int fail(int code, const char *fmt, ...) {
+int fs::fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -41,15 +41,11 @@ int fail(int code, const char *fmt, ...) {
   return code;
 }
 
-int cuda_fail(cudaError_t e, const char *what) {
+int fs::cuda_fail(cudaError_t e, const char *what) {
   return fail(FS_E_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
-#define FS_CUDA(call, what)                         \
-  do {                                              \
-    cudaError_t e__ = (call);                       \
-    if (e__ != cudaSuccess) return cuda_fail(e__, what); \
-  } while (0)
+namespace {
 
 static_assert(sizeof(SphParticle3D) == 64, "SphParticle3D layout");
 static_assert(sizeof(GpuSphParams3D) == 64, "GpuSphParams3D layout");
@@ -70,46 +66,6 @@ static_assert(FS_BATCH_MAX_SCENES <= 65535u, "scene ids are 16-bit");
 }  // namespace
 
 void fs::set_last_error(const char *msg) { g_last_error = msg; }
-
-// Step graphs: one captured graph per step count, a few kept.
-constexpr uint32_t kMaxGraphSteps = 256;
-constexpr int kGraphSlots = 4;
-
-struct StepGraph {
-  cudaGraphExec_t exec = nullptr;
-  uint32_t steps = 0, n_canon = 0, n_sorted = 0, iters = 0;
-  cudaStream_t stream = nullptr;
-  uint64_t last_use = 0;
-};
-
-struct FsSim {
-  int device = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  bool batch = false;       // made by fs_batch_create
-  uint32_t max_n = 0;       // canonical capacity
-  uint32_t iterations = 5;  // sph_3d_grid.rs:1253 default
-  uint32_t sdf_res = 1;
-  std::vector<uint32_t> scene_n;  // canonical particles of each scene
-  std::vector<DevUniforms> hu;    // host mirror of the per-scene parameter blocks
-  DevBatch hb{};                  // host mirror of the batch header
-  uint32_t cells_total = 0;
-  DevState d{};
-  void *arena = nullptr;
-  size_t arena_bytes = 0;
-  StepGraph graphs[kGraphSlots];
-  uint64_t graph_clock = 0;
-  float *splat_buf = nullptr;  // device staging of host-bound density fields
-  size_t splat_cap = 0;
-  // stage timing
-  bool timing = false;
-  cudaEvent_t ev[FS_STAGE_COUNT + 1] = {};
-  double stage_ms[FS_STAGE_COUNT] = {};
-  uint32_t timed_steps = 0;
-
-  uint32_t scenes() const { return uint32_t(scene_n.size()); }
-  uint32_t active(uint32_t k) const { return std::min(hu[k].sph.num_particles, scene_n[k]); }
-};
 
 namespace {
 
@@ -235,7 +191,9 @@ int upload_scene(FsSim *s, uint32_t k) {
   return FS_OK;
 }
 
-int check_device_error(FsSim *s) {
+}  // namespace
+
+int fs::check_device_error(FsSim *s) {
   uint32_t err = 0;
   FS_CUDA(cudaStreamSynchronize(s->stream), "synchronize");
   FS_CUDA(cudaMemcpy(&err, s->d.err, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read error word");
@@ -247,6 +205,8 @@ int check_device_error(FsSim *s) {
   }
   return FS_OK;
 }
+
+namespace {
 
 // AoS <-> SoA conversion of canonical records on the host.
 void aos_to_soa(const SphParticle3D *in, uint32_t count, std::vector<float4> &pos,
@@ -280,14 +240,17 @@ int write_particles(FsSim *s, const SphParticle3D *parts, uint32_t offset, uint3
   return FS_OK;
 }
 
+}  // namespace
+
 // One step: the stage sequence of step(), sph_3d_grid.rs:1261-1444, over all
-// scenes at once.
-int enqueue_step(FsSim *s, bool timed) {
+// scenes at once, on the simulation's buffers or on `dv` (the same buffers
+// with some replaced, e.g. by a recording for the reverse pass).
+int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv) {
   const uint32_t n = s->hb.n_sorted;
   const uint32_t n_canon = s->hb.n_canon;
   const uint32_t G = s->cells_total;
   cudaStream_t st = s->stream;
-  const DevState &d = s->d;
+  const DevState &d = dv ? *dv : s->d;
   auto mark = [&](int i) -> int {
     if (timed) FS_CUDA(cudaEventRecord(s->ev[i], st), "record stage event");
     return FS_OK;
@@ -317,6 +280,21 @@ int enqueue_step(FsSim *s, bool timed) {
   if ((rc = mark(9))) return rc;
   return FS_OK;
 }
+
+// The grid build of the current canonical state alone (grid_clear, hash,
+// scan, reorder: the first stages of a step).
+int fs::enqueue_grid_build(FsSim *s) {
+  const DevState &d = s->d;
+  cudaStream_t st = s->stream;
+  FS_CUDA(cudaMemsetAsync(d.counts, 0, sizeof(uint32_t) * s->cells_total, st), "grid clear");
+  FS_CUDA(launch_hash(d, s->hb.n_canon, st), "grid build (hash)");
+  FS_CUDA(launch_scan(d, s->cells_total, st), "prefix scan");
+  FS_CUDA(launch_scatter(d, s->hb.n_canon, st), "reorder (scatter)");
+  FS_CUDA(launch_sort_gather(d, s->hb.n_sorted, st), "reorder (sort/gather)");
+  return FS_OK;
+}
+
+namespace {
 
 // The graph of `steps` back-to-back steps for the current counts, captured
 // on first use (least recently used slot replaced).
@@ -367,10 +345,14 @@ int graph_for(FsSim *s, uint32_t steps, cudaGraphExec_t *out) {
 #define CHECK_SIM(s) \
   if (!(s)) return fail(FS_E_INVALID_ARGUMENT, "%s: null simulation", __func__)
 
-int set_device(FsSim *s) {
+}  // namespace
+
+int fs::set_device(FsSim *s) {
   FS_CUDA(cudaSetDevice(s->device), "cudaSetDevice");
   return FS_OK;
 }
+
+namespace {
 
 // Plain entry points act on a simulation's single scene.
 #define CHECK_PLAIN(s)                                                                        \

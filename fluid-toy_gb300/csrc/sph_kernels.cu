@@ -26,39 +26,6 @@
 namespace fs {
 namespace {
 
-// Nine contiguous slot runs around the UNCLAMPED cell of `pos`
-// (position_to_cell / is_valid_cell of the neighbour shaders).
-struct Runs {
-  uint32_t lo[9], hi[9];
-  int count;
-  uint32_t total;  // candidates over all runs
-};
-__device__ __forceinline__ void neighbor_runs(float3 pos, const GpuGridParams &g,
-                                              const uint32_t *__restrict__ begin, Runs &R) {
-  const long long cx = __float2int_rd((pos.x - g.grid_origin_x) * g.inv_cell_size);
-  const long long cy = __float2int_rd((pos.y - g.grid_origin_y) * g.inv_cell_size);
-  const long long cz = __float2int_rd((pos.z - g.grid_origin_z) * g.inv_cell_size);
-  const long long gx = g.grid_size_x, gy = g.grid_size_y, gz = g.grid_size_z;
-  const long long x0 = cx - 1 < 0 ? 0 : cx - 1;
-  const long long x1 = cx + 1 > gx - 1 ? gx - 1 : cx + 1;
-  R.count = 0;
-  R.total = 0;
-  if (x0 > x1) return;
-#pragma unroll
-  for (int dz = -1; dz <= 1; dz++) {
-#pragma unroll
-    for (int dy = -1; dy <= 1; dy++) {
-      const long long z = cz + dz, y = cy + dy;
-      if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
-      const uint32_t row = uint32_t(y) * g.grid_size_x + uint32_t(z) * g.grid_size_x * g.grid_size_y;
-      R.lo[R.count] = __ldg(begin + row + uint32_t(x0));
-      R.hi[R.count] = __ldg(begin + row + uint32_t(x1) + 1u);
-      R.total += R.hi[R.count] - R.lo[R.count];
-      R.count++;
-    }
-  }
-}
-
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -135,13 +102,6 @@ __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, 
   }
 }
 
-// Close-pair fallback direction normalize(sin(d), cos(2d), sin(3d)) for the
-// slot difference d = s - j (sph_force_3d_grid.wgsl:163-172). It depends on d
-// only, so it is tabulated once per simulation for |d| <= dir_half (same
-// function, same bits) and evaluated directly beyond that.
-__device__ __forceinline__ float3 fallback_dir_eval(float idx_diff) {
-  return normalize3(f3(sin_d(idx_diff * 1.0f), cos_d(idx_diff * 2.0f), sin_d(idx_diff * 3.0f)));
-}
 __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int dir_half) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t > 2 * dir_half) return;
@@ -149,25 +109,6 @@ __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int
   tab[t] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-// ---- density ----------------------------------------------------------------
-// boundary_gamma, sph_density_3d_grid.wgsl:86-109
-__device__ __forceinline__ float boundary_gamma(const GpuContainerGeometry &c, float h, float3 pos) {
-  float3 l = world_to_local(c, pos);
-  float gamma = 1.0f;
-  const float d_nx = l.x - (-c.half_width);
-  const float d_px = c.half_width - l.x;
-  const float d_fl = l.y - (-c.half_height);
-  const float d_ce = c.half_height - l.y;
-  const float d_nz = l.z - (-c.half_depth);
-  const float d_pz = c.half_depth - l.z;
-  if (d_nx < h) gamma *= 0.5f + 0.5f * clampf(d_nx / h, 0.0f, 1.0f);
-  if (d_px < h) gamma *= 0.5f + 0.5f * clampf(d_px / h, 0.0f, 1.0f);
-  if (d_fl < h) gamma *= 0.5f + 0.5f * clampf(d_fl / h, 0.0f, 1.0f);
-  if (d_ce < h) gamma *= 0.5f + 0.5f * clampf(d_ce / h, 0.0f, 1.0f);
-  if (d_nz < h) gamma *= 0.5f + 0.5f * clampf(d_nz / h, 0.0f, 1.0f);
-  if (d_pz < h) gamma *= 0.5f + 0.5f * clampf(d_pz / h, 0.0f, 1.0f);
-  return fmaxf(gamma, 0.1f);
-}
 
 // sph_density_3d_grid.wgsl:111-194 (writes the sorted copy only). Besides the
 // density it records each particle's hit mask (1e-12 < r^2 < h^2, the XSPH and
@@ -425,7 +366,7 @@ __device__ __forceinline__ void solve_one(
             const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
             const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float4 *__restrict__ v_out,
-            unsigned long long *__restrict__ stats) {
+            unsigned long long *__restrict__ stats, float4 *__restrict__ ap_out) {
   const bool active = s < v.b->n_sorted;
   const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
@@ -493,6 +434,7 @@ __device__ __forceinline__ void solve_one(
     const float max_accel = 0.25f * h / (dt * dt);
     const float mag_sq = dot3(a_p, a_p);
     const float max_sq = max_accel * max_accel;
+    if (ap_out) ap_out[s] = make_float4(a_p.x, a_p.y, a_p.z, 0.0f);  // recording for the reverse pass
     if (mag_sq > max_sq) a_p = a_p * (max_accel / sqrtf(mag_sq));
     const float3 a_total = xyz(anp[s]) + a_p;
     const float3 v_star = xyz(vel_x[s]) + dt * a_total;
@@ -627,10 +569,10 @@ __global__ void __launch_bounds__(128)
             const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
             const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float4 *__restrict__ v_out,
-            unsigned long long *__restrict__ stats) {
+            unsigned long long *__restrict__ stats, float4 *__restrict__ ap_out) {
   for_warp_tasks(q, [&](uint32_t s) {
     solve_one<HAS_PRESSURE, LAST>(s, v, s_pos, vel_x, anp, begin, xp_in, rho_in, mask_words,
-                                  mask_off, xp_out, rho_out, v_out, stats);
+                                  mask_off, xp_out, rho_out, v_out, stats, ap_out);
   });
 }
 
@@ -968,15 +910,23 @@ cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st)
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count);
+  float4 *xp_out = d.rec_xp ? d.rec_xp[0] : d.pred_xp[0];
+  float *rho_out = d.rec_rho ? d.rec_rho[0] : d.pred_rho[0];
   k_force_predict<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x,
                                           d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
-                                          d.mask_off, d.anp, d.pred_xp[0], d.pred_rho[0]);
+                                          d.mask_off, d.anp, xp_out, rho_out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const int in = iter & 1, out = in ^ 1;
+  // ping-pong, or the recorded levels iter -> iter + 1 when recording
+  const float4 *xp_in = d.rec_xp ? d.rec_xp[iter] : d.pred_xp[in];
+  const float *rho_in = d.rec_rho ? d.rec_rho[iter] : d.pred_rho[in];
+  float4 *xp_out = d.rec_xp ? d.rec_xp[iter + 1] : d.pred_xp[out];
+  float *rho_out = d.rec_rho ? d.rec_rho[iter + 1] : d.pred_rho[out];
+  float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
   TaskQueue q;
   cudaError_t e = prepare_queue(d, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
@@ -985,9 +935,8 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     static unsigned blocks = 0;                                                               \
     if (!blocks) blocks = persistent_blocks(k_solve<P_, L_>, d.sm_count);                    \
     k_solve<P_, L_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp, d.cell_begin,    \
-                                            d.pred_xp[in], d.pred_rho[in], d.mask_words,      \
-                                            d.mask_off, d.pred_xp[out], d.pred_rho[out],      \
-                                            d.pred_v, d.stats);                               \
+                                            xp_in, rho_in, d.mask_words, d.mask_off, xp_out,  \
+                                            rho_out, d.pred_v, d.stats, ap_out);              \
   } while (0)
   if (iter == 0 && last) FS_SOLVE(false, true);
   else if (iter == 0) FS_SOLVE(false, false);

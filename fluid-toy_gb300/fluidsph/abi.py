@@ -180,6 +180,13 @@ SIGNATURES = {
     "fs_batch_download_scene_cells": (C.c_int, [_vp, _u32, _vp, _vp, _u32]),
     "fs_batch_download_scene_index_maps": (C.c_int, [_vp, _u32, _vp, _vp, _u32]),
     "fs_batch_upload_scene": (C.c_int, [_vp, _u32, _vp, _u32]),
+    "fs_adj_create": (C.c_int, [_vp, _u32, _P(_vp)]),
+    "fs_adj_destroy": (C.c_int, [_vp]),
+    "fs_adj_forward": (C.c_int, [_vp, _u32]),
+    "fs_adj_set_cotangents": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "fs_adj_splat_mse_loss": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),
+                                        _vp, C.c_int, _P(C.c_double)]),
+    "fs_adj_backward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
 }
 FS_BATCH_MAX_SCENES = 65535
 FS_NOALLOC_SCAN_MAX_CELLS = 1 << 26

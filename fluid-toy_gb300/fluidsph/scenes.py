@@ -150,14 +150,59 @@ def fourier_velocity(pos: np.ndarray, seed: int, modes: int = 8, amplitude: floa
     return v
 
 
+def rollout_scene(nx: int, ny: int, nz: int, box, seed: int = 0, steps: int = 200,
+                  name: str | None = None) -> Scene:
+    """A lattice block with a smooth random initial velocity (8 Fourier
+    modes, largest speed 0.5 m/s): the differentiable-rollout workload."""
+    parts = lattice_block(nx, ny, nz, box, seed=seed)
+    v = fourier_velocity(parts[:, COL_POS].astype(np.float64), seed + 1000, box=box)
+    parts[:, COL_VEL] = v.astype(np.float32)
+    return make_scene(name or f"rollout_{nx * ny * nz}", parts, box, steps=steps)
+
+
 def config3(seed: int = 0) -> Scene:
     """Differentiable rollout: 32^3 = 32,768 particles in a 1.2x1x1 box with a
     smooth random initial velocity (8 Fourier modes, 0.5 m/s), 200 steps."""
-    box = (1.2, 1.0, 1.0)
-    parts = lattice_block(32, 32, 32, box, seed=seed)
+    return rollout_scene(32, 32, 32, (1.2, 1.0, 1.0), seed, 200, "rollout_32768")
+
+
+def config3_small(seed: int = 0) -> Scene:
+    """The checking copy of the rollout: 2,048 particles (16x8x16), 20 steps."""
+    return rollout_scene(16, 8, 16, (0.6, 0.5, 0.6), seed, 20, "rollout_2048")
+
+
+def reference_physics_rollout(nx: int = 16, ny: int = 8, nz: int = 16, steps: int = 20,
+                              seed: int = 0) -> Scene:
+    """The rollout with the reference application's own default physics
+    (SphConfig::default, src/state/simulation.rs:287-299: h 0.035, near
+    stiffness 0.7, viscosity 0.7, surface tension 0.005, mass 1, wall
+    stiffness 200; rest density from compute_rest_density; dt = 1/60/6 with
+    the default 6 substeps) on a lattice at the spacing that rest density
+    assumes (0.6 h), with the same smooth random initial velocity. Unlike the
+    h = 0.08 / spacing 0.02 / surface tension 6.5 workloads, which start far
+    from equilibrium and blow up within a few steps, this rollout stays smooth,
+    so finite differences of its loss converge."""
+    h = 0.035
+    sp = 0.6 * h
+    box = (0.5, 0.4, 0.5)
+    parts = lattice_block(nx, ny, nz, box, spacing=sp, jitter=0.0005, seed=seed)
     v = fourier_velocity(parts[:, COL_POS].astype(np.float64), seed + 1000, box=box)
     parts[:, COL_VEL] = v.astype(np.float32)
-    return make_scene("rollout_32768", parts, box, steps=200)
+    dt = 1.0 / 60.0 / 6.0
+    rho0 = P.compute_rest_density(h, 1.0)
+    sph = P.sph_params_3d(h, 1.0, rho0, 35.0, 0.7, 0.7, 0.005, 0.305, dt, len(parts))
+    geom = P.container_geometry(box[0], box[2], 0.0, box[1], 0.0, 0.0, 200.0, 0.55)
+    return Scene(f"reference_physics_rollout_{len(parts)}", parts, sph, geom, P.gravity(-9.81),
+                 None, 4, steps, box)
+
+
+def loss_grid(scene: Scene, grid_size: int = 64):
+    """The MC grid of the rollout loss: grid_size^3 voxels over the scene's
+    box (cell = largest extent / grid_size), splat radius h."""
+    from . import params as Pm
+    Lx, Ly, Lz = scene.box
+    return Pm.mc_grid_params((-Lx / 2, 0.0, -Lz / 2), (Lx / 2, Ly, Lz / 2), grid_size,
+                             scene.sph.kernel_radius)
 
 
 def _to_container(parts: np.ndarray, geom: GpuContainerGeometry) -> np.ndarray:

@@ -417,6 +417,48 @@ int fs_batch_download_scene_index_maps(FsSim *sim, uint32_t scene,
 int fs_batch_upload_scene(FsSim *sim, uint32_t scene, const SphParticle3D *particles,
                           uint32_t count);
 
+/* ---- differentiable rollout (reverse mode) ------------------------------------ */
+
+/* No counterpart in the reference. Gradients of a rollout of fs_step with
+ * respect to the initial canonical positions and velocities and to each
+ * scene's viscosity, stiffness and surface_tension, the counterpart of a
+ * torch.autograd.Function: fs_adj_forward records, fs_adj_backward consumes
+ * cotangents of the final state. Cell assignment and neighbour sets are
+ * piecewise constant (taken from the recorded steps, not differentiated); the
+ * r < 0.1h fallback direction is constant. The forward keeps the state every
+ * `checkpoint_every` steps; the backward recomputes each segment from its
+ * checkpoint, recording the step intermediates, and reverses it. Per-particle
+ * adjoints are FP32; the parameter gradients are reduced in FP64 (stiffness
+ * is read by no stage of the step: its gradient is 0). Supported: every
+ * particle active, mouse force and rigid body inactive, at most 16 PCISPH
+ * iterations, every particle inside the SPH grid (else fs_adj_backward
+ * returns FS_E_STATE). Works on plain simulations and batches. */
+typedef struct FsAdj FsAdj;
+int fs_adj_create(FsSim *sim, uint32_t checkpoint_every, FsAdj **out);
+int fs_adj_destroy(FsAdj *adj);
+/* Run nsteps steps from the simulation's current state, recording; the
+ * cotangents are cleared. The parameters must not change until the
+ * backward. */
+int fs_adj_forward(FsAdj *adj, uint32_t nsteps);
+/* Cotangents dL/dpos and dL/dvel of the final canonical state, (N, 3) float
+ * rows (N = fs_num_particles), host or device memory; NULL = zero. */
+int fs_adj_set_cotangents(FsAdj *adj, const float *dl_dpos, const float *dl_dvel,
+                          int on_device);
+/* A loss as cotangent source: the mean squared difference between the
+ * density splat (fs_density_splat) of the scene's final positions and
+ * `target` (grid_size^3 floats, host or device). Writes the loss and sets
+ * the cotangents of that scene's particles (velocity cotangent 0). */
+int fs_adj_splat_mse_loss(FsAdj *adj, uint32_t scene, const GpuMcGridParams *grid,
+                          const GpuContainerGeometry *geom, const float *target,
+                          int target_on_device, double *loss);
+/* Reverse the recorded rollout: dL/dpos0 and dL/dvel0 as (N, 3) float rows
+ * (host or device, either may be NULL) and, if dl_dparams is not NULL,
+ * 3 doubles per scene (viscosity, stiffness, surface_tension). Leaves the
+ * simulation at the rollout's final canonical state (its sorted views are
+ * unspecified until the next step). Synchronises. */
+int fs_adj_backward(FsAdj *adj, float *dl_dpos0, float *dl_dvel0, int on_device,
+                    double *dl_dparams);
+
 /* ---- prefix scan without allocation -------------------------------------- */
 
 /* No counterpart in the reference. The inclusive prefix scan of a cell-count

@@ -27,7 +27,8 @@ CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenm
 
 
 def build(force: bool = False) -> Path:
-    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+    deps = [SRC, HERE / "dual.hpp"]
+    if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     cxx = shutil.which("g++") or "c++"
     tmp = LIB.with_suffix(".so.tmp")
@@ -93,6 +94,11 @@ def _bind(lib):
         lib.or_sincos_f32.argtypes = [vp, vp, vp, u32]
         lib.or_set_threads.argtypes = [C.c_int]
         lib.or_density_splat.argtypes = [vp, vp, vp, vp]
+        if hasattr(lib, "or_tangent_rollout_loss"):
+            lib.or_tangent_rollout_loss.argtypes = [vp, u32, vp, vp, vp, u32, u32, vp, vp,
+                                                    C.c_double, C.c_double, vp, vp, C.c_int,
+                                                    C.POINTER(C.c_double),
+                                                    C.POINTER(C.c_double)]
         lib.or_max_threads.restype = C.c_int
     return lib
 
@@ -105,6 +111,28 @@ def sincos_f32(x: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     c = np.empty_like(x)
     load().or_sincos_f32(x.ctypes.data, s.ctypes.data, c.ctypes.data, x.size)
     return s, c
+
+
+def tangent_rollout_loss(particles, sph_params, container_geom, gravity, iterations: int,
+                         steps: int, mc_params, target, dpos=None, dvel=None,
+                         dvisc: float = 0.0, dst: float = 0.0, precision: int = 32):
+    """(L, dL) of L = mean((splat(x_T) - target)^2) after `steps` steps, with
+    dL its forward-mode derivative along (dpos, dvel, dvisc, dst): the oracle
+    on dual numbers (precision 32: the FP32 restatement's own trajectory)."""
+    lib = load()
+    parts = np.ascontiguousarray(particles, np.float32)
+    g = (C.c_float * 3)(*gravity.direction)
+    t = np.ascontiguousarray(target, np.float32)
+    dp = None if dpos is None else np.ascontiguousarray(dpos, np.float64)
+    dv = None if dvel is None else np.ascontiguousarray(dvel, np.float64)
+    loss, dloss = C.c_double(), C.c_double()
+    lib.or_tangent_rollout_loss(parts.ctypes.data, len(parts), C.addressof(sph_params),
+                                C.addressof(container_geom), g, int(iterations), int(steps),
+                                None if dp is None else dp.ctypes.data,
+                                None if dv is None else dv.ctypes.data, float(dvisc),
+                                float(dst), C.addressof(mc_params), t.ctypes.data,
+                                int(precision), C.byref(loss), C.byref(dloss))
+    return loss.value, dloss.value
 
 
 def set_threads(n: int) -> int:

@@ -31,7 +31,11 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <memory>
+#include <type_traits>
 #include <vector>
+
+#include "dual.hpp"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -125,14 +129,23 @@ template <class R> inline V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a
 template <class R> inline V3<R> operator/(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
 // dot(a, b) = (a.x*b.x + a.y*b.y) + a.z*b.z, left to right, no fusion.
 template <class R> inline R dot3(V3<R> a, V3<R> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-template <class R> inline R len3(V3<R> a) { return std::sqrt(dot3(a, a)); }
+// math on R: the std functions for float/double, dual.hpp's for Dual
+template <class R, class = std::enable_if_t<std::is_arithmetic_v<R>>>
+inline R sqrt_(R x) { return std::sqrt(x); }
+template <class R, class = std::enable_if_t<std::is_arithmetic_v<R>>>
+inline R floor_(R x) { return std::floor(x); }
+template <class R, class = std::enable_if_t<std::is_arithmetic_v<R>>>
+inline R fabs_(R x) { return std::fabs(x); }
+template <class R> inline R len3(V3<R> a) { return sqrt_(dot3(a, a)); }
 template <class R> inline V3<R> normalize3(V3<R> a) { return a / len3(a); }
 template <class R> inline V3<R> cross3(V3<R> a, V3<R> b) {
   return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 template <class R> inline V3<R> from4(const float *r) { return {R(r[0]), R(r[1]), R(r[2])}; }
-template <class R> inline R fmax_(R a, R b) { return std::fmax(a, b); }
-template <class R> inline R fmin_(R a, R b) { return std::fmin(a, b); }
+template <class R, class = std::enable_if_t<std::is_arithmetic_v<R>>>
+inline R fmax_(R a, R b) { return std::fmax(a, b); }
+template <class R, class = std::enable_if_t<std::is_arithmetic_v<R>>>
+inline R fmin_(R a, R b) { return std::fmin(a, b); }
 template <class R> inline R clamp_(R e, R lo, R hi) { return fmin_(fmax_(e, lo), hi); }
 template <class R> inline R sign_(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
 // sin/cos of the close-pair fallback direction (sph_force_3d_grid.wgsl:
@@ -181,6 +194,12 @@ inline float sin_(float x) { return sin_f32(x); }
 inline float cos_(float x) { return cos_f32(x); }
 inline double sin_(double x) { return std::sin(x); }
 inline double cos_(double x) { return std::cos(x); }
+template <class V> inline Dual<V> sin_(Dual<V> x) {
+  return Dual<V>(sin_(x.v), std::cos(double(x.v)) * x.d);
+}
+template <class V> inline Dual<V> cos_(Dual<V> x) {
+  return Dual<V>(cos_(x.v), -std::sin(double(x.v)) * x.d);
+}
 
 // WGSL f32 -> i32 conversion: truncate toward zero, saturate, NaN -> 0.
 inline int32_t f2i_sat(double x) {
@@ -191,6 +210,9 @@ inline int32_t f2i_sat(double x) {
 }
 
 const float PI_F = 3.14159265359f;  // `const PI: f32` in every step shader
+
+template <class R> struct value_is_f32 : std::is_same<R, float> {};
+template <> struct value_is_f32<Dual<float>> : std::true_type {};
 
 // ---- per-particle records at precision R ---------------------------------
 template <class R>
@@ -261,9 +283,9 @@ struct Oracle {
   // grid_build.wgsl:33-44 / sph_density_3d_grid.wgsl:68-81
   inline void position_to_cell(V3<R> pos, int32_t c[3]) const {
     V3<R> l{pos.x - R(grid.ox), pos.y - R(grid.oy), pos.z - R(grid.oz)};
-    c[0] = f2i_sat(double(std::floor(l.x * R(grid.inv_cell_size))));
-    c[1] = f2i_sat(double(std::floor(l.y * R(grid.inv_cell_size))));
-    c[2] = f2i_sat(double(std::floor(l.z * R(grid.inv_cell_size))));
+    c[0] = f2i_sat(double(floor_(l.x * R(grid.inv_cell_size))));
+    c[1] = f2i_sat(double(floor_(l.y * R(grid.inv_cell_size))));
+    c[2] = f2i_sat(double(floor_(l.z * R(grid.inv_cell_size))));
   }
   inline uint32_t cell_to_index_clamped(const int32_t c[3]) const {
     int32_t cx = std::min(std::max(c[0], 0), int32_t(grid.gx) - 1);
@@ -372,7 +394,7 @@ struct Oracle {
         cand++;
         if (r_sq < p.h2) {
           hits++;
-          R r = std::sqrt(r_sq);
+          R r = sqrt_(r_sq);
           R diff = p.h2 - r_sq;
           density += p.mass * (scale_d * diff * diff * diff);
           R dn = p.h - r;
@@ -441,7 +463,7 @@ struct Oracle {
         V3<R> r_vec = pos_i - pos_j;
         R r_sq = dot3(r_vec, r_vec);
         if (r_sq < p.h2 && r_sq > R(1e-12f)) {
-          R r = std::sqrt(r_sq);
+          R r = sqrt_(r_sq);
           V3<R> dir;
           R min_dist = h * R(0.1f);
           if (r < min_dist) {
@@ -530,7 +552,7 @@ struct Oracle {
           R diff = p.h2 - r_sq;
           pred_density += p.mass * (scale_d * diff * diff * diff);
           if (r_sq > R(1e-12f)) {
-            R r = std::sqrt(r_sq);
+            R r = sqrt_(r_sq);
             R nd = fmax_(nb.density, R(1));
             R np = nb.pressure;
             R sd = fmax_(self.density, R(1));
@@ -546,7 +568,7 @@ struct Oracle {
       R max_accel = R(0.25f) * h / (p.dt * p.dt);
       R mag_sq = dot3(a_p, a_p);
       R max_sq = max_accel * max_accel;
-      if (mag_sq > max_sq) a_p = a_p * (max_accel / std::sqrt(mag_sq));
+      if (mag_sq > max_sq) a_p = a_p * (max_accel / sqrt_(mag_sq));
       V3<R> a_total = P[orig].force + a_p;
       V3<R> v_star = P[orig].vel + p.dt * a_total;
       V3<R> x_star = P[orig].pos + p.dt * v_star;
@@ -582,7 +604,7 @@ struct Oracle {
     R tx = uvw.x * R(float(res)) - R(0.5f);
     R ty = uvw.y * R(float(res)) - R(0.5f);
     R tz = uvw.z * R(float(res)) - R(0.5f);
-    R fx0 = std::floor(tx), fy0 = std::floor(ty), fz0 = std::floor(tz);
+    R fx0 = floor_(tx), fy0 = floor_(ty), fz0 = floor_(tz);
     R ax = tx - fx0, ay = ty - fy0, az = tz - fz0;
     int x0 = std::min(std::max(f2i_sat(double(fx0)), -1), res);
     int y0 = std::min(std::max(f2i_sat(double(fy0)), -1), res);
@@ -671,9 +693,9 @@ struct Oracle {
             break;
           }
           case 2: {  // cylinder
-            R radial = std::sqrt(rl.x * rl.x + rl.z * rl.z);
+            R radial = sqrt_(rl.x * rl.x + rl.z * rl.z);
             R d_radial = radial - he;
-            R d_cap = std::fabs(rl.y) - he;
+            R d_cap = fabs_(rl.y) - he;
             sdf_v = fmax_(d_radial, d_cap);
             if (d_radial > d_cap) {
               if (radial > R(0.001f)) ln = v3(rl.x / radial, R(0), rl.z / radial);
@@ -685,9 +707,9 @@ struct Oracle {
           }
           case 3: {  // torus
             R minor_r = he * R(0.3f);
-            R xz_len = std::sqrt(rl.x * rl.x + rl.z * rl.z);
+            R xz_len = sqrt_(rl.x * rl.x + rl.z * rl.z);
             R qx = xz_len - he, qy = rl.y;
-            R q_len = std::sqrt(qx * qx + qy * qy);
+            R q_len = sqrt_(qx * qx + qy * qy);
             sdf_v = q_len - minor_r;
             if (q_len > R(0.001f) && xz_len > R(0.001f)) {
               R rdx = qx / q_len, rdy = qy / q_len;
@@ -713,7 +735,7 @@ struct Oracle {
             break;
           }
           default: {  // cube
-            V3<R> dd{std::fabs(rl.x) - he, std::fabs(rl.y) - he, std::fabs(rl.z) - he};
+            V3<R> dd{fabs_(rl.x) - he, fabs_(rl.y) - he, fabs_(rl.z) - he};
             sdf_v = fmax_(dd.x, fmax_(dd.y, dd.z));
             if (dd.x >= dd.y && dd.x >= dd.z) ln = v3(sign_(rl.x), R(0), R(0));
             else if (dd.y >= dd.x && dd.y >= dd.z) ln = v3(R(0), sign_(rl.y), R(0));
@@ -756,12 +778,12 @@ struct Oracle {
       V3<R> lpn = world_to_local(c, pos);
       V3<R> lvn = world_dir_to_local(c, vel);
       const R rest = c.damping;
-      if (lpn.x < -c.hw) { lpn.x = -c.hw; lvn.x = std::fabs(lvn.x) * rest; }
-      else if (lpn.x > c.hw) { lpn.x = c.hw; lvn.x = -std::fabs(lvn.x) * rest; }
-      if (lpn.y < -c.hh) { lpn.y = -c.hh; lvn.y = std::fabs(lvn.y) * rest; }
-      else if (lpn.y > c.hh) { lpn.y = c.hh; lvn.y = -std::fabs(lvn.y) * rest; }
-      if (lpn.z < -c.hd) { lpn.z = -c.hd; lvn.z = std::fabs(lvn.z) * rest; }
-      else if (lpn.z > c.hd) { lpn.z = c.hd; lvn.z = -std::fabs(lvn.z) * rest; }
+      if (lpn.x < -c.hw) { lpn.x = -c.hw; lvn.x = fabs_(lvn.x) * rest; }
+      else if (lpn.x > c.hw) { lpn.x = c.hw; lvn.x = -fabs_(lvn.x) * rest; }
+      if (lpn.y < -c.hh) { lpn.y = -c.hh; lvn.y = fabs_(lvn.y) * rest; }
+      else if (lpn.y > c.hh) { lpn.y = c.hh; lvn.y = -fabs_(lvn.y) * rest; }
+      if (lpn.z < -c.hd) { lpn.z = -c.hd; lvn.z = fabs_(lvn.z) * rest; }
+      else if (lpn.z > c.hd) { lpn.z = c.hd; lvn.z = -fabs_(lvn.z) * rest; }
       P[i].pos = local_to_world(c, lpn);
       P[i].vel = local_dir_to_world(c, lvn);
     }
@@ -830,7 +852,8 @@ struct Oracle {
   // unclamped cell in dz, dy, dx, slot order; -1 outside the box when
   // clipping; else divided by the five-wall gamma (mc_density.wgsl:110-128).
   // The cell radius is an index quantity and is taken in f32 at any R.
-  void density_splat(const McGridF &mc, const GeomF &cgf, double *out) const {
+  template <class T>
+  void splat_into(const McGridF &mc, const GeomF &cgf, T *out) const {
     Geom<R> cg;
     cg.hw = R(cgf.half_width); cg.hh = R(cgf.half_height); cg.hd = R(cgf.half_depth);
     cg.cy = R(cgf.center_y);
@@ -838,8 +861,8 @@ struct Oracle {
     const uint32_t gs = mc.grid_size;
     const R h = R(mc.kernel_radius);
     const R h_sq = h * h;
-    const R pow9 = sizeof(R) == 4 ? R(float(pow_int_d(double(mc.kernel_radius), 9)))
-                                  : R(pow_int_d(double(mc.kernel_radius), 9));
+    const R pow9 = value_is_f32<R>::value ? R(float(pow_int_d(double(mc.kernel_radius), 9)))
+                                          : R(pow_int_d(double(mc.kernel_radius), 9));
     const R coeff = R(315) / (R(64) * R(PI_F) * pow9);
     const int32_t cr = f2i_sat(double(std::ceil(mc.kernel_radius * grid.inv_cell_size)));
     const R cs = R(mc.cell_size);
@@ -877,11 +900,11 @@ struct Oracle {
               }
           const V3<R> q{wp.x, wp.y - cg.cy, wp.z};
           const V3<R> l{dot3(cg.i0, q), dot3(cg.i1, q), dot3(cg.i2, q)};
-          double &o = out[size_t(x) + size_t(gs) * (size_t(y) + size_t(gs) * z)];
+          T &o = out[size_t(x) + size_t(gs) * (size_t(y) + size_t(gs) * z)];
           if (cgf.clip_enabled != 0u &&
               !(l.x >= -cg.hw && l.x <= cg.hw && l.y >= -cg.hh && l.y <= cg.hh &&
                 l.z >= -cg.hd && l.z <= cg.hd)) {
-            o = -1.0;
+            o = T(-1.0);
             continue;
           }
           R gamma = R(1);
@@ -898,9 +921,13 @@ struct Oracle {
           if (dnz < h) gamma *= fac(dnz);
           if (dpz < h) gamma *= fac(dpz);
           gamma = std::max(gamma, R(0.15f));
-          o = double(density / gamma);
+          o = T(density / gamma);
         }
     }
+  }
+
+  void density_splat(const McGridF &mc, const GeomF &cgf, double *out) const {
+    splat_into<double>(mc, cgf, out);
   }
 
   void set_geom(const GeomF &q) {
@@ -969,6 +996,51 @@ Oracle<R> *create_impl(const ParticleF *parts, uint32_t n, const SphParamsF *par
 }
 
 }  // namespace
+
+// Forward-mode derivative of the rollout loss L = mean((splat(x_T) - target)^2)
+// along one direction of (initial positions, initial velocities, viscosity,
+// surface tension): the oracle run on Dual<V> numbers (V = float follows the
+// FP32 restatement's trajectory bit for bit, V = double the FP64 twin's).
+template <class V>
+void tangent_loss_impl(const ParticleF *parts, uint32_t n, const SphParamsF *params,
+                       const GeomF *geom, const float *gravity, uint32_t iterations,
+                       uint32_t steps, const double *dpos, const double *dvel, double dvisc,
+                       double dst, const McGridF *mc, const float *target, double *loss,
+                       double *dloss) {
+  using R = Dual<V>;
+  std::unique_ptr<Oracle<R>> o(create_impl<R>(parts, n, params, geom, 0, nullptr, 0));
+  for (int a = 0; a < 3; a++) o->gravity[a] = R(gravity[a]);
+  o->iterations = std::max(iterations, 1u);
+  for (uint32_t i = 0; i < n; i++) {
+    if (dpos) {
+      o->P[i].pos.x.d = dpos[3 * size_t(i)];
+      o->P[i].pos.y.d = dpos[3 * size_t(i) + 1];
+      o->P[i].pos.z.d = dpos[3 * size_t(i) + 2];
+    }
+    if (dvel) {
+      o->P[i].vel.x.d = dvel[3 * size_t(i)];
+      o->P[i].vel.y.d = dvel[3 * size_t(i) + 1];
+      o->P[i].vel.z.d = dvel[3 * size_t(i) + 2];
+    }
+  }
+  o->p.visc.d = dvisc;
+  o->p.st.d = dst;
+  for (uint32_t k = 0; k < steps; k++) o->step(nullptr, nullptr);
+  o->stage_hash();
+  o->stage_scan();
+  o->stage_reorder();
+  const size_t nvox = size_t(mc->grid_size) * mc->grid_size * mc->grid_size;
+  std::vector<R> f(nvox);
+  o->template splat_into<R>(*mc, *geom, f.data());
+  double L = 0.0, dL = 0.0;
+  for (size_t v = 0; v < nvox; v++) {
+    const double diff = double(f[v].v) - double(target[v]);
+    L += diff * diff;
+    dL += 2.0 * diff * f[v].d;
+  }
+  *loss = L / double(nvox);
+  *dloss = dL / double(nvox);
+}
 
 // ---- C ABI for the test harness (ctypes) ------------------------------------
 extern "C" {
@@ -1144,6 +1216,22 @@ void or_sincos_f32(const float *x, float *s, float *c, uint32_t n) {
 void or_get_grid(void *hv, void *out) {
   auto *h = (Handle *)hv;
   DISPATCH(h, std::memcpy(out, &o->grid, sizeof(GridF)));
+}
+
+// Tangent of the rollout loss (see tangent_loss_impl); precision 32 or 64.
+void or_tangent_rollout_loss(const void *particles, uint32_t n, const void *params,
+                             const void *geom, const float *gravity, uint32_t iterations,
+                             uint32_t steps, const double *dpos, const double *dvel, double dvisc,
+                             double dst, const void *mc, const float *target, int precision,
+                             double *loss, double *dloss) {
+  if (precision == 64)
+    tangent_loss_impl<double>((const ParticleF *)particles, n, (const SphParamsF *)params,
+                              (const GeomF *)geom, gravity, iterations, steps, dpos, dvel, dvisc,
+                              dst, (const McGridF *)mc, target, loss, dloss);
+  else
+    tangent_loss_impl<float>((const ParticleF *)particles, n, (const SphParamsF *)params,
+                             (const GeomF *)geom, gravity, iterations, steps, dpos, dvel, dvisc,
+                             dst, (const McGridF *)mc, target, loss, dloss);
 }
 
 // The MC density field of the last step's sorted positions (gs^3 doubles).
