@@ -19,6 +19,7 @@ struct TapeView {
   const float4 *xp[kMaxAdjIters + 1];  // predicted (x*, p) per level
   const float *rho[kMaxAdjIters + 1];  // predicted densities per level
   const float4 *ap[kMaxAdjIters];      // pressure acceleration before the clamp
+  const uint32_t *order;               // the step's neighbour-pass task order
 };
 
 // Reverse accumulators, grid-sorted order.
@@ -32,15 +33,20 @@ struct AdjView {
   float *gp;      // d/d pressure carried between PCISPH levels
   float4 *gu[2];  // per level: d/d pressure acceleration (pre-clamp), d/d next density
   double *gparam; // [scenes][3]: viscosity, stiffness, surface_tension (FP64)
+  double2 *gpart; // [N] canonical: each particle's share of d/d (viscosity, surface tension)
+  uint32_t *counters;  // task counters of the gather launches [kMaxAdjIters + 3]
   uint32_t *err;
 };
 
 cudaError_t launch_adj_step(const SceneView &v, const TapeView &t, const AdjView &a,
                             const float4 *xbar_in, const float4 *vbar_in, float4 *xbar_out,
                             float4 *vbar_out, const float4 *dir_tab, int dir_half, uint32_t n,
-                            int K, cudaStream_t st);
+                            int K, int lanes, int sm_count, cudaStream_t st);
 cudaError_t launch_splat_mse(const SplatArgs &sa, const float *field, const float *target,
                              float *gg, double *loss, cudaStream_t st);
+cudaError_t launch_reduce_params(const double2 *gpart, const uint32_t *scene_first,
+                                 const uint32_t *scene_count, uint32_t scenes, double *gparam,
+                                 cudaStream_t st);
 cudaError_t launch_rows_to_f4(uint32_t n, const float *rows, float4 *out, cudaStream_t st);
 cudaError_t launch_f4_to_rows(uint32_t n, const float4 *in, float *rows, cudaStream_t st);
 cudaError_t launch_splat_adjoint(const SplatArgs &sa, uint32_t n, const float4 *pos,

@@ -55,10 +55,47 @@ __device__ __forceinline__ bool runs_checked(float3 pos, const GpuGridParams &g,
          cy < (long long)g.grid_size_y && cz < (long long)g.grid_size_z;
 }
 
-template <class F>
-__device__ __forceinline__ void for_candidates(const Runs &R, F &&f) {
-  for (int r = 0; r < R.count; r++)
-    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) f(j);
+// L lanes share one particle's candidate list: lane `sub` of the group takes
+// the flat candidate indices congruent to sub mod L. Small particle counts
+// leave the GPU latency bound at one particle per lane; splitting each list
+// multiplies the warps in flight. Partial sums then combine in a fixed
+// butterfly, so the result depends on L but not on the run.
+template <int L, class F>
+__device__ __forceinline__ void for_candidates_sub(const Runs &R, uint32_t sub, F &&f) {
+  uint32_t base = 0;
+  for (int r = 0; r < R.count; r++) {
+    const uint32_t lo = R.lo[r], hi = R.hi[r];
+    const uint32_t first = L == 1 ? lo : lo + (sub + L - base % L) % L;
+    for (uint32_t j = first; j < hi; j += L) f(j);
+    base += hi - lo;
+  }
+}
+template <int L>
+__device__ __forceinline__ float group_sum(float x) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+template <int L>
+__device__ __forceinline__ float3 group_sum3(float3 x) {
+  return make_float3(group_sum<L>(x.x), group_sum<L>(x.y), group_sum<L>(x.z));
+}
+// Tasks of 32 / L sorted slots with L lanes per particle: the recorded order
+// of 32-slot warps (heaviest first) split L ways, so a heavy warp's particles
+// spread over L concurrently running warps and the critical path (the
+// heaviest particle's candidate list) shrinks L-fold.
+template <int L, class F>
+__device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t ntasks = q.nwarps * uint32_t(L);
+  while (true) {
+    uint32_t t = 0u;
+    if (lane == 0u) t = atomicAdd(q.counter, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= ntasks) break;
+    const uint32_t base = __ldg(q.order + t / L) * 32u + (t % L) * (32u / L);
+    f(base + lane / L, lane % L);
+  }
 }
 
 // Reverse of the acceleration clamp |a| <= A (pcisph_solve.wgsl:190-196):
@@ -75,32 +112,11 @@ __device__ __forceinline__ void flag_outside(uint32_t *err, bool inside) {
   if (!inside) atomicOr(err, ERR_ADJ_OUTSIDE_GRID);
 }
 
-__device__ __forceinline__ void warp_add_params(double *gparam, uint32_t scene, double gv,
-                                                double gs) {
-  // FP64 reduction of the scalar-parameter gradients: warp sums, one atomic
-  // per warp when its lanes share a scene, else per lane
-  const unsigned full = 0xffffffffu;
-  const uint32_t s0 = __shfl_sync(full, scene, 0);
-  if (__all_sync(full, scene == s0)) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      gv += __shfl_xor_sync(full, gv, o);
-      gs += __shfl_xor_sync(full, gs, o);
-    }
-    if ((threadIdx.x & 31u) == 0u && (gv != 0.0 || gs != 0.0)) {
-      atomicAdd(gparam + 3 * s0 + 0, gv);
-      atomicAdd(gparam + 3 * s0 + 2, gs);
-    }
-  } else if (gv != 0.0 || gs != 0.0) {
-    atomicAdd(gparam + 3 * scene + 0, gv);
-    atomicAdd(gparam + 3 * scene + 2, gs);
-  }
-}
-
 // ---- integrate + finalize --------------------------------------------------------
 __global__ void __launch_bounds__(128)
     k_adj_integrate(SceneView v, TapeView t, AdjView a, const float4 *__restrict__ xbar_in,
-                    const float4 *__restrict__ vbar_in, int K) {
+                    const float4 *__restrict__ vbar_in, const float4 *__restrict__ ap_last,
+                    int K) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= v.b->n_sorted) return;
   const DevUniforms *U = v.u + t.scene_of_slot[s];
@@ -169,7 +185,7 @@ __global__ void __launch_bounds__(128)
   // finalize: v_fin = v*^K. Elementwise half of the last iteration's reverse:
   // v*^K = vhat + dt (a + clamp(a~p)); its x*, p, rho* outputs are unused.
   const float max_accel = 0.25f * h / (dt * dt);
-  const float3 apb = clamp_adjoint(f3of(t.ap[K - 1][s]), dt * vfb, max_accel);
+  const float3 apb = clamp_adjoint(f3of(ap_last[s]), dt * vfb, max_accel);
   a.gx[s] = f4(xb, 0.f);
   a.gvhat[s] = f4(vfb, 0.f);
   a.ga[s] = f4(dt * vfb, 0.f);
@@ -181,168 +197,231 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---- one PCISPH iteration (level k) ------------------------------------------------
-__global__ void __launch_bounds__(128)
-    k_adj_solve(SceneView v, TapeView t, AdjView a, int k, int K) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= v.b->n_sorted) return;
-  const DevUniforms *U = v.u + t.scene_of_slot[q];
+// Level k's recorded arrays come as arguments (xpk = x*^k with p^k, rhok =
+// rho*^k, ap_prev = iteration k-1's pressure acceleration before the clamp).
+template <int L>
+__device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const SceneView &v,
+                                              const TapeView &t, const AdjView &a,
+                                              const float4 *__restrict__ xpk,
+                                              const float *__restrict__ rhok,
+                                              const float4 *__restrict__ ap_prev,
+                                              const float4 *__restrict__ gu_in,
+                                              float4 *__restrict__ gu_out, int k, int K) {
+  const bool active = q < v.b->n_sorted;
+  const uint32_t qq = active ? q : 0u;
+  const DevUniforms *U = v.u + t.scene_of_slot[qq];
   const GpuSphParams3D &P = U->sph;
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass, dt = P.dt;
-  const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
-  const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
-  const float4 xq4 = t.xp[k][q];
-  const float3 xq = f3of(xq4);
+  const float4 xq4 = xpk[qq];
   const float pq = xq4.w;
-  const float rho_q = t.rho[k][q];
+  const float rho_q = rhok[qq];
   const float rt_q = fmaxf(rho_q, 1.0f);
-  const float4 uq4 = a.gu[k & 1][q];
-  const float3 uq = f3of(uq4);
-  const float rhat_q = uq4.w;
-  const bool has_rho = k < K - 1;  // level K's density and pressure are unused
-  const bool has_p = k >= 1;       // level 0 holds zero pressures
-  Runs R;
-  flag_outside(a.err, runs_checked(f3of(t.pos[q]), U->grid, t.cell_begin + U->c_offset, R));
   float3 xsb = f3(0.f, 0.f, 0.f);
-  float pb = 0.f, rb = 0.f;
-  for_candidates(R, [&](uint32_t j) {
-    const float4 xj4 = __ldg(t.xp[k] + j);
-    const float3 r = xq - f3of(xj4);
-    const float r2 = dot3(r, r);
-    if (!(r2 < h2)) return;
-    const float4 uj4 = __ldg(a.gu[k & 1] + j);
-    const float diff = h2 - r2;
-    if (has_rho) xsb = mad3(xsb, -6.0f * mass * scale_d * diff * diff * (rhat_q + uj4.w), r);
-    if (has_p && r2 > MIN_R2) {
-      const float rt_j = fmaxf(__ldg(t.rho[k] + j), 1.0f);
-      const float cij = pq / (rt_q * rt_q) + xj4.w / (rt_j * rt_j);
-      const float rr = sqrtf(r2);
-      const float3 e = r * (1.0f / rr);
-      const float dg = h - rr;
-      const float g = scale_g * dg * dg;
-      const float gp = -2.0f * scale_g * dg;
-      const float3 du = uq - f3of(uj4);
-      const float edu = dot3(e, du);
-      // J du = g' (e.du) e + (g / r)(du - (e.du) e)
-      const float3 Jdu = e * (gp * edu) + (du - e * edu) * (g / rr);
-      xsb = mad3(xsb, mass * cij, Jdu);
-      const float phidu = g * edu;  // phi . du with phi = g e
-      pb += mass / (rt_q * rt_q) * phidu;
-      if (rho_q > 1.0f) rb += mass * (-2.0f * pq / (rt_q * rt_q * rt_q)) * phidu;
-    }
-  });
+  float phisum = 0.f;  // sum over pairs of m g e.du (pressure terms of p and rho*)
+  if (active) {
+    const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
+    const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
+    const float3 xq = f3of(xq4);
+    const float cq = pq / (rt_q * rt_q);
+    const float4 uq4 = gu_in[q];
+    const float3 uq = f3of(uq4);
+    const float rhat_q = uq4.w;
+    const bool has_rho = k < K - 1;  // level K's density and pressure are unused
+    const bool has_p = k >= 1;       // level 0 holds zero pressures
+    Runs R;
+    flag_outside(a.err, runs_checked(f3of(t.pos[q]), U->grid, t.cell_begin + U->c_offset, R));
+    const float c_rho = -6.0f * mass * scale_d;
+    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
+      const float4 xj4 = __ldg(xpk + j);
+      const float3 r = xq - f3of(xj4);
+      const float r2 = dot3(r, r);
+      if (!(r2 < h2)) return;
+      const float4 uj4 = __ldg(gu_in + j);
+      if (has_rho) {
+        const float diff = h2 - r2;
+        xsb = mad3(xsb, c_rho * diff * diff * (rhat_q + uj4.w), r);
+      }
+      if (has_p && r2 > MIN_R2) {
+        const float rt_j = fmaxf(__ldg(rhok + j), 1.0f);
+        const float cij = cq + xj4.w / (rt_j * rt_j);
+        const float rr = sqrtf(r2);
+        const float inv_rr = 1.0f / rr;
+        const float3 e = r * inv_rr;
+        const float dg = h - rr;
+        const float g = scale_g * dg * dg;
+        const float gp = -2.0f * scale_g * dg;
+        const float3 du = uq - f3of(uj4);
+        const float edu = dot3(e, du);
+        // J du = g' (e.du) e + (g / r)(du - (e.du) e)
+        const float3 Jdu = e * (gp * edu) + (du - e * edu) * (g * inv_rr);
+        xsb = mad3(xsb, mass * cij, Jdu);
+        phisum += mass * g * edu;
+      }
+    });
+  }
+  xsb = group_sum3<L>(xsb);
+  phisum = group_sum<L>(phisum);
+  if (!active || sub != 0u) return;
+  const float pb = phisum / (rt_q * rt_q);
+  const float rb = rho_q > 1.0f ? (-2.0f * pq / (rt_q * rt_q * rt_q)) * phisum : 0.0f;
   const float p_bar = a.gp[q] + pb;  // p^{k+1} = p^k + ...: identity part
   const float3 vstar_b = dt * xsb;   // x*^k = x + dt v*^k
-  float4 gx = a.gx[q], gvh = a.gvhat[q], ga = a.ga[q];
-  gx = f4(add3(f3of(gx), xsb), 0.f);
-  gvh = f4(add3(f3of(gvh), vstar_b), 0.f);
-  ga = f4(add3(f3of(ga), dt * vstar_b), 0.f);
-  a.gx[q] = gx;
-  a.gvhat[q] = gvh;
-  a.ga[q] = ga;
+  a.gx[q] = f4(add3(f3of(a.gx[q]), xsb), 0.f);
+  a.gvhat[q] = f4(add3(f3of(a.gvhat[q]), vstar_b), 0.f);
+  a.ga[q] = f4(add3(f3of(a.ga[q]), dt * vstar_b), 0.f);
   if (k >= 1) {
     // elementwise half of iteration k-1's reverse: its outputs are level k
     const float max_accel = 0.25f * h / (dt * dt);
-    const float3 apb = clamp_adjoint(f3of(t.ap[k - 1][q]), dt * vstar_b, max_accel);
+    const float3 apb = clamp_adjoint(f3of(ap_prev[q]), dt * vstar_b, max_accel);
     const float rhat = rb + (rho_q > P.rest_density ? P.pcisph_delta * p_bar : 0.0f);
-    a.gu[(k - 1) & 1][q] = f4(apb, rhat);
+    gu_out[q] = f4(apb, rhat);
     a.gp[q] = p_bar;
   }
   // k == 0: predict, x*^0 = x + dt v*^0, v*^0 = vhat + dt a (done above)
 }
 
+template <int L>
+__global__ void __launch_bounds__(128)
+    k_adj_solve(TaskQueue tq, SceneView v, TapeView t, AdjView a, const float4 *__restrict__ xpk,
+                const float *__restrict__ rhok, const float4 *__restrict__ ap_prev,
+                const float4 *__restrict__ gu_in, float4 *__restrict__ gu_out, int k, int K) {
+  for_warp_tasks_sub<L>(tq, [&](uint32_t q, uint32_t sub) {
+    adj_solve_one<L>(q, sub, v, t, a, xpk, rhok, ap_prev, gu_in, gu_out, k, K);
+  });
+}
+
 // ---- force (non-pressure acceleration) -----------------------------------------------
+struct ForceConst {
+  float h, mass, scale_g, scale_c, near_k, visc, rho0, st, min_dist, eps_h2, h_half, h6_64,
+      sep_k;
+};
+__device__ __forceinline__ ForceConst force_const(const GpuSphParams3D &P) {
+  ForceConst c;
+  c.h = P.kernel_radius;
+  c.mass = P.mass;
+  c.scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
+  c.scale_c = 32.0f / (PI_F * P.kernel_radius_pow9);
+  c.near_k = P.near_stiffness;
+  c.visc = P.viscosity;
+  c.rho0 = P.rest_density;
+  c.st = P.surface_tension;
+  c.min_dist = c.h * 0.1f;
+  c.eps_h2 = 0.01f * P.kernel_radius_sq;
+  c.h_half = c.h * 0.5f;
+  c.h6_64 = P.kernel_radius_pow6 / 64.0f;
+  c.sep_k = 200.0f / c.min_dist;
+  return c;
+}
+
+// One particle of a force pair: recorded inputs with the density clamps of
+// sph_force_3d_grid.wgsl (max(rho, 1)) and their derivative masks.
 struct ForceSide {
   float3 x, vhat, vpre, n;
-  float rho, rhon;
+  float rb, rnb;  // max(rho, 1), max(rho_near, 1)
+  bool m, mn;     // rho > 1, rho_near > 1
 };
-struct ForcePair {  // reverse outputs of one pair term T_{i<-j}
-  float3 g_r;       // d/d(x_i - x_j)
-  float3 g_vhat_i, g_vpre_j, g_n_i, g_n_j;
-  float g_rho_i, g_rho_j, g_rhon_i, g_rhon_j, g_visc, g_st;
+// Geometry shared by both orientations of a pair, r = x_q - x_j.
+struct PairGeom {
+  float3 r, u;  // u = r / |r|
+  float r2, rr, inv_rr, dg, G, Gp, D, C, Cp;
+  bool close;
+};
+__device__ __forceinline__ PairGeom pair_geom(float3 r, float r2, const ForceConst &c) {
+  PairGeom g;
+  g.r = r;
+  g.r2 = r2;
+  g.rr = sqrtf(r2);
+  g.inv_rr = 1.0f / g.rr;
+  g.u = r * g.inv_rr;
+  g.close = g.rr < c.min_dist;
+  g.dg = c.h - g.rr;
+  const float dg2 = g.dg * g.dg, dg3 = dg2 * g.dg;
+  g.G = c.scale_g * dg2;
+  g.Gp = -2.0f * c.scale_g * g.dg;
+  g.D = r2 + c.eps_h2;
+  const float r3 = g.rr * r2;
+  const bool far_c = g.rr >= c.h_half;
+  g.C = far_c ? c.scale_c * dg3 * r3 : c.scale_c * (2.0f * dg3 * r3 - c.h6_64);
+  g.Cp = (far_c ? 1.0f : 2.0f) * c.scale_c * (-3.0f * dg2 * r3 + 3.0f * dg3 * r2);
+  return g;
+}
+
+struct ForceAcc {
+  float3 gx, gvh, gv, gn;
+  float grho, grhon, sv, ss;
 };
 
-// w . T_{i<-j} reversed, T from sph_force_3d_grid.wgsl:127-220 (see
-// force_predict_one for the forward). e_close is the tabulated fallback
-// direction of the pair (constant in the positions). The cohesion part of
-// the pair is scaled by the surface tension in the forward (a_c *= st).
-__device__ __forceinline__ ForcePair force_pair_vjp(const ForceSide &I, const ForceSide &J,
-                                                    float3 w, float3 e_close,
-                                                    const GpuSphParams3D &P) {
-  ForcePair o;
-  const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
-  const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
-  const float scale_c = 32.0f / (PI_F * P.kernel_radius_pow9);
-  const float near_k = P.near_stiffness, visc = P.viscosity, rho0 = P.rest_density;
-  const float st = P.surface_tension;
-  const float min_dist = h * 0.1f;
-  const float3 r = I.x - J.x;
-  const float r2 = dot3(r, r);
-  const float rr = sqrtf(r2);
-  const float3 u = r * (1.0f / rr);  // d rr / d r
-  const bool close = rr < min_dist;
-  const float3 e = close ? e_close : -u;
-  const float rho_i = fmaxf(I.rho, 1.0f), rho_j = fmaxf(J.rho, 1.0f);
-  const float rhon_i = fmaxf(I.rhon, 1.0f), rhon_j = fmaxf(J.rhon, 1.0f);
-  const bool mi = I.rho > 1.0f, mj = J.rho > 1.0f, mni = I.rhon > 1.0f, mnj = J.rhon > 1.0f;
-  const float Pn_i = near_k * rhon_i, Pn_j = near_k * rhon_j;
-  const float dg = h - rr;
-  const float G = scale_g * dg * dg;
-  const float Gp = -2.0f * scale_g * dg;
+// w . T_{i<-j} reversed (T from sph_force_3d_grid.wgsl:127-220, forward in
+// force_predict_one), accumulated into particle q's adjoints. JSIDE = false:
+// q is i (the pair (q, j) with q's cotangent w = abar_q; q's i-side
+// derivatives and the parameter gradients); JSIDE = true: q is j (the pair
+// (j, q) with w = abar_j; q's j-side derivatives). e_close is the pair's
+// tabulated fallback direction (constant in the positions); the cohesion
+// part is scaled by the surface tension as in the forward (a_c *= st).
+template <bool JSIDE>
+__device__ __forceinline__ void force_half(const ForceSide &I, const ForceSide &J,
+                                           const PairGeom &g, float3 w, float3 e_close,
+                                           const ForceConst &c, ForceAcc &acc) {
+  const float3 r_ij = JSIDE ? -g.r : g.r;
+  const float3 u_ij = JSIDE ? -g.u : g.u;
+  const float3 e = g.close ? e_close : -u_ij;
   const float we = dot3(w, e);
-  const float3 dwe = close ? f3(0.f, 0.f, 0.f) : (w - e * we) * (-1.0f / rr);
-  float3 g_r = f3(0.f, 0.f, 0.f);
+  const float3 dwe = g.close ? f3(0.f, 0.f, 0.f) : (w - e * we) * (-g.inv_rr);
   // near pressure: alpha G e
-  const float alpha = -mass * (Pn_i + Pn_j) / (2.0f * rho_i * rhon_j);
-  g_r = g_r + (u * (Gp * we) + dwe * G) * alpha;
-  o.g_rho_i = mi ? (-alpha / rho_i) * G * we : 0.f;
-  o.g_rhon_i = mni ? (-mass * near_k / (2.0f * rho_i * rhon_j)) * G * we : 0.f;
-  o.g_rhon_j = mnj ? (mass * Pn_i / (2.0f * rho_i * rhon_j * rhon_j)) * G * we : 0.f;
-  o.g_rho_j = 0.f;
+  const float Pn_i = c.near_k * I.rnb, Pn_j = c.near_k * J.rnb;
+  const float inv2 = 1.0f / (2.0f * I.rb * J.rnb);
+  const float alpha = -c.mass * (Pn_i + Pn_j) * inv2;
+  float3 g_r = (u_ij * (g.Gp * we) + dwe * g.G) * alpha;
+  const float Gwe = g.G * we;
+  if (!JSIDE) {
+    if (I.m) acc.grho += (-alpha / I.rb) * Gwe;
+    if (I.mn) acc.grhon += (-c.mass * c.near_k * inv2) * Gwe;
+  } else {
+    if (J.mn) acc.grhon += (c.mass * Pn_i * inv2 / J.rnb) * Gwe;
+  }
   // separation (close pairs): -200 (1 - r / min_dist) e
-  if (close) g_r = g_r + u * ((200.0f / min_dist) * we);
-  // viscosity (v_ij . x_ij < 0): beta G e, beta = m visc h vdx / (D avg)
+  if (g.close) g_r = g_r + u_ij * (c.sep_k * we);
+  // viscosity where v_ij . x_ij < 0: beta G e, beta = m visc h vdx / (D avg)
   const float3 vij = I.vhat - J.vpre;
-  const float vdx = dot3(vij, r);
-  o.g_vhat_i = f3(0.f, 0.f, 0.f);
-  o.g_vpre_j = f3(0.f, 0.f, 0.f);
-  o.g_visc = 0.f;
+  const float vdx = dot3(vij, r_ij);
   if (vdx < 0.0f) {
-    const float D = r2 + 0.01f * h2;
-    const float avg = (rho_i + rho_j) * 0.5f;
-    const float bG = mass * h * vdx / (D * avg);  // per unit viscosity and G
-    const float beta = visc * bG * G;
-    const float dbeta_dvdx = visc * mass * h * G / (D * avg);
-    g_r = g_r + (vij * dbeta_dvdx + u * (visc * bG * Gp) - r * (2.0f * beta / D)) * we + dwe * beta;
-    o.g_vhat_i = r * (we * dbeta_dvdx);
-    o.g_vpre_j = r * (-we * dbeta_dvdx);
+    const float avg = (I.rb + J.rb) * 0.5f;
+    const float inv_Davg = 1.0f / (g.D * avg);
+    const float bG = c.mass * c.h * vdx * inv_Davg;
+    const float beta = c.visc * bG * g.G;
+    const float dbdv = c.visc * c.mass * c.h * g.G * inv_Davg;
+    g_r = g_r + (vij * dbdv + u_ij * (c.visc * bG * g.Gp) - r_ij * (2.0f * beta / g.D)) * we +
+          dwe * beta;
     const float drho = -beta / (2.0f * avg) * we;
-    o.g_rho_i += mi ? drho : 0.f;
-    o.g_rho_j += mj ? drho : 0.f;
-    o.g_visc = bG * G * we;
+    if (!JSIDE) {
+      acc.gvh = acc.gvh + r_ij * (we * dbdv);
+      if (I.m) acc.grho += drho;
+      acc.sv += bG * Gwe;
+    } else {
+      acc.gv = acc.gv + r_ij * (-we * dbdv);
+      if (J.m) acc.grho += drho;
+    }
   }
   // cohesion, scaled by st: m K C e - m K (n_i - n_j)
-  const float3 wc = w * st;
+  const float3 wc = w * c.st;
   const float wce = dot3(wc, e);
-  const float3 dwce = close ? f3(0.f, 0.f, 0.f) : (wc - e * wce) * (-1.0f / rr);
-  const float rs = rho_i + rho_j;
-  const float Kij = 2.0f * rho0 / rs;
-  const float dK = -Kij / rs;
-  const float r3 = rr * rr * rr;
-  const float dg2 = dg * dg, dg3 = dg2 * dg;
-  const bool far_c = rr >= h * 0.5f;
-  const float C = far_c ? scale_c * dg3 * r3
-                        : scale_c * (2.0f * dg3 * r3 - P.kernel_radius_pow6 / 64.0f);
-  const float Cp = (far_c ? 1.0f : 2.0f) * scale_c * (-3.0f * dg2 * r3 + 3.0f * dg3 * rr * rr);
-  g_r = g_r + (u * (Cp * wce) + dwce * C) * (mass * Kij);
+  const float3 dwce = g.close ? f3(0.f, 0.f, 0.f) : (wc - e * wce) * (-g.inv_rr);
+  const float rs = I.rb + J.rb;
+  const float Kij = 2.0f * c.rho0 / rs;
+  const float mK = c.mass * Kij;
+  g_r = g_r + (u_ij * (g.Cp * wce) + dwce * g.C) * mK;
   const float3 nij = I.n - J.n;
-  o.g_n_i = wc * (-mass * Kij);
-  o.g_n_j = wc * (mass * Kij);
-  const float dKterm = dK * (mass * C * wce - mass * dot3(wc, nij));
-  o.g_rho_i += mi ? dKterm : 0.f;
-  o.g_rho_j += mj ? dKterm : 0.f;
-  o.g_st = mass * Kij * C * we - mass * Kij * dot3(w, nij);
-  o.g_r = g_r;
-  return o;
+  const float dKterm = (-Kij / rs) * (c.mass * g.C * wce - c.mass * dot3(wc, nij));
+  if (!JSIDE) {
+    acc.gn = acc.gn + wc * (-mK);
+    if (I.m) acc.grho += dKterm;
+    acc.ss += mK * g.C * we - mK * dot3(w, nij);
+    acc.gx = acc.gx + g_r;
+  } else {
+    acc.gn = acc.gn + wc * mK;
+    if (J.m) acc.grho += dKterm;
+    acc.gx = acc.gx - g_r;
+  }
 }
 
 __device__ __forceinline__ float3 close_dir(const float4 *dir_tab, int dir_half, uint32_t si,
@@ -352,94 +431,104 @@ __device__ __forceinline__ float3 close_dir(const float4 *dir_tab, int dir_half,
   return fallback_dir_eval(float(si - s_off) - float(sj - s_off));
 }
 
-__global__ void __launch_bounds__(128)
-    k_adj_force(SceneView v, TapeView t, AdjView a, const float4 *__restrict__ dir_tab,
-                int dir_half) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ ForceSide force_side(const TapeView &t, uint32_t i) {
+  ForceSide S;
+  S.x = f3of(__ldg(t.pos + i));
+  S.vhat = f3of(__ldg(t.vhat + i));
+  S.vpre = f3of(__ldg(t.vel + i));
+  S.n = f3of(__ldg(t.nrm + i));
+  const float2 d = __ldg(t.dens + i);
+  S.rb = fmaxf(d.x, 1.0f);
+  S.rnb = fmaxf(d.y, 1.0f);
+  S.m = d.x > 1.0f;
+  S.mn = d.y > 1.0f;
+  return S;
+}
+
+template <int L>
+__device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const SceneView &v,
+                                              const TapeView &t, const AdjView &a,
+                                              const float4 *dir_tab, int dir_half) {
   const bool active = q < v.b->n_sorted;
   const uint32_t scene = active ? t.scene_of_slot[q] : 0u;
-  double acc_visc = 0.0, acc_st = 0.0;
+  (void)scene;
+  ForceAcc acc;
+  acc.gx = acc.gvh = acc.gv = acc.gn = f3(0.f, 0.f, 0.f);
+  acc.grho = acc.grhon = acc.sv = acc.ss = 0.f;
   if (active) {
     const DevUniforms *U = v.u + scene;
-    const GpuSphParams3D &P = U->sph;
-    const float h2 = P.kernel_radius_sq;
-    auto side = [&](uint32_t i) {
-      ForceSide S;
-      S.x = f3of(__ldg(t.pos + i));
-      S.vhat = f3of(__ldg(t.vhat + i));
-      S.vpre = f3of(__ldg(t.vel + i));
-      S.n = f3of(__ldg(t.nrm + i));
-      const float2 d = __ldg(t.dens + i);
-      S.rho = d.x;
-      S.rhon = d.y;
-      return S;
-    };
-    const ForceSide Q = side(q);
+    const ForceConst c = force_const(U->sph);
+    const float h2 = U->sph.kernel_radius_sq;
+    const ForceSide Q = force_side(t, q);
     const float3 wq = f3of(a.ga[q]);
     Runs R;
     flag_outside(a.err, runs_checked(Q.x, U->grid, t.cell_begin + U->c_offset, R));
-    float3 gx = f3(0.f, 0.f, 0.f), gvh = f3(0.f, 0.f, 0.f), gv = f3(0.f, 0.f, 0.f);
-    float3 gn = f3(0.f, 0.f, 0.f);
-    float grho = 0.f, grhon = 0.f;
-    float sv = 0.f, ss = 0.f;
-    for_candidates(R, [&](uint32_t j) {
+    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
       const float3 xj = f3of(__ldg(t.pos + j));
       const float3 r = Q.x - xj;
       const float r2 = dot3(r, r);
       if (!(r2 < h2 && r2 > MIN_R2)) return;
-      const ForceSide Jn = side(j);
-      // (A) T_{q<-j} with q's cotangent: q's i-side
-      const ForcePair A = force_pair_vjp(Q, Jn, wq, close_dir(dir_tab, dir_half, q, j, U->s_offset), P);
-      gx = gx + A.g_r;
-      gvh = gvh + A.g_vhat_i;
-      grho += A.g_rho_i;
-      grhon += A.g_rhon_i;
-      gn = gn + A.g_n_i;
-      sv += A.g_visc;
-      ss += A.g_st;
-      // (B) T_{j<-q} with j's cotangent: q's j-side
+      const ForceSide Jn = force_side(t, j);
+      const PairGeom g = pair_geom(r, r2, c);
       const float3 wj = f3of(__ldg(a.ga + j));
-      const ForcePair B = force_pair_vjp(Jn, Q, wj, close_dir(dir_tab, dir_half, j, q, U->s_offset), P);
-      gx = gx - B.g_r;
-      gv = gv + B.g_vpre_j;
-      grho += B.g_rho_j;
-      grhon += B.g_rhon_j;
-      gn = gn + B.g_n_j;
+      const float3 ec_qj = g.close ? close_dir(dir_tab, dir_half, q, j, U->s_offset) : f3(0.f, 0.f, 0.f);
+      const float3 ec_jq = g.close ? close_dir(dir_tab, dir_half, j, q, U->s_offset) : f3(0.f, 0.f, 0.f);
+      force_half<false>(Q, Jn, g, wq, ec_qj, c, acc);
+      force_half<true>(Jn, Q, g, wj, ec_jq, c, acc);
     });
-    a.gx[q] = f4(add3(f3of(a.gx[q]), gx), 0.f);
-    a.gvhat[q] = f4(add3(f3of(a.gvhat[q]), gvh), 0.f);
-    a.gv[q] = f4(gv, 0.f);
-    a.grho[q] = make_float2(grho, grhon);
-    a.gn[q] = f4(gn, 0.f);
-    // a_c *= st and a = ... + a_c: d/d st = w . sum of raw cohesion terms
-    acc_visc = double(sv);
-    acc_st = double(ss);
   }
-  warp_add_params(a.gparam, scene, acc_visc, acc_st);
+  acc.sv = group_sum<L>(acc.sv);
+  acc.ss = group_sum<L>(acc.ss);
+  acc.gx = group_sum3<L>(acc.gx);
+  acc.gvh = group_sum3<L>(acc.gvh);
+  acc.gv = group_sum3<L>(acc.gv);
+  acc.gn = group_sum3<L>(acc.gn);
+  acc.grho = group_sum<L>(acc.grho);
+  acc.grhon = group_sum<L>(acc.grhon);
+  if (!active || sub != 0u) return;
+  a.gx[q] = f4(add3(f3of(a.gx[q]), acc.gx), 0.f);
+  a.gvhat[q] = f4(add3(f3of(a.gvhat[q]), acc.gvh), 0.f);
+  a.gv[q] = f4(acc.gv, 0.f);
+  a.grho[q] = make_float2(acc.grho, acc.grhon);
+  a.gn[q] = f4(acc.gn, 0.f);
+  // the particle's share of d/d viscosity and d/d surface tension, summed
+  // over steps in canonical order (FP64), reduced per scene at the end
+  double2 &gp = a.gpart[t.s2o[q]];
+  gp = make_double2(gp.x + double(acc.sv), gp.y + double(acc.ss));
+}
+
+template <int L>
+__global__ void __launch_bounds__(128)
+    k_adj_force(TaskQueue tq, SceneView v, TapeView t, AdjView a, const float4 *__restrict__ dir_tab,
+                int dir_half) {
+  for_warp_tasks_sub<L>(tq, [&](uint32_t q, uint32_t sub) {
+    adj_force_one<L>(q, sub, v, t, a, dir_tab, dir_half);
+  });
 }
 
 // ---- XSPH -------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_adj_xsph(SceneView v, TapeView t, AdjView a) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= v.b->n_sorted) return;
-  const DevUniforms *U = v.u + t.scene_of_slot[q];
+template <int L>
+__device__ __forceinline__ void adj_xsph_one(uint32_t q, uint32_t sub, const SceneView &v,
+                                             const TapeView &t, const AdjView &a) {
+  const bool active = q < v.b->n_sorted;
+  const uint32_t qq = active ? q : 0u;
+  const DevUniforms *U = v.u + t.scene_of_slot[qq];
   const GpuSphParams3D &P = U->sph;
   const float h2 = P.kernel_radius_sq, mass = P.mass, eps = P.xsph_epsilon;
-  const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
-  const float3 wq = f3of(a.gvhat[q]);
-  float3 gv = add3(f3of(a.gv[q]), wq);  // vhat = v + eps * sum
-  float3 gx = f3(0.f, 0.f, 0.f);
-  float grho = a.grho[q].x;
-  const float3 xq = f3of(t.pos[q]);
-  const float rho_q = t.dens[q].x;
-  const float gamma_q = boundary_gamma(U->geom, P.kernel_radius, xq);
-  if (eps > 0.0f) {
+  const float3 xq = f3of(t.pos[qq]);
+  const float rho_q = t.dens[qq].x;
+  const float3 wq = f3of(a.gvhat[qq]);
+  float3 gvp = f3(0.f, 0.f, 0.f), gx = f3(0.f, 0.f, 0.f);
+  float grhop = 0.f;
+  if (active && eps > 0.0f) {
+    const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
     const float3 vq = f3of(t.vel[q]);
     const float rb_q = fmaxf(rho_q, 1.0f);
     const float fq = eps * mass / rb_q;
+    const float grho_k = rho_q > 1.0f ? -eps * mass / (rb_q * rb_q) : 0.0f;
     Runs R;
     flag_outside(a.err, runs_checked(xq, U->grid, t.cell_begin + U->c_offset, R));
-    for_candidates(R, [&](uint32_t j) {
+    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
       const float3 xj = f3of(__ldg(t.pos + j));
       const float3 r = xq - xj;  // r_qj
       const float r2 = dot3(r, r);
@@ -448,88 +537,107 @@ __global__ void __launch_bounds__(128) k_adj_xsph(SceneView v, TapeView t, AdjVi
       const float W = scale_d * diff * diff * diff;
       const float dWs = -6.0f * scale_d * diff * diff;  // dW/dr = dWs * r
       const float3 vj = f3of(__ldg(t.vel + j));
-      const float rho_j = __ldg(&t.dens[j].x);
-      const float fj = eps * mass / fmaxf(rho_j, 1.0f);
-      // (A) term_{q<-j} = fj W (v_j - v_q), cotangent wq
-      gv = gv - wq * (fj * W);
-      gx = gx + r * (fj * dot3(wq, vj - vq) * dWs);
-      // (B) term_{j<-q} = fq W (v_q - v_j), cotangent wj; dW/dr_jq = dWs * (-r)
+      const float fj = eps * mass / fmaxf(__ldg(&t.dens[j].x), 1.0f);
       const float3 wj = f3of(__ldg(a.gvhat + j));
-      const float wdv = dot3(wj, vq - vj);
-      gv = gv + wj * (fq * W);
-      if (rho_q > 1.0f) grho += (-eps * mass / (rb_q * rb_q)) * W * wdv;
-      gx = gx + r * (fq * wdv * dWs);  // -(fq wdv dWs (-r))
+      const float3 dv = vj - vq;
+      // (A) term_{q<-j} = fj W (v_j - v_q) with wq; (B) term_{j<-q} = fq W (v_q - v_j) with wj
+      gvp = gvp + (wj * fq - wq * fj) * W;
+      const float wdv = -dot3(wj, dv);
+      grhop += grho_k * W * wdv;
+      gx = gx + r * ((fj * dot3(wq, dv) + fq * wdv) * dWs);
     });
   }
-  a.gv[q] = f4(gv, 0.f);
-  a.gx[q] = f4(add3(f3of(a.gx[q]), gx), 0.f);
+  gvp = group_sum3<L>(gvp);
+  gx = group_sum3<L>(gx);
+  grhop = group_sum<L>(grhop);
+  if (!active || sub != 0u) return;
+  a.gv[q] = f4(add3(add3(f3of(a.gv[q]), wq), gvp), 0.f);  // vhat = v + eps * sum
+  const float grho = a.grho[q].x + grhop;
   // rho = rho_raw / gamma: store the raw density's cotangent and fold the
   // gamma derivative here (d gamma / d x is local to q)
-  const float rb_raw = grho / gamma_q;
-  a.grho[q] = make_float2(rb_raw, a.grho[q].y);
-  // gamma = max(prod_w f_w, 0.1), f_w = 0.5 + 0.5 clamp(d_w / h, 0, 1)
   const GpuContainerGeometry &c = U->geom;
   const float h = P.kernel_radius;
   const float3 l = world_to_local(c, xq);
   const float dw[6] = {l.x + c.half_width, c.half_width - l.x, l.y + c.half_height,
                        c.half_height - l.y, l.z + c.half_depth, c.half_depth - l.z};
-  const float sgn[6] = {1.f, -1.f, 1.f, -1.f, 1.f, -1.f};
   float fw[6], prod = 1.0f;
+#pragma unroll
   for (int w = 0; w < 6; w++) {
     fw[w] = dw[w] < h ? 0.5f + 0.5f * clampf(dw[w] / h, 0.0f, 1.0f) : 1.0f;
     prod *= fw[w];
   }
+  const float gamma_q = fmaxf(prod, 0.1f);
+  const float rb_raw = grho / gamma_q;
+  a.grho[q] = make_float2(rb_raw, a.grho[q].y);
   if (prod > 0.1f && grho != 0.0f) {
     const float gamma_b = -rb_raw * rho_q;  // d rho / d gamma = -rho_raw / gamma^2
     float lg[3] = {0.f, 0.f, 0.f};
+#pragma unroll
     for (int w = 0; w < 6; w++) {
       if (!(dw[w] < h && dw[w] > 0.0f)) continue;  // clamp saturated or inactive
       float others = 1.0f;
+#pragma unroll
       for (int o = 0; o < 6; o++)
         if (o != w) others *= fw[o];
-      lg[w >> 1] += gamma_b * others * (0.5f / h) * sgn[w];
+      lg[w >> 1] += gamma_b * others * (0.5f / h) * ((w & 1) ? -1.0f : 1.0f);
     }
-    const float3 xg = local_dir_to_world(c, f3(lg[0], lg[1], lg[2]));  // Ri^T
-    a.gx[q] = f4(add3(f3of(a.gx[q]), xg), 0.f);
+    gx = gx + local_dir_to_world(c, f3(lg[0], lg[1], lg[2]));  // Ri^T
   }
+  a.gx[q] = f4(add3(f3of(a.gx[q]), gx), 0.f);
+}
+
+template <int L>
+__global__ void __launch_bounds__(128) k_adj_xsph(TaskQueue tq, SceneView v, TapeView t, AdjView a) {
+  for_warp_tasks_sub<L>(tq, [&](uint32_t q, uint32_t sub) { adj_xsph_one<L>(q, sub, v, t, a); });
 }
 
 // ---- density, near density, normal ------------------------------------------------------
-__global__ void __launch_bounds__(128) k_adj_density(SceneView v, TapeView t, AdjView a) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= v.b->n_sorted) return;
-  const DevUniforms *U = v.u + t.scene_of_slot[q];
-  const GpuSphParams3D &P = U->sph;
-  const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
-  const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
-  const float scale_n = 15.0f / (PI_F * P.kernel_radius_pow6);
-  const float h8 = P.kernel_radius_pow6 * h * h;
-  const float cnorm = 945.0f / (32.0f * PI_F * h8) * (mass / P.rest_density);
-  const float3 xq = f3of(t.pos[q]);
-  const float2 gq = a.grho[q];
-  const float3 nq = f3of(a.gn[q]);
-  Runs R;
-  flag_outside(a.err, runs_checked(xq, U->grid, t.cell_begin + U->c_offset, R));
+template <int L>
+__device__ __forceinline__ void adj_density_one(uint32_t q, uint32_t sub, const SceneView &v,
+                                                const TapeView &t, const AdjView &a) {
+  const bool active = q < v.b->n_sorted;
   float3 gx = f3(0.f, 0.f, 0.f);
-  // d/dr of one ordered pair's terms, r = x_i - x_j, with i's cotangents
-  auto pair = [&](float3 r, float r2, float2 gi, float3 ni) {
-    const float diff = h2 - r2;
-    const float rr = sqrtf(r2);
-    const float dn = h - rr;
-    float3 g = r * (-6.0f * mass * scale_d * diff * diff * gi.x);
-    g = g + r * (-3.0f * mass * scale_n * dn * dn * gi.y / rr);
-    g = g + (ni * (diff * diff) - r * (4.0f * diff * dot3(ni, r))) * cnorm;
-    return g;
-  };
-  for_candidates(R, [&](uint32_t j) {
-    const float3 xj = f3of(__ldg(t.pos + j));
-    const float3 r = xq - xj;
-    const float r2 = dot3(r, r);
-    if (!(r2 < h2 && r2 > MIN_R2)) return;
-    gx = gx + pair(r, r2, gq, nq);
-    gx = gx - pair(-r, r2, __ldg(a.grho + j), f3of(__ldg(a.gn + j)));
-  });
+  if (active) {
+    const DevUniforms *U = v.u + t.scene_of_slot[q];
+    const GpuSphParams3D &P = U->sph;
+    const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
+    const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
+    const float scale_n = 15.0f / (PI_F * P.kernel_radius_pow6);
+    const float h8 = P.kernel_radius_pow6 * h * h;
+    const float cnorm = 945.0f / (32.0f * PI_F * h8) * (mass / P.rest_density);
+    const float c_rho = -6.0f * mass * scale_d, c_near = -3.0f * mass * scale_n;
+    const float3 xq = f3of(t.pos[q]);
+    const float2 gq = a.grho[q];
+    const float3 nq = f3of(a.gn[q]);
+    Runs R;
+    flag_outside(a.err, runs_checked(xq, U->grid, t.cell_begin + U->c_offset, R));
+    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
+      const float3 xj = f3of(__ldg(t.pos + j));
+      const float3 r = xq - xj;  // r_qj; the pair (j, q) has r_jq = -r
+      const float r2 = dot3(r, r);
+      if (!(r2 < h2 && r2 > MIN_R2)) return;
+      const float2 gj = __ldg(a.grho + j);
+      const float3 nj = f3of(__ldg(a.gn + j));
+      const float diff = h2 - r2;
+      const float rr = sqrtf(r2);
+      const float dn = h - rr;
+      // d/dr_qj of q's terms minus d/dr_jq of j's terms (both odd in r except
+      // the normal's, which is even): the radial parts add, the normal parts
+      // subtract
+      const float radial =
+          c_rho * diff * diff * (gq.x + gj.x) + c_near * dn * dn * (gq.y + gj.y) / rr;
+      const float3 dnrm = nq - nj;
+      gx = gx + r * radial + (dnrm * (diff * diff) - r * (4.0f * diff * dot3(dnrm, r))) * cnorm;
+    });
+  }
+  gx = group_sum3<L>(gx);
+  if (!active || sub != 0u) return;
   a.gx[q] = f4(add3(f3of(a.gx[q]), gx), 0.f);
+}
+
+template <int L>
+__global__ void __launch_bounds__(128) k_adj_density(TaskQueue tq, SceneView v, TapeView t, AdjView a) {
+  for_warp_tasks_sub<L>(tq, [&](uint32_t q, uint32_t sub) { adj_density_one<L>(q, sub, v, t, a); });
 }
 
 // ---- back to canonical order ---------------------------------------------------------------
@@ -616,6 +724,37 @@ __global__ void __launch_bounds__(128)
   xbar[i] = f4(g, 0.f);
 }
 
+// Per-scene sums of the particles' parameter-gradient shares in a fixed
+// order: one block per scene, strided partial sums then a shared-memory tree.
+__global__ void __launch_bounds__(256)
+    k_reduce_params(const double2 *__restrict__ gpart, const uint32_t *__restrict__ scene_first,
+                    const uint32_t *__restrict__ scene_count, double *__restrict__ gparam) {
+  __shared__ double sv[256], ss[256];
+  const uint32_t sc = blockIdx.x;
+  const uint32_t first = scene_first[sc], count = scene_count[sc];
+  double v = 0.0, w = 0.0;
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    const double2 g = gpart[first + i];
+    v += g.x;
+    w += g.y;
+  }
+  sv[threadIdx.x] = v;
+  ss[threadIdx.x] = w;
+  __syncthreads();
+  for (unsigned o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sv[threadIdx.x] += sv[threadIdx.x + o];
+      ss[threadIdx.x] += ss[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    gparam[3 * sc + 0] = sv[0];
+    gparam[3 * sc + 1] = 0.0;  // stiffness: read by no stage of the step
+    gparam[3 * sc + 2] = ss[0];
+  }
+}
+
 // (N, 3) float rows <-> float4 records (w = 0)
 __global__ void __launch_bounds__(256)
     k_rows_to_f4(uint32_t n, const float *__restrict__ rows, float4 *__restrict__ out) {
@@ -636,6 +775,14 @@ inline unsigned blocks_for(uint32_t n, unsigned threads) { return (n + threads -
 
 }  // namespace
 
+cudaError_t launch_reduce_params(const double2 *gpart, const uint32_t *scene_first,
+                                 const uint32_t *scene_count, uint32_t scenes, double *gparam,
+                                 cudaStream_t st) {
+  if (scenes == 0) return cudaSuccess;
+  k_reduce_params<<<scenes, 256, 0, st>>>(gpart, scene_first, scene_count, gparam);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_rows_to_f4(uint32_t n, const float *rows, float4 *out, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_rows_to_f4<<<blocks_for(n, 256), 256, 0, st>>>(n, rows, out);
@@ -647,17 +794,61 @@ cudaError_t launch_f4_to_rows(uint32_t n, const float4 *in, float *rows, cudaStr
   return cudaGetLastError();
 }
 
+template <class K>
+unsigned resident_blocks(K kernel, int sm_count) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return unsigned(per_sm * sm_count);
+}
+
+namespace {
+template <int L>
+struct AdjBlocks {
+  unsigned solve = 0, force = 0, xsph = 0, density = 0;
+};
+
+template <int L>
+cudaError_t adj_gathers(const SceneView &v, const TapeView &t, const AdjView &a,
+                        const float4 *dir_tab, int dir_half, uint32_t n, int K, int sm_count,
+                        cudaStream_t st) {
+  static AdjBlocks<L> b;
+  if (!b.solve) {
+    b.solve = resident_blocks(k_adj_solve<L>, sm_count);
+    b.force = resident_blocks(k_adj_force<L>, sm_count);
+    b.xsph = resident_blocks(k_adj_xsph<L>, sm_count);
+    b.density = resident_blocks(k_adj_density<L>, sm_count);
+  }
+  const uint32_t nwarps = (n + 31u) / 32u;
+  auto queue = [&](int slot) { return TaskQueue{t.order, a.counters + slot, nwarps}; };
+  for (int k = K - 1; k >= 0; k--)
+    k_adj_solve<L><<<b.solve, 128, 0, st>>>(queue(k), v, t, a, t.xp[k], t.rho[k],
+                                            k >= 1 ? t.ap[k - 1] : nullptr, a.gu[k & 1],
+                                            a.gu[(k + 1) & 1], k, K);
+  k_adj_force<L><<<b.force, 128, 0, st>>>(queue(K), v, t, a, dir_tab, dir_half);
+  k_adj_xsph<L><<<b.xsph, 128, 0, st>>>(queue(K + 1), v, t, a);
+  k_adj_density<L><<<b.density, 128, 0, st>>>(queue(K + 2), v, t, a);
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_adj_step(const SceneView &v, const TapeView &t, const AdjView &a,
                             const float4 *xbar_in, const float4 *vbar_in, float4 *xbar_out,
                             float4 *vbar_out, const float4 *dir_tab, int dir_half, uint32_t n,
-                            int K, cudaStream_t st) {
+                            int K, int lanes, int sm_count, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  const unsigned b = blocks_for(n, 128);
-  k_adj_integrate<<<b, 128, 0, st>>>(v, t, a, xbar_in, vbar_in, K);
-  for (int k = K - 1; k >= 0; k--) k_adj_solve<<<b, 128, 0, st>>>(v, t, a, k, K);
-  k_adj_force<<<b, 128, 0, st>>>(v, t, a, dir_tab, dir_half);
-  k_adj_xsph<<<b, 128, 0, st>>>(v, t, a);
-  k_adj_density<<<b, 128, 0, st>>>(v, t, a);
+  // one task counter per gather launch: K solves, force, XSPH, density
+  cudaError_t e = cudaMemsetAsync(a.counters, 0, sizeof(uint32_t) * (K + 3), st);
+  if (e != cudaSuccess) return e;
+  k_adj_integrate<<<blocks_for(n, 128), 128, 0, st>>>(v, t, a, xbar_in, vbar_in, t.ap[K - 1], K);
+  switch (lanes) {
+    case 8: e = adj_gathers<8>(v, t, a, dir_tab, dir_half, n, K, sm_count, st); break;
+    case 4: e = adj_gathers<4>(v, t, a, dir_tab, dir_half, n, K, sm_count, st); break;
+    case 2: e = adj_gathers<2>(v, t, a, dir_tab, dir_half, n, K, sm_count, st); break;
+    default: e = adj_gathers<1>(v, t, a, dir_tab, dir_half, n, K, sm_count, st); break;
+  }
+  if (e != cudaSuccess) return e;
   k_adj_to_canonical<<<blocks_for(n, 256), 256, 0, st>>>(v, t, a, xbar_out, vbar_out);
   return cudaGetLastError();
 }

@@ -12,6 +12,8 @@
 // with the kernels of adj_kernels.cu. Memory: the checkpoints, one segment of
 // tape and the reverse accumulators.
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -31,6 +33,7 @@ struct TapeSlot {
   float4 *xp[kMaxAdjIters + 1];
   float *rho[kMaxAdjIters + 1];
   float4 *ap[kMaxAdjIters];
+  uint32_t *order;
 };
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -72,6 +75,8 @@ struct FsAdj {
   float *field = nullptr, *target = nullptr, *gg = nullptr;
   double *loss = nullptr;
   size_t vox_cap = 0;
+  int lanes = 0;  // lanes per particle of the reverse gathers (autotuned)
+  uint32_t *scene_first = nullptr, *scene_count = nullptr;  // device, canonical ranges
 };
 
 namespace {
@@ -107,6 +112,7 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
       t.rho[k] = c.take<float>(N);
     }
     for (uint32_t k = 0; k < a->K; k++) t.ap[k] = c.take<float4>(N);
+    t.order = c.take<uint32_t>((N + 31) / 32);
   }
   AdjView &v = a->av;
   v.gx = c.take<float4>(N);
@@ -119,6 +125,10 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
   v.gu[0] = c.take<float4>(N);
   v.gu[1] = c.take<float4>(N);
   v.gparam = c.take<double>(3 * size_t(a->scenes));
+  v.gpart = c.take<double2>(N);
+  a->scene_first = c.take<uint32_t>(a->scenes);
+  a->scene_count = c.take<uint32_t>(a->scenes);
+  v.counters = c.take<uint32_t>(kMaxAdjIters + 3);
   for (auto &b : a->cot)
     for (auto &p : b) p = c.take<float4>(N);
   *bytes = c.off;
@@ -164,6 +174,7 @@ DevState recording_state(const FsAdj *a, const TapeSlot &t) {
   dv.rec_xp = t.xp;
   dv.rec_rho = t.rho;
   dv.rec_ap = t.ap;
+  dv.warp_order = t.order;
   return dv;
 }
 
@@ -184,6 +195,7 @@ TapeView tape_view(const TapeSlot &t, uint32_t K) {
     v.rho[k] = t.rho[k];
   }
   for (uint32_t k = 0; k < K; k++) v.ap[k] = t.ap[k];
+  v.order = t.order;
   return v;
 }
 
@@ -214,6 +226,59 @@ int check_supported(const char *who, FsSim *s) {
                   k);
   }
   return FS_OK;
+}
+
+// Autotuner of the reverse gathers' lanes per particle, per particle-count
+// bucket (floor(log2 N)) and iteration count: on the first backward of a
+// bucket every candidate runs the last recorded step's reverse once (the
+// reverse of a step is idempotent apart from the parameter sums, which are
+// cleared afterwards) and the fastest is kept for the process.
+std::mutex g_tune_mu;
+std::map<uint64_t, int> g_tuned_lanes;
+
+int tune_lanes(FsAdj *a, const SceneView &v, const TapeView &tv) {
+  FsSim *s = a->sim;
+  uint32_t bucket = 0;
+  while ((2u << bucket) <= a->N && bucket < 31) bucket++;
+  const uint64_t key = (uint64_t(bucket) << 32) | a->K;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned_lanes.find(key);
+    if (it != g_tuned_lanes.end()) return it->second;
+  }
+  cudaEvent_t e0, e1;
+  FS_CUDA(cudaEventCreate(&e0), "tuner event");
+  FS_CUDA(cudaEventCreate(&e1), "tuner event");
+  int best = 1;
+  float best_ms = 0.0f;
+  const int cand[4] = {1, 2, 4, 8};
+  for (int rep = 0; rep < 2; rep++)  // the first pass warms every variant up
+    for (int L : cand) {
+      cudaEventRecord(e0, s->stream);
+      cudaError_t e = launch_adj_step(v, tv, a->av, a->cot[a->cur][0], a->cot[a->cur][1],
+                                      a->cot[a->cur ^ 1][0], a->cot[a->cur ^ 1][1], s->d.dir_tab,
+                                      s->d.dir_half, a->N, int(a->K), L, s->d.sm_count, s->stream);
+      cudaEventRecord(e1, s->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(e, "reverse-pass tuning");
+      }
+      if (rep == 1 && (best_ms == 0.0f || ms < best_ms)) {
+        best_ms = ms;
+        best = L;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  FS_CUDA(cudaMemsetAsync(a->av.gpart, 0, sizeof(double2) * a->N, s->stream),
+          "clear parameter gradients");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tuned_lanes[key] = best;
+  return best;
 }
 
 #define CHECK_ADJ(a) \
@@ -255,6 +320,7 @@ int fs_adj_forward(FsAdj *a, uint32_t nsteps) {
   int rc;
   if ((rc = set_device(s))) return rc;
   if ((rc = check_supported(__func__, s))) return rc;
+  if (a->K != s->iterations || a->N != s->hb.n_canon) a->lanes = 0;
   a->K = s->iterations;
   a->N = s->hb.n_canon;
   a->G = s->cells_total;
@@ -393,8 +459,22 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
       std::memcmp(s->hu.data(), a->hu_snapshot.data(), sizeof(DevUniforms) * a->scenes) != 0)
     return fail(FS_E_STATE, "fs_adj_backward: parameters changed since fs_adj_forward");
   const uint32_t N = a->N, K = a->K;
-  FS_CUDA(cudaMemsetAsync(a->av.gparam, 0, sizeof(double) * 3 * a->scenes, s->stream),
+  FS_CUDA(cudaMemsetAsync(a->av.gpart, 0, sizeof(double2) * N, s->stream),
           "clear parameter gradients");
+  {
+    std::vector<uint32_t> first(a->scenes), count(a->scenes);
+    for (uint32_t k = 0; k < a->scenes; k++) {
+      first[k] = s->hu[k].p_offset;
+      count[k] = s->scene_n[k];
+    }
+    FS_CUDA(cudaMemcpyAsync(a->scene_first, first.data(), sizeof(uint32_t) * a->scenes,
+                            cudaMemcpyHostToDevice, s->stream),
+            "scene ranges");
+    FS_CUDA(cudaMemcpyAsync(a->scene_count, count.data(), sizeof(uint32_t) * a->scenes,
+                            cudaMemcpyHostToDevice, s->stream),
+            "scene ranges");
+    FS_CUDA(cudaStreamSynchronize(s->stream), "scene ranges");
+  }
   const uint32_t nck = (a->steps + a->every - 1) / a->every;
   const SceneView base = s->d.view();
   for (uint32_t seg = nck; seg-- > 0;) {
@@ -409,10 +489,15 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
       const TapeSlot &slot = a->tape[t];
       SceneView v = base;
       v.scene_of_slot = slot.sos;
+      if (a->lanes == 0) {
+        const int L = tune_lanes(a, v, tape_view(slot, K));
+        if (L < 0) return L;
+        a->lanes = L;
+      }
       const int nxt = a->cur ^ 1;
       FS_CUDA(launch_adj_step(v, tape_view(slot, K), a->av, a->cot[a->cur][0], a->cot[a->cur][1],
                               a->cot[nxt][0], a->cot[nxt][1], s->d.dir_tab, s->d.dir_half, N,
-                              int(K), s->stream),
+                              int(K), a->lanes, s->d.sm_count, s->stream),
               "reverse step");
       a->cur = nxt;
     }
@@ -437,6 +522,9 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
       }
     }
   }
+  FS_CUDA(launch_reduce_params(a->av.gpart, a->scene_first, a->scene_count, a->scenes,
+                               a->av.gparam, s->stream),
+          "parameter gradients");
   if (dl_dparams)
     FS_CUDA(cudaMemcpyAsync(dl_dparams, a->av.gparam, sizeof(double) * 3 * a->scenes,
                             cudaMemcpyDeviceToHost, s->stream),

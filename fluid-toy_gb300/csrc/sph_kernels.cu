@@ -460,24 +460,6 @@ __device__ __forceinline__ void solve_one(
 // order, the heaviest blocks form a tail. Instead, persistent warps pull
 // 32-slot tasks from a queue ordered heaviest first (longest-processing-time
 // scheduling); which warp computes a particle does not change its result.
-struct TaskQueue {
-  const uint32_t *order;  // task t -> warp index (32 slots)
-  uint32_t *counter;      // next task, zeroed before each launch
-  uint32_t nwarps;
-};
-
-template <class F>
-__device__ __forceinline__ void for_warp_tasks(const TaskQueue &q, F &&f) {
-  const unsigned lane = threadIdx.x & 31u;
-  while (true) {
-    uint32_t t = 0u;
-    if (lane == 0u) t = atomicAdd(q.counter, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= q.nwarps) break;
-    f(__ldg(q.order + t) * 32u + lane);
-  }
-}
-
 // Task order, heaviest first: k_warp_work puts every warp (32 sorted slots)
 // in a bucket floor(log2(max candidates of its particles)) + 1 and counts the
 // buckets; k_scatter_order writes the warps bucket by bucket, heaviest bucket

@@ -6,6 +6,9 @@ with nvcc for ``sm_103a`` only and linked in-tree into
 ``-fmad=false`` keeps every float expression in the shaders' evaluation order
 (no fused multiply-add), IEEE division and square root are nvcc's defaults,
 and host code is built with ``-ffp-contract=off`` for the same reason.
+The reverse-pass kernels (``adj_kernels.cu``) reproduce no reference bits:
+they are built with fused multiply-add and the approximate division and
+square root (``FILE_FLAGS``).
 """
 from __future__ import annotations
 
@@ -35,6 +38,20 @@ NVCC_FLAGS = [
     "-I",
     str(INCLUDE),
 ]
+
+
+# per-file replacements of NVCC_FLAGS entries
+FILE_FLAGS = {
+    "adj_kernels.cu": {"-fmad=false": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]},
+}
+
+
+def _flags_for(src: Path) -> list[str]:
+    sub = FILE_FLAGS.get(src.name, {})
+    out: list[str] = []
+    for f in NVCC_FLAGS:
+        out.extend(sub.get(f, [f]))
+    return out
 
 
 def _nvcc() -> str:
@@ -67,7 +84,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src: Path) -> Path:
         obj = BUILD_DIR / (src.name + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *ARCH, *_flags_for(src), "-c", str(src), "-o", str(obj)]
         if src.suffix == ".cpp":
             cmd = [nvcc, *NVCC_FLAGS, "-x", "c++", "-c", str(src), "-o", str(obj)]
         if verbose:
