@@ -285,6 +285,23 @@ def run_ours(args, dist: Dist) -> dict | None:
     e2e_value, _ = aggregate(n * K, e2e_secs, dist)
     sim.close()
 
+    forms = None
+    if not args.no_forms:
+        # the two other forms of the metric, on their own workloads (every rank
+        # takes part: the batched arm aggregates over ranks)
+        import argparse as _ap
+        b = run_batch(_ap.Namespace(steps=50, warmup=3, loop_steps=10), dist)
+        a = run_adjoint(_ap.Namespace(steps=200, warmup=3), dist)
+        if dist.rank == 0:
+            forms = {
+                "batched": {k: b[k] for k in ("value", "unit", "ms_per_step", "looped_plain",
+                                              "batched_over_looped", "config", "clocks",
+                                              "gpu_launches")},
+                "adjoint": {k: a[k] for k in ("value", "unit", "forward_ms_per_step",
+                                              "fwd_adjoint_over_forward", "gradient_finite",
+                                              "config")},
+            }
+
     if dist.rank != 0:
         return None
 
@@ -356,9 +373,11 @@ def run_ours(args, dist: Dist) -> dict | None:
                 "d2h_bytes_per_step": d2h,
                 "pattern": "per step: upload sph/geometry/gravity/rigid-body structs, "
                            "fs_step(1), read rigid-body accumulator (sync)"},
-        "gpu_launches": K * (8 + scene.iterations),
+        "gpu_launches": K * (10 + scene.iterations),
         "clocks": clk,
     }
+    if forms is not None:
+        out["forms"] = forms
     if state_after_warmup is not None:
         cs = cpu_sample(scene, state_after_warmup, args.cpu_steps)
         cs["sample"] = (f"{scene.name}: oracle (FP32 C++ restatement, OpenMP) from the GPU "
@@ -454,7 +473,7 @@ def run_batch(args, dist: Dist) -> dict | None:
                          "pattern": "one SphSimulation3DGrid per scene on one stream, "
                                     "each fs_step(k) graph-replayed, scene after scene"},
         "batched_over_looped": round(value / loop_value, 3) if loop_value else None,
-        "gpu_launches": K * (8 + scenes[0].iterations),
+        "gpu_launches": K * (10 + scenes[0].iterations),
         "clocks": clk,
     }
 
@@ -576,6 +595,8 @@ def main():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched and differentiable forms in the default run")
     ap.add_argument("--loop-steps", type=int, default=20,
                     help="steps per scene of the looped-plain comparison (--config 2)")
     args = ap.parse_args()
