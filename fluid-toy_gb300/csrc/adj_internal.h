@@ -19,7 +19,7 @@ struct TapeView {
   const float4 *xp[kMaxAdjIters + 1];  // predicted (x*, p) per level
   const float *rho[kMaxAdjIters + 1];  // predicted densities per level
   const float4 *ap[kMaxAdjIters];      // pressure acceleration before the clamp
-  const uint32_t *order;               // the step's neighbour-pass task order
+  const uint32_t *order;               // the step's task order (warp ids, heaviest first)
 };
 
 // Reverse accumulators, grid-sorted order.

@@ -80,10 +80,10 @@ template <int L>
 __device__ __forceinline__ float3 group_sum3(float3 x) {
   return make_float3(group_sum<L>(x.x), group_sum<L>(x.y), group_sum<L>(x.z));
 }
-// Tasks of 32 / L sorted slots with L lanes per particle: the recorded order
-// of 32-slot warps (heaviest first) split L ways, so a heavy warp's particles
-// spread over L concurrently running warps and the critical path (the
-// heaviest particle's candidate list) shrinks L-fold.
+// Tasks of 32 / L slots with L lanes per particle: each 32-slot warp of the
+// recorded task order (heaviest first) split L ways, so a heavy warp's
+// particles spread over L concurrently running warps and the critical path
+// (the heaviest particle's candidate list) shrinks L-fold.
 template <int L, class F>
 __device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
   const unsigned lane = threadIdx.x & 31u;
@@ -93,8 +93,7 @@ __device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
     if (lane == 0u) t = atomicAdd(q.counter, 1u);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= ntasks) break;
-    const uint32_t base = __ldg(q.order + t / L) * 32u + (t % L) * (32u / L);
-    f(base + lane / L, lane % L);
+    f(__ldg(q.perm + t / L) * 32u + (t % L) * (32u / L) + lane / L, lane % L);
   }
 }
 
@@ -821,7 +820,7 @@ cudaError_t adj_gathers(const SceneView &v, const TapeView &t, const AdjView &a,
     b.density = resident_blocks(k_adj_density<L>, sm_count);
   }
   const uint32_t nwarps = (n + 31u) / 32u;
-  auto queue = [&](int slot) { return TaskQueue{t.order, a.counters + slot, nwarps}; };
+  auto queue = [&](int slot) { return TaskQueue{t.order, a.counters + slot, n, nwarps, false}; };
   for (int k = K - 1; k >= 0; k--)
     k_adj_solve<L><<<b.solve, 128, 0, st>>>(queue(k), v, t, a, t.xp[k], t.rho[k],
                                             k >= 1 ? t.ap[k - 1] : nullptr, a.gu[k & 1],

@@ -95,10 +95,15 @@ struct DevState {
   uint32_t *mask_words;            // per-particle hit bitmasks (see sph_kernels.cu)
   uint32_t *mask_off;              // word offset of each sorted slot's mask
   uint32_t *mask_hits;             // set bits in each sorted slot's mask
-  uint32_t *warp_order;            // neighbour-pass task order (warp ids, heaviest first)
-  uint32_t *task_counters;         // one task counter per neighbour-pass launch
-  uint8_t *warp_bucket;            // work bucket of each warp of sorted slots
+  // Neighbour-pass work order (heaviest first): warps of 32 sorted slots for
+  // density, XSPH and solve; a slot permutation by hit count for force.
+  uint32_t *warp_order;            // [M / 32] warp ids
+  uint8_t *warp_bucket;            // [M / 32] work bucket of each warp
   uint32_t *order_hist;            // bucket counts, then bucket cursors
+  uint32_t *perm_hit;              // [M] sorted slots by decreasing hit count
+  uint16_t *work_key;              // [M] hit-count bucket of each sorted slot
+  uint32_t *key_hist;              // [3 * KEY_BUCKETS]: counts, bases, cursors
+  uint32_t *task_counters;         // one task counter per neighbour-pass launch
   int sm_count;                    // streaming multiprocessors of the device
   unsigned long long *mask_alloc;  // bump allocator of mask words
   unsigned long long mask_cap;     // mask capacity in words
@@ -163,7 +168,10 @@ cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_
 cudaError_t launch_dir_table(const DevState &d, cudaStream_t st);
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st);
 constexpr int TASK_COUNTERS = 16;
+constexpr int KEY_BUCKETS = 8192;
+// Warp order (before density) and the force pass's hit permutation (after it).
 cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st);
+cudaError_t launch_order_hits(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last,

@@ -122,9 +122,12 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.mask_off = c.take<uint32_t>(M);
   d.mask_hits = c.take<uint32_t>(M);
   d.warp_order = c.take<uint32_t>((M + 31) / 32);
-  d.task_counters = c.take<uint32_t>(TASK_COUNTERS);
   d.warp_bucket = c.take<uint8_t>((M + 31) / 32);
   d.order_hist = c.take<uint32_t>(2 * 33);
+  d.perm_hit = c.take<uint32_t>(M);
+  d.work_key = c.take<uint16_t>(M);
+  d.key_hist = c.take<uint32_t>(3 * KEY_BUCKETS);
+  d.task_counters = c.take<uint32_t>(TASK_COUNTERS);
   d.mask_alloc = c.take<unsigned long long>(1);
   d.dir_half = int(std::min<size_t>(M, size_t(1) << 20));
   d.dir_tab = c.take<float4>(2 * size_t(d.dir_half) + 1);
@@ -268,6 +271,7 @@ int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv) {
   if ((rc = mark(4))) return rc;
   FS_CUDA(launch_order_warps(d, n, st), "neighbour-pass work order");
   FS_CUDA(launch_density(d, n, st), "density");
+  FS_CUDA(launch_order_hits(d, n, st), "neighbour-pass work order (hits)");
   if ((rc = mark(5))) return rc;
   FS_CUDA(launch_xsph(d, n, st), "xsph");
   if ((rc = mark(6))) return rc;

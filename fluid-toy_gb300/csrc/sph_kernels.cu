@@ -455,11 +455,27 @@ __device__ __forceinline__ void solve_one(
 }
 
 // ---- work ordering -------------------------------------------------------------
-// The neighbour passes' cost per warp (32 consecutive sorted slots) ranges over
-// two orders of magnitude: the clumps carry most of the pairs. Launched in slot
-// order, the heaviest blocks form a tail. Instead, persistent warps pull
+// The neighbour passes' cost per particle ranges over two orders of
+// magnitude (the clumps carry most of the pairs). Persistent warps take
 // 32-slot tasks from a queue ordered heaviest first (longest-processing-time
-// scheduling); which warp computes a particle does not change its result.
+// scheduling). Density, XSPH and solve take warps of 32 consecutive sorted
+// slots (neighbouring particles share their neighbours' loads in L1); the
+// force pass, whose per-hit body is long, takes 32 slots of similar hit
+// count from a permutation built by a counting sort on a log-linear work key,
+// so its lanes finish together. Which lane computes a particle does not
+// change its result.
+__device__ __forceinline__ uint32_t work_key(uint32_t c) {
+  return c < 4096u ? c : 4096u + min((c - 4096u) >> 4, 4095u);
+}
+
+// Count a key with warp-aggregated atomics; returns nothing.
+__device__ __forceinline__ void count_key(bool active, uint32_t k, uint32_t *hist) {
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const unsigned peers = __match_any_sync(act, k);
+  if (int(threadIdx.x & 31u) == __ffs(peers) - 1) atomicAdd(&hist[k], uint32_t(__popc(peers)));
+}
+
 // Task order, heaviest first: k_warp_work puts every warp (32 sorted slots)
 // in a bucket floor(log2(max candidates of its particles)) + 1 and counts the
 // buckets; k_scatter_order writes the warps bucket by bucket, heaviest bucket
@@ -503,6 +519,64 @@ __global__ void __launch_bounds__(256)
   if (w >= (v.b->n_sorted + 31u) / 32u) return;
   const uint32_t b = warp_bucket[w];
   order[base[b] + atomicAdd(&cursor[b], 1u)] = w;
+}
+
+__global__ void __launch_bounds__(256)
+    k_hit_keys(SceneView v, const uint32_t *__restrict__ mask_hits, uint16_t *__restrict__ key,
+               uint32_t *__restrict__ hist) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = s < v.b->n_sorted;
+  uint32_t k = 0u;
+  if (active) {
+    k = work_key(mask_hits[s]);
+    key[s] = uint16_t(k);
+  }
+  count_key(active, k, hist);
+}
+
+// Exclusive bases of the key buckets, heaviest bucket first (one block).
+__global__ void __launch_bounds__(1024) k_key_bases(const uint32_t *__restrict__ hist,
+                                                    uint32_t *__restrict__ base) {
+  constexpr int PER = KEY_BUCKETS / 1024;
+  __shared__ uint32_t part[1024];
+  const int t = threadIdx.x;
+  uint32_t local[PER], sum = 0u;
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    local[i] = hist[KEY_BUCKETS - 1 - (t * PER + i)];
+    sum += local[i];
+  }
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const uint32_t add = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += add;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - sum;
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    base[KEY_BUCKETS - 1 - (t * PER + i)] = run;
+    run += local[i];
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_key_scatter(SceneView v, const uint16_t *__restrict__ key, const uint32_t *__restrict__ base,
+                  uint32_t *__restrict__ cursor, uint32_t *__restrict__ perm) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = s < v.b->n_sorted;
+  const uint32_t k = active ? key[s] : 0u;
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  if (!active) return;
+  const unsigned peers = __match_any_sync(act, k);
+  const int leader = __ffs(peers) - 1;
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t pos = 0u;
+  if (int(lane) == leader) pos = atomicAdd(&cursor[k], uint32_t(__popc(peers)));
+  pos = __shfl_sync(peers, pos, leader);
+  perm[base[k] + pos + uint32_t(__popc(peers & ((1u << lane) - 1u)))] = s;
 }
 
 __global__ void __launch_bounds__(128)
@@ -837,11 +911,21 @@ unsigned persistent_blocks(K kernel, int sm_count) {
   return unsigned(per_sm * sm_count);
 }
 
-cudaError_t prepare_queue(const DevState &d, uint32_t n, int slot, cudaStream_t st, TaskQueue *q) {
-  q->order = d.warp_order;
+cudaError_t prepare_queue(const DevState &d, const uint32_t *order, bool slots, uint32_t n,
+                          int slot, cudaStream_t st, TaskQueue *q) {
+  q->perm = order;
+  q->slots = slots;
   q->counter = d.task_counters + slot;
+  q->n = n;
   q->nwarps = (n + 31u) / 32u;
   return cudaMemsetAsync(q->counter, 0, sizeof(uint32_t), st);
+}
+
+cudaError_t order_by_keys(const DevState &d, uint32_t n, uint32_t *perm, cudaStream_t st) {
+  k_key_bases<<<1, 1024, 0, st>>>(d.key_hist, d.key_hist + KEY_BUCKETS);
+  k_key_scatter<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.work_key, d.key_hist + KEY_BUCKETS,
+                                                    d.key_hist + 2 * KEY_BUCKETS, perm);
+  return cudaGetLastError();
 }
 }  // namespace
 
@@ -858,12 +942,20 @@ cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+cudaError_t launch_order_hits(const DevState &d, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d.key_hist, 0, sizeof(uint32_t) * 3 * KEY_BUCKETS, st);
+  if (e != cudaSuccess) return e;
+  k_hit_keys<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.mask_hits, d.work_key, d.key_hist);
+  return order_by_keys(d, n, d.perm_hit, st);
+}
+
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d.mask_alloc, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   TaskQueue q;
-  e = prepare_queue(d, n, TASK_COUNTERS - 1, st, &q);
+  e = prepare_queue(d, d.warp_order, false, n, TASK_COUNTERS - 1, st, &q);
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_density, d.sm_count);
@@ -876,7 +968,7 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   TaskQueue q;
-  cudaError_t e = prepare_queue(d, n, 0, st, &q);
+  cudaError_t e = prepare_queue(d, d.warp_order, false, n, 0, st, &q);
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_xsph, d.sm_count);
@@ -888,7 +980,7 @@ cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   TaskQueue q;
-  cudaError_t e = prepare_queue(d, n, 1, st, &q);
+  cudaError_t e = prepare_queue(d, d.perm_hit, true, n, 1, st, &q);
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count);
@@ -910,7 +1002,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   float *rho_out = d.rec_rho ? d.rec_rho[iter + 1] : d.pred_rho[out];
   float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
   TaskQueue q;
-  cudaError_t e = prepare_queue(d, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
+  cudaError_t e = prepare_queue(d, d.warp_order, false, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
 #define FS_SOLVE(P_, L_)                                                                      \
   do {                                                                                        \
