@@ -110,6 +110,8 @@ struct DevState {
   float4 *dir_tab;  // close-pair fallback directions for slot differences
   int dir_half;     // table covers d in [-dir_half, dir_half]
   GpuRigidBodyAccum *accum;  // [n_scenes]
+  FsRigidBodyState *rb_state;  // [n_scenes] device-resident coupled bodies
+  uint8_t *rb_coupled;         // [n_scenes] 1 = coupled
   uint32_t *err;
   unsigned long long *stats;
   DevUniforms *u;           // [n_scenes]
@@ -176,6 +178,9 @@ cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st);
 cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last,
                          cudaStream_t st);
+cudaError_t launch_rigid_frame(const DevState &d, uint32_t n_scenes, uint32_t substeps,
+                               cudaStream_t st);
+cudaError_t launch_rigid_sync(const DevState &d, uint32_t n_scenes, cudaStream_t st);
 cudaError_t launch_finalize_integrate(const DevState &d, uint32_t n, int final_buf,
                                       cudaStream_t st);
 

@@ -51,6 +51,8 @@ struct FsSim {
   size_t arena_bytes = 0;
   fs::StepGraph graphs[fs::kGraphSlots];
   uint64_t graph_clock = 0;
+  fs::StepGraph frame_graph;    // one frame of fs_frames (steps + rigid-body integration)
+  std::vector<uint8_t> coupled;  // scenes whose rigid body is device-coupled
   float *splat_buf = nullptr;  // device staging of host-bound density fields
   size_t splat_cap = 0;
   // stage timing
@@ -60,6 +62,11 @@ struct FsSim {
   uint32_t timed_steps = 0;
 
   uint32_t scenes() const { return uint32_t(scene_n.size()); }
+  bool any_coupled() const {
+    for (uint8_t c : coupled)
+      if (c) return true;
+    return false;
+  }
   uint32_t active(uint32_t k) const { return std::min(hu[k].sph.num_particles, scene_n[k]); }
 };
 

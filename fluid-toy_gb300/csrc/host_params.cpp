@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "../../include/fluidsph.h"
+#include "rigid_math.h"
 
 namespace {
 
@@ -201,6 +202,27 @@ int fs_mc_grid_params(const float grid_min[3], const float grid_max[3], uint32_t
   p.num_particles = num_particles;
   p.max_vertices = 4000000u;
   *out = p;
+  return FS_OK;
+}
+
+int fs_rigid_body_to_gpu(const FsRigidBodyState *state, GpuRigidBody *out) {
+  if (!state || !out) return FS_E_INVALID_ARGUMENT;
+  fs::rb::to_gpu(*state, *out);
+  return FS_OK;
+}
+
+int fs_integrate_rigid_body(FsRigidBodyState *state, const GpuContainerGeometry *container,
+                            float substep_dt, uint32_t num_substeps, const float gravity[3],
+                            const GpuRigidBodyAccum *accum) {
+  if (!state || !container || !gravity || !accum) return FS_E_INVALID_ARGUMENT;
+  fs::rb::integrate(*state, *container, substep_dt, num_substeps, gravity, *accum);
+  return FS_OK;
+}
+
+int fs_clamp_rigid_body(FsRigidBodyState *state, const GpuContainerGeometry *container,
+                        int bounce_velocity) {
+  if (!state || !container) return FS_E_INVALID_ARGUMENT;
+  fs::rb::clamp_to_container(*state, *container, bounce_velocity != 0);
   return FS_OK;
 }
 

@@ -61,6 +61,7 @@ static_assert(offsetof(GpuContainerGeometry, wall_stiffness) == 112, "geometry o
 static_assert(offsetof(GpuRigidBody, rot_row0) == 48, "rigid offset");
 static_assert(sizeof(FsSceneInfo) == 80, "FsSceneInfo layout");
 static_assert(sizeof(GpuMcGridParams) == 48, "GpuMcGridParams layout");
+static_assert(sizeof(FsRigidBodyState) == 80, "FsRigidBodyState layout");
 static_assert(FS_BATCH_MAX_SCENES <= 65535u, "scene ids are 16-bit");
 
 }  // namespace
@@ -133,6 +134,8 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.dir_tab = c.take<float4>(2 * size_t(d.dir_half) + 1);
   const size_t S = s->scenes();
   d.accum = c.take<GpuRigidBodyAccum>(S);
+  d.rb_state = c.take<FsRigidBodyState>(S);
+  d.rb_coupled = c.take<uint8_t>(S);
   d.err = c.take<uint32_t>(4);
   d.stats = c.take<unsigned long long>(STAT_COUNT);
   d.u = c.take<DevUniforms>(S);
@@ -179,6 +182,8 @@ int upload_uniforms(FsSim *s) {
           "upload parameters");
   FS_CUDA(cudaMemcpyAsync(s->d.b, &s->hb, sizeof(DevBatch), cudaMemcpyHostToDevice, s->stream),
           "upload batch header");
+  if (s->any_coupled())
+    FS_CUDA(launch_rigid_sync(s->d, s->scenes(), s->stream), "coupled rigid bodies");
   return FS_OK;
 }
 
@@ -191,6 +196,8 @@ int upload_scene(FsSim *s, uint32_t k) {
   FS_CUDA(cudaMemcpyAsync(s->d.u + k, &s->hu[k], sizeof(DevUniforms), cudaMemcpyHostToDevice,
                           s->stream),
           "upload scene parameters");
+  if (s->any_coupled())
+    FS_CUDA(launch_rigid_sync(s->d, s->scenes(), s->stream), "coupled rigid bodies");
   return FS_OK;
 }
 
@@ -420,6 +427,7 @@ int create_sim(const char *who, const SphParticle3D *particles, const uint32_t *
   s->max_n = uint32_t(max_n);
   s->sdf_res = sdf ? sdf_res : 1u;
   s->scene_n.assign(counts, counts + num_scenes);
+  s->coupled.assign(num_scenes, 0);
   s->hu.resize(num_scenes);
   uint64_t cells = 0;
   for (uint32_t k = 0; k < num_scenes; k++) {
@@ -594,6 +602,7 @@ int fs_destroy(FsSim *s) {
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   destroy_graphs(s);
+  if (s->frame_graph.exec) cudaGraphExecDestroy(s->frame_graph.exec);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
   if (s->splat_buf) cudaFree(s->splat_buf);
@@ -780,6 +789,84 @@ int fs_upload_particles(FsSim *s, const SphParticle3D *particles, uint32_t count
   CHECK_SIM(s);
   CHECK_PLAIN(s);
   return fs_batch_upload_scene(s, 0, particles, count);
+}
+
+int fs_rigid_coupling_set_state(FsSim *s, uint32_t scene, const FsRigidBodyState *state) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  const uint8_t flag = state ? 1 : 0;
+  if (state)
+    FS_CUDA(cudaMemcpyAsync(s->d.rb_state + scene, state, sizeof(FsRigidBodyState),
+                            cudaMemcpyHostToDevice, s->stream),
+            "upload rigid-body state");
+  FS_CUDA(cudaMemcpyAsync(s->d.rb_coupled + scene, &flag, 1, cudaMemcpyHostToDevice, s->stream),
+          "rigid-body coupling flag");
+  FS_CUDA(cudaStreamSynchronize(s->stream), "rigid-body coupling");
+  s->coupled[scene] = flag;
+  if (state) FS_CUDA(launch_rigid_sync(s->d, s->scenes(), s->stream), "coupled rigid bodies");
+  return FS_OK;
+}
+
+int fs_rigid_coupling_get_state(FsSim *s, uint32_t scene, FsRigidBodyState *out) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_rigid_coupling_get_state: null out");
+  if (!s->coupled[scene])
+    return fail(FS_E_STATE, "fs_rigid_coupling_get_state: scene %u is not coupled", scene);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  FS_CUDA(cudaMemcpyAsync(out, s->d.rb_state + scene, sizeof(FsRigidBodyState),
+                          cudaMemcpyDeviceToHost, s->stream),
+          "download rigid-body state");
+  return check_device_error(s);
+}
+
+int fs_frames(FsSim *s, uint32_t substeps, uint32_t frames) {
+  CHECK_SIM(s);
+  if (substeps == 0 || substeps > kMaxGraphSteps)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_frames: substeps %u outside [1, %u]", substeps,
+                kMaxGraphSteps);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (frames == 0) return FS_OK;
+  StepGraph &g = s->frame_graph;
+  if (!(g.exec && g.steps == substeps && g.n_canon == s->hb.n_canon &&
+        g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream)) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = StepGraph{};
+    cudaGraph_t graph = nullptr;
+    FS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = cudaMemsetAsync(s->d.accum, 0, sizeof(GpuRigidBodyAccum) * s->scenes(),
+                                    s->stream);
+    rc = e == cudaSuccess ? FS_OK : cuda_fail(e, "clear accumulators");
+    for (uint32_t k = 0; k < substeps && rc == FS_OK; k++) rc = enqueue_step(s, false);
+    if (rc == FS_OK) {
+      e = launch_rigid_frame(s->d, s->scenes(), substeps, s->stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "rigid-body integration");
+    }
+    e = cudaStreamEndCapture(s->stream, &graph);
+    if (rc != FS_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      g.exec = nullptr;
+      return cuda_fail(e, "instantiate frame graph");
+    }
+    g.steps = substeps;
+    g.n_canon = s->hb.n_canon;
+    g.n_sorted = s->hb.n_sorted;
+    g.iters = s->iterations;
+    g.stream = s->stream;
+  }
+  for (uint32_t f = 0; f < frames; f++)
+    FS_CUDA(cudaGraphLaunch(g.exec, s->stream), "launch frame graph");
+  return FS_OK;
 }
 
 int fs_density_splat(FsSim *s, uint32_t scene, const GpuMcGridParams *grid,

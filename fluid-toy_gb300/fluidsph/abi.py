@@ -82,6 +82,14 @@ class GpuRigidBodyAccum(C.Structure):
                 self.torque_x, self.torque_y, self.torque_z)
 
 
+class FsRigidBodyState(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("half_extent", C.c_float),
+                ("velocity", C.c_float * 3), ("density", C.c_float),
+                ("orientation", C.c_float * 4), ("angular_velocity", C.c_float * 3),
+                ("shape", C.c_uint32), ("enabled", C.c_uint32), ("held", C.c_uint32),
+                ("wall_stiffness", C.c_float), ("_pad", C.c_uint32)]
+
+
 class GpuGridParams(C.Structure):
     _fields_ = [("grid_size_x", C.c_uint32), ("grid_size_y", C.c_uint32),
                 ("grid_size_z", C.c_uint32), ("total_cells", C.c_uint32),
@@ -115,7 +123,7 @@ class FsSceneInfo(C.Structure):
 STRUCT_SIZES = {
     GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
     GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48, FsSceneInfo: 80,
-    GpuMcGridParams: 48,
+    GpuMcGridParams: 48, FsRigidBodyState: 80,
 }
 for _t, _n in STRUCT_SIZES.items():
     assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))
@@ -137,6 +145,13 @@ SIGNATURES = {
                                         _P(GpuContainerGeometry)]),
     "fs_quat_to_rotation_rows": (C.c_int, [_P(_f), _P(_f)]),
     "fs_grid_params_for": (C.c_int, [_f, _u32, _P(GpuGridParams)]),
+    "fs_rigid_body_to_gpu": (C.c_int, [_P(FsRigidBodyState), _P(GpuRigidBody)]),
+    "fs_integrate_rigid_body": (C.c_int, [_P(FsRigidBodyState), _P(GpuContainerGeometry), _f,
+                                          _u32, _P(_f), _P(GpuRigidBodyAccum)]),
+    "fs_clamp_rigid_body": (C.c_int, [_P(FsRigidBodyState), _P(GpuContainerGeometry), C.c_int]),
+    "fs_rigid_coupling_set_state": (C.c_int, [_vp, _u32, _P(FsRigidBodyState)]),
+    "fs_rigid_coupling_get_state": (C.c_int, [_vp, _u32, _P(FsRigidBodyState)]),
+    "fs_frames": (C.c_int, [_vp, _u32, _u32]),
     "fs_mc_grid_params": (C.c_int, [_P(_f), _P(_f), _u32, _f, _f, _u32, _P(GpuMcGridParams)]),
     "fs_create": (C.c_int, [_vp, _u32, _P(GpuSphParams3D), _P(GpuContainerGeometry), _u32,
                             _vp, _u32, C.c_int, _u32, _P(_vp)]),

@@ -103,3 +103,39 @@ def mc_grid_params(grid_min, grid_max, grid_size: int, kernel_radius: float,
     check(abi.load().fs_mc_grid_params(lo, hi, int(grid_size), float(kernel_radius),
                                        float(iso_value), int(num_particles), C.byref(out)))
     return out
+
+
+def rigid_body_state(position=(0.0, 0.2, 0.0), half_extent: float = 0.15, shape: int = 0,
+                     density: float = 300.0, velocity=(0.0, 0.0, 0.0),
+                     orientation=(0.0, 0.0, 0.0, 1.0), angular_velocity=(0.0, 0.0, 0.0),
+                     enabled: bool = True, held: bool = False, wall_stiffness: float = 200.0):
+    """FsRigidBodyState (RigidBodyConfig, src/state/rigid_body.rs:86-128)."""
+    from .abi import FsRigidBodyState
+    s = FsRigidBodyState()
+    s.position[:] = list(position)
+    s.half_extent = half_extent
+    s.shape = int(shape)
+    s.density = density
+    s.velocity[:] = list(velocity)
+    s.orientation[:] = list(orientation)
+    s.angular_velocity[:] = list(angular_velocity)
+    s.enabled = 1 if enabled else 0
+    s.held = 1 if held else 0
+    s.wall_stiffness = wall_stiffness
+    return s
+
+
+def rigid_body_to_gpu(state):
+    """RigidBodyConfig::to_gpu_rigid_body (rigid_body.rs:131-146)."""
+    out = GpuRigidBody()
+    check(abi.load().fs_rigid_body_to_gpu(C.byref(state), C.byref(out)))
+    return out
+
+
+def integrate_rigid_body(state, container_geom, substep_dt: float, num_substeps: int, gravity,
+                         accum) -> None:
+    """integrate_rigid_body (rigid_body.rs:277-365), in place on `state`."""
+    g = (C.c_float * 3)(*[float(v) for v in gravity])
+    check(abi.load().fs_integrate_rigid_body(C.byref(state), C.byref(container_geom),
+                                             float(substep_dt), int(num_substeps), g,
+                                             C.byref(accum)))

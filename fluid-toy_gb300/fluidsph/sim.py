@@ -167,6 +167,19 @@ class SphSimulation3DGrid:
                                          C.byref(container_geom), out.ctypes.data, 0))
         return out
 
+    # -- device-resident rigid-body coupling (app.rs:1205-1290 on the GPU) ---------
+    def rigid_coupling_set_state(self, state, scene: int = 0) -> None:
+        check(self._lib.fs_rigid_coupling_set_state(self._h, int(scene),
+                                                    None if state is None else C.byref(state)))
+
+    def rigid_coupling_get_state(self, scene: int = 0):
+        out = abi.FsRigidBodyState()
+        check(self._lib.fs_rigid_coupling_get_state(self._h, int(scene), C.byref(out)))
+        return out
+
+    def frames(self, substeps: int, frames: int = 1) -> None:
+        check(self._lib.fs_frames(self._h, int(substeps), int(frames)))
+
     def device_pointers(self) -> abi.FsDevicePointers:
         p = abi.FsDevicePointers()
         check(self._lib.fs_device_pointers(self._h, C.byref(p)))

@@ -149,6 +149,24 @@ typedef struct GpuRigidBodyAccum {
     uint32_t _pad;
 } GpuRigidBodyAccum;
 
+/* The simulated rigid body of RigidBodyConfig (src/state/rigid_body.rs:86-113)
+ * in the form integrate_rigid_body reads and writes, plus the wall
+ * stiffness its GpuRigidBody carries — 80 bytes. shape: 0 cube, 1 sphere,
+ * 2 cylinder, 3 torus, 4 custom. */
+typedef struct FsRigidBodyState {
+    float position[3];
+    float half_extent;
+    float velocity[3];
+    float density;            /* body density (mass = density * shape volume) */
+    float orientation[4];     /* quaternion x, y, z, w */
+    float angular_velocity[3];
+    uint32_t shape;
+    uint32_t enabled;
+    uint32_t held;            /* user-positioned: clamped, not integrated */
+    float wall_stiffness;     /* GpuRigidBody.stiffness */
+    uint32_t _pad;
+} FsRigidBodyState;
+
 /* GpuGridParams, src/simulation/sph_3d_grid.rs:15-30 — 48 bytes. */
 typedef struct GpuGridParams {
     uint32_t grid_size_x;
@@ -228,6 +246,17 @@ int fs_container_geometry(float width, float depth, float floor_y, float height,
                           GpuContainerGeometry *out);
 /* quat_to_rotation_rows, src/state/rigid_body.rs:188-205 (q = x,y,z,w). */
 int fs_quat_to_rotation_rows(const float q[4], float rows[12]);
+/* RigidBodyConfig::to_gpu_rigid_body, src/state/rigid_body.rs:131-146. */
+int fs_rigid_body_to_gpu(const FsRigidBodyState *state, GpuRigidBody *out);
+/* integrate_rigid_body, src/state/rigid_body.rs:277-365 (reaction forces and
+ * torques of the accumulator -> velocities -> pose, then the container clamp
+ * with bounce): the reference's per-frame CPU step, on the host. */
+int fs_integrate_rigid_body(FsRigidBodyState *state, const GpuContainerGeometry *container,
+                            float substep_dt, uint32_t num_substeps, const float gravity[3],
+                            const GpuRigidBodyAccum *accum);
+/* clamp_rigid_body_to_container, src/state/rigid_body.rs:415-479. */
+int fs_clamp_rigid_body(FsRigidBodyState *state, const GpuContainerGeometry *container,
+                        int bounce_velocity);
 /* Grid sizing of SphSimulation3DGrid::new, sph_3d_grid.rs:121-143. */
 int fs_grid_params_for(float kernel_radius, uint32_t num_particles,
                        GpuGridParams *out);
@@ -287,6 +316,27 @@ int fs_grid_params(const FsSim *sim, GpuGridParams *out);
  * capacity; *spawned receives the count actually added. */
 int fs_spawn_particles(FsSim *sim, const float position[3], uint32_t count,
                        float spread, uint32_t *spawned);
+
+/* ---- device-resident rigid-body coupling ----------------------------------- */
+
+/* The reference's frame (src/app.rs:1205-1290): clear the accumulator, run the
+ * substeps, read the accumulator back (a blocking map) and integrate the body
+ * on the CPU (integrate_rigid_body), then upload its GpuRigidBody for the
+ * next frame. Here the body's state lives on the device and the integration
+ * runs as a kernel after the substeps, with the same arithmetic as
+ * fs_integrate_rigid_body, so frames queue without host synchronisation.
+ * fs_rigid_coupling_set_state couples a scene's body (NULL uncouples; the
+ * scene's GpuRigidBody is then whatever was last written). While coupled,
+ * the state drives the scene's GpuRigidBody (fs_update_rigid_body is
+ * overridden at the next frame). */
+int fs_rigid_coupling_set_state(FsSim *sim, uint32_t scene, const FsRigidBodyState *state);
+/* The coupled body's current state (synchronises). */
+int fs_rigid_coupling_get_state(FsSim *sim, uint32_t scene, FsRigidBodyState *out);
+/* `frames` frames of `substeps` steps each, graph-replayed. Per frame:
+ * clear every scene's accumulator, step, then integrate each coupled body
+ * (enabled and not held) or clamp it to its container (held). The
+ * accumulators of the last frame stay readable. */
+int fs_frames(FsSim *sim, uint32_t substeps, uint32_t frames);
 
 /* ---- read-outs (synchronising) ------------------------------------------- */
 
