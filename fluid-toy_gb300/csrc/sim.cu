@@ -62,6 +62,8 @@ static_assert(offsetof(GpuRigidBody, rot_row0) == 48, "rigid offset");
 static_assert(sizeof(FsSceneInfo) == 80, "FsSceneInfo layout");
 static_assert(sizeof(GpuMcGridParams) == 48, "GpuMcGridParams layout");
 static_assert(sizeof(FsRigidBodyState) == 80, "FsRigidBodyState layout");
+static_assert(sizeof(GpuSprayParams) == 80, "GpuSprayParams layout");
+static_assert(sizeof(GpuSprayParticle) == 48, "GpuSprayParticle layout");
 static_assert(FS_BATCH_MAX_SCENES <= 65535u, "scene ids are 16-bit");
 
 }  // namespace

@@ -106,6 +106,24 @@ class GpuMcGridParams(C.Structure):
                 ("num_particles", C.c_uint32), ("max_vertices", C.c_uint32)]
 
 
+class GpuSprayParams(C.Structure):
+    _fields_ = [("min_speed", C.c_float), ("emission_rate", C.c_float), ("lifetime", C.c_float),
+                ("lifetime_variation", C.c_float), ("drag", C.c_float),
+                ("speed_multiplier", C.c_float), ("velocity_jitter", C.c_float),
+                ("dt", C.c_float), ("max_particles", C.c_uint32),
+                ("num_sph_particles", C.c_uint32), ("frame_count", C.c_uint32),
+                ("gravity_y", C.c_float), ("k_trapped_air", C.c_float),
+                ("k_wave_crest", C.c_float), ("ta_limit", C.c_float),
+                ("bubble_buoyancy", C.c_float), ("bubble_drag", C.c_float),
+                ("wc_limit", C.c_float), ("_pad", C.c_float * 2)]
+
+
+# GpuSprayParticle as numpy rows of 12 float32 (kind is a uint32 bit pattern)
+SPRAY_DTYPE = np.dtype([("pos", "<f4", 3), ("lifetime", "<f4"), ("vel", "<f4", 3),
+                        ("max_lifetime", "<f4"), ("kind", "<u4"), ("age", "<f4"),
+                        ("pad", "<f4", 2)])
+
+
 class FsDevicePointers(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in (
         "pos", "vel", "force", "sorted_pos", "sorted_vel", "sorted_density", "sorted_normal",
@@ -123,7 +141,7 @@ class FsSceneInfo(C.Structure):
 STRUCT_SIZES = {
     GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
     GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48, FsSceneInfo: 80,
-    GpuMcGridParams: 48, FsRigidBodyState: 80,
+    GpuMcGridParams: 48, FsRigidBodyState: 80, GpuSprayParams: 80,
 }
 for _t, _n in STRUCT_SIZES.items():
     assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))
@@ -195,6 +213,14 @@ SIGNATURES = {
     "fs_batch_download_scene_cells": (C.c_int, [_vp, _u32, _vp, _vp, _u32]),
     "fs_batch_download_scene_index_maps": (C.c_int, [_vp, _u32, _vp, _vp, _u32]),
     "fs_batch_upload_scene": (C.c_int, [_vp, _u32, _vp, _u32]),
+    "fs_spray_create": (C.c_int, [_vp, _u32, _u32, _P(_vp)]),
+    "fs_spray_destroy": (C.c_int, [_vp]),
+    "fs_spray_step": (C.c_int, [_vp, _P(GpuSprayParams)]),
+    "fs_spray_reset": (C.c_int, [_vp]),
+    "fs_spray_stats": (C.c_int, [_vp, _P(_u32)]),
+    "fs_spray_limits": (C.c_int, [_vp, _P(_f), _P(_u32)]),
+    "fs_spray_download": (C.c_int, [_vp, _vp, _u32]),
+    "fs_spray_device_buffer": (C.c_int, [_vp, _P(_vp)]),
     "fs_adj_create": (C.c_int, [_vp, _u32, _P(_vp)]),
     "fs_adj_destroy": (C.c_int, [_vp]),
     "fs_adj_forward": (C.c_int, [_vp, _u32]),

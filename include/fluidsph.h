@@ -196,6 +196,41 @@ typedef struct GpuMcGridParams {
     uint32_t max_vertices;
 } GpuMcGridParams;
 
+/* GpuSprayParams, src/state/interaction.rs:129-153 — 80 bytes. */
+typedef struct GpuSprayParams {
+    float min_speed;
+    float emission_rate;
+    float lifetime;
+    float lifetime_variation;
+    float drag;
+    float speed_multiplier;
+    float velocity_jitter;
+    float dt;                 /* frame time: substep dt x substeps */
+    uint32_t max_particles;
+    uint32_t num_sph_particles;
+    uint32_t frame_count;
+    float gravity_y;
+    float k_trapped_air;
+    float k_wave_crest;
+    float ta_limit;           /* potential ceilings: see fs_spray_step */
+    float bubble_buoyancy;
+    float bubble_drag;
+    float wc_limit;
+    float _pad[2];
+} GpuSprayParams;
+
+/* GpuSprayParticle, src/state/interaction.rs:155-174 — 48 bytes. kind: 0
+ * spray, 1 foam, 2 bubble; lifetime <= 0 is a dead slot. */
+typedef struct GpuSprayParticle {
+    float pos[3];
+    float lifetime;
+    float vel[3];
+    float max_lifetime;
+    uint32_t kind;
+    float age;
+    float _pad[2];
+} GpuSprayParticle;
+
 /* Device pointers of a simulation, the analogue of the reference's buffer
  * getters (sph_3d_grid.rs:1500-1530). The library keeps particles as
  * structure-of-arrays float4 records (one coalesced 16-byte load per field),
@@ -337,6 +372,37 @@ int fs_rigid_coupling_get_state(FsSim *sim, uint32_t scene, FsRigidBodyState *ou
  * (enabled and not held) or clamp it to its container (held). The
  * accumulators of the last frame stay readable. */
 int fs_frames(FsSim *sim, uint32_t substeps, uint32_t frames);
+
+/* ---- whitewater (spray, foam, bubbles) ------------------------------------- */
+
+/* SpraySystem, src/simulation/spray.rs (Ihmsen et al. 2012 diffuse particles):
+ * emission from trapped-air and wave-crest potentials over the scene's
+ * grid-sorted particles and cell tables of the last step
+ * (spray_emit.wgsl), then per-class simulation of every slot of the ring
+ * buffer (spray_simulate.wgsl). Two deliberate differences, both
+ * deterministic: a frame's spawns take consecutive ring slots in sorted
+ * particle order (the reference takes them with an atomic counter, so its
+ * order is unspecified; this is its order when invocations run in index
+ * order), and the potential ceilings' running average (spray.rs:40-50) is
+ * updated on the device from each frame's maxima and used from the next
+ * frame on (the reference reads the maxima back asynchronously, at least
+ * one frame late). fs_spray_step ignores params->ta_limit and wc_limit. */
+typedef struct FsSpray FsSpray;
+int fs_spray_create(FsSim *sim, uint32_t scene, uint32_t max_particles, FsSpray **out);
+int fs_spray_destroy(FsSpray *spray);
+/* One frame: emit, simulate, update the ceilings. Asynchronous. */
+int fs_spray_step(FsSpray *spray, const GpuSprayParams *params);
+/* SpraySystem::reset: every slot dead, write head 0, ceilings to their
+ * initial 3.0 / 1.0. */
+int fs_spray_reset(FsSpray *spray);
+/* Live counts after the last frame: total, spray, foam, bubble (synchronises). */
+int fs_spray_stats(FsSpray *spray, uint32_t out[4]);
+/* The current ceilings (trapped air, wave crest) and write head (synchronises). */
+int fs_spray_limits(FsSpray *spray, float limits[2], uint32_t *write_head);
+/* The ring buffer's first `count` records (synchronises), or its device
+ * address (GpuSprayParticle[max_particles]) for a renderer. */
+int fs_spray_download(FsSpray *spray, GpuSprayParticle *out, uint32_t count);
+int fs_spray_device_buffer(FsSpray *spray, void **out);
 
 /* ---- read-outs (synchronising) ------------------------------------------- */
 

@@ -36,6 +36,10 @@ SHADERS = [
     ("sph_integrate", "sph_integrate_3d.wgsl", True),
     # the MC density splat (marching_cubes.rs:663-669 prepends container_common)
     ("mc_density", "mc_density.wgsl", True),
+    # whitewater (spray.rs:52 compiles spray_emit alone; spray_simulate expects
+    # container_common prepended)
+    ("spray_emit", "spray_emit.wgsl", False),
+    ("spray_simulate", "spray_simulate.wgsl", True),
 ]
 
 CXXFLAGS = ["-std=c++20", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fno-strict-aliasing",

@@ -94,6 +94,8 @@ def _bind(lib):
         lib.or_sincos_f32.argtypes = [vp, vp, vp, u32]
         lib.or_set_threads.argtypes = [C.c_int]
         lib.or_density_splat.argtypes = [vp, vp, vp, vp]
+        if hasattr(lib, "or_spray_frame"):
+            lib.or_spray_frame.argtypes = [vp, vp, vp, vp, vp, vp]
         if hasattr(lib, "or_tangent_rollout_loss"):
             lib.or_tangent_rollout_loss.argtypes = [vp, u32, vp, vp, vp, u32, u32, vp, vp,
                                                     C.c_double, C.c_double, vp, vp, C.c_int,
@@ -250,6 +252,16 @@ class OracleSim:
         self._lib.or_density_splat(self._h, C.addressof(mc_params), C.addressof(container_geom),
                                    out.ctypes.data)
         return out
+
+    def spray_frame(self, params, ring: np.ndarray, head: int, limits) -> tuple:
+        """One whitewater frame on `ring` (structured GpuSprayParticle array,
+        modified in place); returns (head, limits, live counts)."""
+        h = C.c_uint32(head)
+        lim = (C.c_float * 2)(*limits)
+        live = (C.c_uint32 * 4)()
+        self._lib.or_spray_frame(self._h, C.addressof(params), ring.ctypes.data, C.byref(h), lim,
+                                 live)
+        return h.value, (lim[0], lim[1]), np.array(live, np.uint32)
 
     def predicted(self, which: int) -> np.ndarray:
         out = np.empty((self._n, 8), np.float32)

@@ -33,6 +33,7 @@ static_assert(offsetof(sph_integrate::MouseForce, direction) == 32, "MouseForce 
 static_assert(offsetof(sph_integrate::RigidBody, rot_row0) == 48, "RigidBody layout");
 
 using Particle = grid_build::SphParticle3D;  // every shader declares the same struct
+
 using Pred = pcisph_predict::PredictedState;
 
 template <class To, class From>
@@ -314,6 +315,58 @@ void or_get_index_maps(void *h, uint32_t *cell_idx, uint32_t *s2o, uint32_t n) {
 void or_get_predicted(void *, int, float *, uint32_t) {}
 void or_get_grid(void *h, void *out) { std::memcpy(out, ((RefSim *)h)->grid, 48); }
 void or_sincos_f32(const float *, float *, float *, uint32_t) {}
+
+// spray.rs:40-50 (f32)
+static float update_auto_limit(float current, float frame_max, float floor_v) {
+  if (frame_max <= 1e-6f) return current;
+  const float alpha = frame_max > current ? 0.05f : 0.01f;
+  return std::max(current + alpha * (frame_max - current), floor_v);
+}
+
+// One whitewater frame with the reference's own shaders (spray.rs:348-385):
+// the emit pass over the sorted particles of the last step (invocations in
+// index order, so the atomic write head hands out slots in that order), the
+// ceiling update from this frame's maxima, then the simulate pass over the
+// ring. params: GpuSprayParams (its ceilings replaced by `limits`); ring:
+// max_particles records of 48 bytes.
+void or_spray_frame(void *hv, const void *params, void *ring, uint32_t *head, float *limits,
+                    uint32_t *live_stats) {
+  auto *h = (RefSim *)hv;
+  static_assert(sizeof(spray_emit::SprayParams) == 80, "SprayParams");
+  static_assert(sizeof(spray_emit::SprayParticle) == 48, "SprayParticle");
+  static_assert(sizeof(spray_emit::SphParticle) == 64, "SphParticle");
+  std::memcpy(&spray_emit::params, params, 80);
+  spray_emit::params.ta_limit = limits[0];
+  spray_emit::params.wc_limit = limits[1];
+  spray_emit::sorted_particles = as<spray_emit::SphParticle>(h->S.data());
+  spray_emit::spray_particles = (spray_emit::SprayParticle *)ring;
+  spray_emit::write_head = *head;
+  std::memcpy(&spray_emit::sph_params, h->sph, 64);
+  spray_emit::cell_starts = h->starts.data();
+  spray_emit::cell_counts = h->counts.data();
+  std::memcpy(&spray_emit::grid, h->grid, 48);
+  spray_emit::emit_stats = {};
+  const u32 n = spray_emit::params.num_sph_particles;
+  spray_emit::dispatch_main((n + 63u) / 64u);
+  *head = spray_emit::write_head;
+  float ta_max, wc_max;
+  std::memcpy(&ta_max, &spray_emit::emit_stats[0], 4);
+  std::memcpy(&wc_max, &spray_emit::emit_stats[1], 4);
+  limits[0] = update_auto_limit(limits[0], ta_max, 0.2f);
+  limits[1] = update_auto_limit(limits[1], wc_max, 0.05f);
+  std::memcpy(&spray_simulate::params, params, 80);
+  std::memcpy(&spray_simulate::container, h->geom, 128);
+  spray_simulate::spray_particles = (spray_simulate::SprayParticle *)ring;
+  spray_simulate::sorted_particles = as<spray_simulate::SphParticle>(h->S.data());
+  spray_simulate::cell_starts = h->starts.data();
+  spray_simulate::cell_counts = h->counts.data();
+  std::memcpy(&spray_simulate::grid, h->grid, 48);
+  std::memcpy(&spray_simulate::sph_params, h->sph, 64);
+  spray_simulate::live_stats = {};
+  const u32 m = spray_simulate::params.max_particles;
+  spray_simulate::dispatch_main((m + 63u) / 64u);
+  for (int k = 0; k < 4; k++) live_stats[k] = spray_simulate::live_stats[k];
+}
 
 // The MC density pass exactly as mc_density.wgsl runs it, on the sorted
 // buffer and cell tables of the last step (bindings of marching_cubes.rs).

@@ -47,6 +47,8 @@ struct vec3 {
   explicit vec3(const vec3<U> &o);
   vec2<T> xz() const { return vec2<T>(x, z); }
   vec2<T> xy() const { return vec2<T>(x, y); }
+  T &operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  const T &operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
 };
 
 template <class T>
@@ -171,6 +173,15 @@ inline f32 abs(f32 x) { return std::fabs(x); }
 inline vec3<f32> abs(vec3<f32> v) { return vec3<f32>(std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)); }
 inline f32 floor(f32 x) { return std::floor(x); }
 inline f32 ceil(f32 x) { return std::ceil(x); }
+inline f32 fract(f32 x) { return x - std::floor(x); }
+inline f32 round(f32 x) { return std::nearbyint(x); }  // WGSL: half to even
+inline vec3<f32> mix(vec3<f32> a, vec3<f32> b, f32 t) { return a * (1.0f - t) + b * t; }
+template <class T> inline T bitcast(f32 v) {
+  static_assert(sizeof(T) == 4, "32-bit bitcast");
+  T out;
+  std::memcpy(&out, &v, 4);
+  return out;
+}
 // pow: WGSL leaves its precision to the implementation. A positive integral
 // exponent up to 64 is evaluated as binary exponentiation in double, rounded
 // once to f32 (the library's own definition, fs_pow_f32); other exponents use
@@ -204,6 +215,11 @@ template <class T, class U> inline T atomicAdd(T *p, U v) {
   return old;
 }
 template <class T, class U> inline void atomicStore(T *p, U v) { *p = T(v); }
+template <class T, class U> inline T atomicMax(T *p, U v) {
+  const T old = *p;
+  if (T(v) > old) *p = T(v);
+  return old;
+}
 
 // fixed-size arrays (workgroup memory)
 template <class T, int N>

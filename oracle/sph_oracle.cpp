@@ -104,6 +104,35 @@ struct McGridF {  // GpuGridParams of the MC renderer, src/render/marching_cubes
 };
 static_assert(sizeof(McGridF) == 48, "mc grid");
 
+struct SprayParamsF {  // GpuSprayParams, src/state/interaction.rs:129-153
+  float min_speed, emission_rate, lifetime, lifetime_variation, drag, speed_multiplier,
+      velocity_jitter, dt;
+  uint32_t max_particles, num_sph_particles, frame_count;
+  float gravity_y, k_trapped_air, k_wave_crest, ta_limit, bubble_buoyancy, bubble_drag, wc_limit,
+      pad0, pad1;
+};
+static_assert(sizeof(SprayParamsF) == 80, "spray params");
+struct SprayPartF {  // GpuSprayParticle, src/state/interaction.rs:155-174
+  float pos[3], lifetime, vel[3], max_lifetime;
+  uint32_t kind;
+  float age, pad1, pad2;
+};
+static_assert(sizeof(SprayPartF) == 48, "spray particle");
+
+// spray_emit.wgsl:140-152
+inline uint32_t spray_hash(uint32_t x) {
+  x = x ^ (x >> 16u);
+  x = x * 0x45d9f3bu;
+  x = x ^ (x >> 16u);
+  x = x * 0x45d9f3bu;
+  x = x ^ (x >> 16u);
+  return x;
+}
+inline float spray_hash_float(uint32_t seed) { return float(spray_hash(seed) & 0xFFFFu) / 65535.0f; }
+inline float remap_clamp(float x, float lo, float hi) {
+  return std::min(std::max((x - lo) / (hi - lo), 0.0f), 1.0f);
+}
+
 // WGSL pow(x, n.0) for an integral n >= 1: binary exponentiation in double,
 // rounded once (the library's definition; WGSL leaves pow's precision open).
 inline double pow_int_d(double x, unsigned n) {
@@ -926,6 +955,184 @@ struct Oracle {
     }
   }
 
+  // spray_emit.wgsl:180-372 over the sorted particles in index order: the
+  // write head hands out ring slots sequentially. stats: per-frame maxima
+  // bits (trapped air, wave crest). ta/wc: this frame's ceilings.
+  void spray_emit(const SprayParamsF &prm, float ta, float wc, SprayPartF *ring, uint32_t *head,
+                  uint32_t stats[2]) const {
+    const float PI_S = 3.14159265359f, TWO_PI_S = 6.28318530718f;
+    const uint32_t n = std::min(prm.num_sph_particles, p.n);
+    const float h = float(p.h), h_sq = float(p.h2);
+    const float mass = float(p.mass);
+    const float poly6_norm = 315.0f / (64.0f * PI_S * float(p.h9));
+    for (uint32_t i = 0; i < n; i++) {
+      const Part<R> &pi = S[i];
+      const V3<float> pos{float(pi.pos.x), float(pi.pos.y), float(pi.pos.z)};
+      const V3<float> vel{float(pi.vel.x), float(pi.vel.y), float(pi.vel.z)};
+      const float speed = len3(vel);
+      if (speed < prm.min_speed) continue;
+      const V3<float> normal_i{float(pi.normal.x), float(pi.normal.y), float(pi.normal.z)};
+      const float n_len_i = len3(normal_i);
+      const bool crest_eligible = n_len_i > 1e-4f && float(pi.density) < float(p.rho0) * 0.9f;
+      V3<float> n_hat_i{0.0f, 1.0f, 0.0f};
+      if (crest_eligible) n_hat_i = normal_i / n_len_i;
+      float trapped_air = 0.0f, crest = 0.0f, divergence = 0.0f;
+      uint32_t n_neighbors = 0u;
+      for_neighbors(pi.pos, [&](uint32_t j) {
+        const Part<R> &pj = S[j];
+        const V3<float> pjp{float(pj.pos.x), float(pj.pos.y), float(pj.pos.z)};
+        const V3<float> r_vec = pos - pjp;
+        const float r_sq = dot3(r_vec, r_vec);
+        if (r_sq >= h_sq || r_sq < 1e-12f) return;
+        const float r = std::sqrt(r_sq);
+        const float w = 1.0f - r / h;
+        const V3<float> x_hat = r_vec / r;
+        n_neighbors += 1u;
+        const float d2 = h_sq - r_sq;
+        const float w_vol = (mass / std::max(float(pj.density), 1e-6f)) * poly6_norm * d2 * d2 * d2;
+        const V3<float> v_ij = vel - V3<float>{float(pj.vel.x), float(pj.vel.y), float(pj.vel.z)};
+        const float v_ij_len = len3(v_ij);
+        if (v_ij_len > 1e-6f) trapped_air += v_ij_len * (1.0f - dot3(v_ij / v_ij_len, x_hat)) * w_vol;
+        divergence += dot3(v_ij, x_hat) * w;
+        if (crest_eligible && dot3(-x_hat, n_hat_i) < 0.0f) {
+          const V3<float> normal_j{float(pj.normal.x), float(pj.normal.y), float(pj.normal.z)};
+          const float n_len_j = len3(normal_j);
+          if (n_len_j > 1e-4f) crest += (1.0f - dot3(n_hat_i, normal_j / n_len_j)) * w_vol;
+        }
+      });
+      if (n_neighbors < 10u) continue;
+      if (dot3(vel / speed, n_hat_i) < 0.6f) crest = 0.0f;
+      uint32_t bits;
+      if (trapped_air > 0.0f) {
+        std::memcpy(&bits, &trapped_air, 4);
+        stats[0] = std::max(stats[0], bits);
+      }
+      if (crest > 0.0f) {
+        std::memcpy(&bits, &crest, 4);
+        stats[1] = std::max(stats[1], bits);
+      }
+      const float phi_div = remap_clamp(divergence, 0.0f, 0.5f);
+      const float ta_hi = std::max(ta, 1e-4f), wc_hi = std::max(wc, 1e-4f);
+      const float phi_ta = remap_clamp(trapped_air, 0.1f * ta_hi, ta_hi);
+      const float phi_wc = remap_clamp(crest, 0.1f * wc_hi, wc_hi) * phi_div;
+      const float phi_k = remap_clamp(speed, prm.min_speed, 2.5f);
+      const float rate = phi_k * (prm.k_trapped_air * phi_ta + prm.k_wave_crest * phi_wc) * prm.emission_rate;
+      const float expected = rate * prm.dt;
+      const uint32_t base_seed = i + prm.frame_count * 7919u;
+      uint32_t n_emit = uint32_t(std::floor(expected));
+      if (spray_hash_float(base_seed * 13u + 5u) < expected - std::floor(expected)) n_emit = n_emit + 1u;
+      n_emit = std::min(n_emit, 16u);
+      if (n_emit == 0u) continue;
+      const V3<float> v_dir = vel / speed;
+      V3<float> ref_axis{0.0f, 1.0f, 0.0f};
+      if (std::fabs(v_dir.y) > 0.99f) ref_axis = V3<float>{1.0f, 0.0f, 0.0f};
+      const V3<float> e1 = normalize3(cross3(v_dir, ref_axis));
+      const V3<float> e2 = cross3(v_dir, e1);
+      for (uint32_t e = 0u; e < n_emit; e = e + 1u) {
+        const uint32_t slot = ((*head)++) % prm.max_particles;
+        const uint32_t seed = base_seed + e * 3571u;
+        const float r0 = spray_hash_float(seed), r1 = spray_hash_float(seed + 1u);
+        const float r2 = spray_hash_float(seed + 2u), r3 = spray_hash_float(seed + 3u);
+        const float r4 = spray_hash_float(seed + 4u) * 2.0f - 1.0f;
+        const float r5 = spray_hash_float(seed + 5u) * 2.0f - 1.0f;
+        const float r6 = spray_hash_float(seed + 6u) * 2.0f - 1.0f;
+        const float disc_r = h * 0.5f * std::sqrt(r0);
+        const float theta = TWO_PI_S * r1;
+        const float along = r2 * prm.dt * speed;
+        const V3<float> sp = pos + e1 * (disc_r * cos_f32(theta)) +
+                             e2 * (disc_r * sin_f32(theta)) + v_dir * along;
+        const V3<float> jitter = V3<float>{r4, r5, r6} * prm.velocity_jitter;
+        const V3<float> spawn_vel = vel * prm.speed_multiplier + jitter;
+        const float lt_min = prm.lifetime * (1.0f - prm.lifetime_variation);
+        const float lt_span = 2.0f * prm.lifetime * prm.lifetime_variation;
+        const float lt = lt_min + phi_k * r3 * lt_span;
+        SprayPartF q{{sp.x, sp.y, sp.z}, lt, {spawn_vel.x, spawn_vel.y, spawn_vel.z}, lt, 0u, 0.0f,
+                     0.0f, 0.0f};
+        ring[slot] = q;
+      }
+    }
+  }
+
+  // spray_simulate.wgsl:158-280 over every ring slot.
+  void spray_simulate(const SprayParamsF &prm, SprayPartF *ring, uint32_t live[4]) const {
+    const float h = float(p.h), h_sq = float(p.h2), dt = prm.dt;
+    auto cap = [](float t) {
+      const float tc = std::min(std::max(t, 0.0f), 1.0f);
+      return tc * tc * (3.0f - tc) * 0.25f;
+    };
+    for (uint32_t idx = 0; idx < prm.max_particles; idx++) {
+      SprayPartF q = ring[idx];
+      if (q.lifetime <= 0.0f) continue;
+      const V3<float> pos{q.pos[0], q.pos[1], q.pos[2]};
+      V3<float> vel{q.vel[0], q.vel[1], q.vel[2]};
+      uint32_t neighbor_count = 0u;
+      float w_sum = 0.0f;
+      V3<float> v_avg{0.0f, 0.0f, 0.0f};
+      for_neighbors(V3<R>{R(pos.x), R(pos.y), R(pos.z)}, [&](uint32_t j) {
+        const Part<R> &pj = S[j];
+        const V3<float> r_vec = pos - V3<float>{float(pj.pos.x), float(pj.pos.y), float(pj.pos.z)};
+        const float r_sq = dot3(r_vec, r_vec);
+        if (r_sq < h_sq) {
+          const float w = 1.0f - std::sqrt(r_sq) / h;
+          neighbor_count = neighbor_count + 1u;
+          w_sum = w_sum + w;
+          v_avg = v_avg + V3<float>{float(pj.vel.x), float(pj.vel.y), float(pj.vel.z)} * w;
+        }
+      });
+      if (w_sum > 1e-6f) v_avg = v_avg / w_sum;
+      uint32_t kind = 1u;
+      if (neighbor_count <= 6u) kind = 0u;
+      else if (neighbor_count >= 20u) kind = 2u;
+      const float hw = float(geom.hw), hh = float(geom.hh), hd = float(geom.hd);
+      auto to_local = [&](V3<float> w) {
+        const V3<float> c{w.x, w.y - float(geom.cy), w.z};
+        const V3<float> i0{float(geom.i0.x), float(geom.i0.y), float(geom.i0.z)};
+        const V3<float> i1{float(geom.i1.x), float(geom.i1.y), float(geom.i1.z)};
+        const V3<float> i2{float(geom.i2.x), float(geom.i2.y), float(geom.i2.z)};
+        return V3<float>{dot3(i0, c), dot3(i1, c), dot3(i2, c)};
+      };
+      if (kind == 1u) {
+        const V3<float> lp = to_local(pos);
+        const float he[3] = {hw, hh, hd}, la[3] = {lp.x, lp.y, lp.z};
+        float missing = 0.0f;
+        for (int a = 0; a < 3; a++) {
+          const float dlo = he[a] + la[a], dhi = he[a] - la[a];
+          if (dlo < h) missing += cap(1.0f - dlo / h);
+          if (dhi < h) missing += cap(1.0f - dhi / h);
+        }
+        const float visible = std::max(1.0f - missing, 0.25f);
+        if (uint32_t(std::nearbyint(float(neighbor_count) / visible)) >= 20u) kind = 2u;
+      }
+      if (kind == 1u && q.age < 0.15f) kind = 0u;
+      const V3<float> gravity{0.0f, prm.gravity_y, 0.0f};
+      float decay = 0.0f;
+      if (kind == 0u) {
+        vel = vel + dt * (gravity - prm.drag * vel);
+      } else if (kind == 1u) {
+        vel = v_avg;
+        decay = 1.0f;
+      } else {
+        vel = vel + dt * (-prm.bubble_buoyancy * gravity);
+        const float t = std::min(std::max(prm.bubble_drag, 0.0f), 1.0f);
+        vel = vel * (1.0f - t) + v_avg * t;
+      }
+      const V3<float> np = pos + dt * vel;
+      q.pos[0] = np.x; q.pos[1] = np.y; q.pos[2] = np.z;
+      q.vel[0] = vel.x; q.vel[1] = vel.y; q.vel[2] = vel.z;
+      q.kind = kind;
+      q.age = q.age + dt;
+      q.lifetime = q.lifetime - dt * decay;
+      const V3<float> l = to_local(np);
+      if (!(l.x >= -hw && l.x <= hw && l.y >= -hh && l.y <= hh && l.z >= -hd && l.z <= hd))
+        q.lifetime = 0.0f;
+      if (q.lifetime > 0.0f) {
+        live[0] += 1u;
+        live[1 + kind] += 1u;
+      }
+      ring[idx] = q;
+    }
+  }
+
   void density_splat(const McGridF &mc, const GeomF &cgf, double *out) const {
     splat_into<double>(mc, cgf, out);
   }
@@ -1232,6 +1439,27 @@ void or_tangent_rollout_loss(const void *particles, uint32_t n, const void *para
     tangent_loss_impl<float>((const ParticleF *)particles, n, (const SphParamsF *)params,
                              (const GeomF *)geom, gravity, iterations, steps, dpos, dvel, dvisc,
                              dst, (const McGridF *)mc, target, loss, dloss);
+}
+
+// One whitewater frame (FP32 restatement): emit, ceiling update, simulate.
+void or_spray_frame(void *hv, const void *params, void *ring, uint32_t *head, float *limits,
+                    uint32_t *live_stats) {
+  auto *h = (Handle *)hv;
+  if (!h->f) return;  // FP32 only
+  const SprayParamsF &prm = *(const SprayParamsF *)params;
+  uint32_t stats[2] = {0u, 0u};
+  h->f->spray_emit(prm, limits[0], limits[1], (SprayPartF *)ring, head, stats);
+  auto update = [](float current, uint32_t bits, float floor_v) {
+    float frame_max;
+    std::memcpy(&frame_max, &bits, 4);
+    if (frame_max <= 1e-6f) return current;
+    const float alpha = frame_max > current ? 0.05f : 0.01f;
+    return std::max(current + alpha * (frame_max - current), floor_v);
+  };
+  limits[0] = update(limits[0], stats[0], 0.2f);
+  limits[1] = update(limits[1], stats[1], 0.05f);
+  for (int k = 0; k < 4; k++) live_stats[k] = 0u;
+  h->f->spray_simulate(prm, (SprayPartF *)ring, live_stats);
 }
 
 // The MC density field of the last step's sorted positions (gs^3 doubles).

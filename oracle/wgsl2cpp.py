@@ -23,7 +23,7 @@ TOKEN_RE = re.compile(r"""
     (?P<ws>\s+)
   | (?P<comment>//[^\n]*|/\*.*?\*/)
   | (?P<attr>@[A-Za-z_]\w*)
-  | (?P<num>(?:\d+\.\d*|\.\d+|\d+)(?:[eE][+-]?\d+)?[fiu]?)
+  | (?P<num>0[xX][0-9a-fA-F]+[iu]?|(?:\d+\.\d*|\.\d+|\d+)(?:[eE][+-]?\d+)?[fiu]?)
   | (?P<id>[A-Za-z_]\w*)
   | (?P<op>->|\+\+|--|&&|\|\||<=|>=|==|!=|<<|>>|[-+*/%&|^!~<>=]=?|[(){}\[\];:,.?])
 """, re.X | re.S)
@@ -55,6 +55,8 @@ CONVERSIONS = {"i32", "u32", "f32"}
 
 
 def fix_number(t: str) -> str:
+    if t[:2] in ("0x", "0X"):
+        return t[:-1] if t.endswith("i") else t
     if t.endswith("i"):
         return t[:-1]
     if t.endswith("u"):
@@ -366,6 +368,8 @@ class Translator:
                 args = self.read_balanced("(", ")") if self.peek() and self.peek().text == "(" else []
                 attrs.append((a, [x.text for x in args]))
             kw = self.next().text
+            if kw == ";":  # WGSL allows `struct S { ... };`
+                continue
             if kw == "struct":
                 self.top_struct()
             elif kw == "var":
@@ -423,7 +427,10 @@ class Translator:
                 typ_toks.append(tt)
                 j += 1
             typ = self.type_text("".join(typ_toks).replace(">>", ">>"))
-            fields.append(f"  {typ} {fname};")
+            # WGSL host-shareable layout: vec3/vec4 align to 16 bytes, vec2 to 8
+            align = "alignas(16) " if typ.startswith(("vec3<", "vec4<")) else (
+                "alignas(8) " if typ.startswith("vec2<") else "")
+            fields.append(f"  {align}{typ} {fname};")
             k = j + 1
         self.structs.append(f"struct {name} {{\n" + "\n".join(fields) + "\n};")
 

@@ -76,3 +76,31 @@ def test_mc_grid_params_matches_update_params():
     assert g.cell_size == f32(ext) / f32(100)
     assert (g.grid_size, g.num_particles, g.max_vertices) == (100, 77, 4_000_000)
     assert g.kernel_radius == f32(0.12) and g.iso_value == 300.0
+
+
+def test_spray_frames_equal_reference_translation(oracle_mod, ref_lib):
+    """Whitewater frames (emit, ceiling update, simulate) of the restatement
+    against the reference's own spray shaders, ring state carried over."""
+    from fluidsph import scenes
+    from fluidsph.abi import SPRAY_DTYPE
+    from fluidsph.spray import spray_params
+    sc = scenes.small_scene(nx=12, ny=10, nz=9, seed=61)
+    a = oracle_mod.oracle_for_scene(sc)
+    b = oracle_mod.oracle_for_scene(sc, lib=ref_lib)
+    rings = [np.zeros(4096, SPRAY_DTYPE), np.zeros(4096, SPRAY_DTYPE)]
+    state = [(0, (3.0, 1.0)), (0, (3.0, 1.0))]
+    emitted = 0
+    for frame in range(6):
+        prm = spray_params(sc.n, sc.sph.dt * 3, frame_count=frame, max_particles=4096)
+        out = []
+        for k, o in enumerate((a, b)):
+            o.step(3)
+            head, lim = state[k]
+            head, lim, live = o.spray_frame(prm, rings[k], head, lim)
+            state[k] = (head, lim)
+            out.append(live)
+        np.testing.assert_array_equal(rings[0].view(np.uint32), rings[1].view(np.uint32))
+        assert state[0] == state[1]
+        np.testing.assert_array_equal(out[0], out[1])
+        emitted = state[0][0]
+    assert emitted > 0, "no spray emitted"
