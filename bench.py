@@ -557,6 +557,128 @@ def run_adjoint(args, dist: Dist) -> dict | None:
     }
 
 
+def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False):
+    """Batched gradient descent on per-scene viscosity and surface tension
+    (and stiffness, whose gradient is 0) against hidden-parameter targets.
+    Steps are sign steps scaled by a decaying rate relative to each
+    parameter's range, robust to the gradients' magnitude. Returns the
+    parameter errors, the losses and (timed) fwd+adjoint ms/step."""
+    import torch
+    from fluidsph import scenes as S
+    from fluidsph.adjoint import DifferentiableRollout
+    from fluidsph.sim import SphBatch3DGrid
+
+    def batch(params):
+        b = SphBatch3DGrid([s.particles for s in scenes], params, [s.geom for s in scenes],
+                           device=dev)
+        for k, s in enumerate(scenes):
+            b.update_scene(k, gravity=s.gravity)
+        b.set_pcisph_iterations(scenes[0].iterations)
+        return b
+
+    def with_(p, **kw):
+        q = type(p).from_buffer_copy(p)
+        for k, v in kw.items():
+            setattr(q, k, v)
+        return q
+
+    grids = [S.loss_grid(s, grid_size) for s in scenes]
+    hb = batch([with_(s.sph, **h) for s, h in zip(scenes, hidden)])
+    hr = DifferentiableRollout(hb, every)
+    hr.forward(steps)
+    targets = [hr.final_splat(grids[k], scenes[k].geom, scene=k) for k in range(len(scenes))]
+    hr.close()
+    hb.close()
+    params = [with_(s.sph) for s in scenes]
+    b = batch(params)
+    r = DifferentiableRollout(b, every)
+    names = ("viscosity", "stiffness", "surface_tension")
+    init = np.array([[getattr(p, n) for n in names] for p in params], np.float64)
+    cur = init.copy()
+    truth = np.array([[h[n] for n in names] for h in hidden], np.float64)
+    span = np.maximum(np.abs(truth - init).max(axis=0), 1e-3)
+    losses, ms = [], []
+    for it in range(iters):
+        for k, p in enumerate(params):
+            p.viscosity, p.stiffness, p.surface_tension = (float(v) for v in cur[k])
+            b.update_scene(k, sph_params=p)
+        for k, s in enumerate(scenes):
+            b.upload_scene_particles(k, s.particles)
+        b.sync()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r.forward(steps)
+        loss = sum(r.splat_mse_loss(grids[k], scenes[k].geom, targets[k], scene=k)
+                   for k in range(len(scenes)))
+        _, _, g = r.backward(scenes=len(scenes))
+        torch.cuda.synchronize(dev)
+        ms.append((time.perf_counter() - t0) * 1e3 / steps)
+        losses.append(loss)
+        rate = 0.25 * (0.9 ** it)
+        step = np.where(np.isfinite(g) & (g != 0), -np.sign(np.nan_to_num(g)), 0.0) * rate * span
+        cur = cur + step
+    r.close()
+    b.close()
+    err = np.abs(cur - truth) / np.abs(truth)
+    err0 = np.abs(init - truth) / np.abs(truth)
+    return {"relative_error_initial": {n: float(np.mean(err0[:, i])) for i, n in enumerate(names)},
+            "relative_error_final": {n: float(np.mean(err[:, i])) for i, n in enumerate(names)},
+            "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None,
+            "gradient_finite": bool(np.isfinite(g).all()) if iters else None,
+            "fwd_adjoint_ms_per_step": float(np.median(ms)) if ms else None}
+
+
+def run_identify(args, dist: Dist) -> dict | None:
+    """Batched adjoint parameter identification (64 scenes, counts in [8192,
+    32768], 150 steps, checkpoint every 15): fused batched forward + reverse
+    ms/step and the parameter errors after `--gd-iters` iterations; plus the
+    same procedure on 64 small rollouts with the reference app's default
+    physics, where the loss is smooth and the identification converges."""
+    import torch
+    from fluidsph import scenes as S
+    from fluidsph.sim import SphBatch3DGrid
+
+    dev = dist.local_rank
+    torch.cuda.set_device(dev)
+    scs, hidden = S.config4()
+    total = sum(s.n for s in scs)
+    # forward-only ms/step of the same batch (graph-replayed)
+    b = SphBatch3DGrid([s.particles for s in scs], [s.sph for s in scs], [s.geom for s in scs],
+                       device=dev)
+    for k, s in enumerate(scs):
+        b.update_scene(k, gravity=s.gravity)
+    b.set_pcisph_iterations(scs[0].iterations)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.Stream(device=dev)  # events and steps on one stream
+    b.set_stream(stream.cuda_stream)
+    b.prepare_steps(150)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    b.step(150)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    fwd_ms = e0.elapsed_time(e1) / 150
+    b.close()
+    spec = _identify(scs, hidden, 150, 15, args.gd_iters, 64, dev)
+    well = _identify(*S.reference_physics_batch(64, 20), 20, 5, 50, 32, dev)
+    if dist.rank != 0:
+        return None
+    v = spec["fwd_adjoint_ms_per_step"]
+    return {
+        "metric": "batched fwd+adjoint ms/step", "value": round(v, 4), "unit": "ms/step",
+        "n_gpus": dist.world, "steps": 150, "warmup": 0, "ms_per_step": round(v, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene draws, lattice jitter, hidden parameters)",
+        "config": {"workload": "batched_identification_64_scenes", "scenes": len(scs),
+                   "particles": total, "steps": 150, "checkpoint_every": 15,
+                   "gd_iterations": args.gd_iters},
+        "forward_ms_per_step": round(fwd_ms, 4),
+        "fwd_adjoint_over_forward": round(v / fwd_ms, 3),
+        "identification": spec,
+        "identification_reference_physics": well,
+    }
+
+
 def run_reference(args, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
@@ -597,6 +719,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched and differentiable forms in the default run")
+    ap.add_argument("--gd-iters", type=int, default=3,
+                    help="gradient-descent iterations of the --config 4 workload")
     ap.add_argument("--loop-steps", type=int, default=20,
                     help="steps per scene of the looped-plain comparison (--config 2)")
     args = ap.parse_args()
@@ -616,6 +740,8 @@ def main():
                 out = run_batch(args, dist)
             elif args.config == 3:
                 out = run_adjoint(args, dist)
+            elif args.config == 4:
+                out = run_identify(args, dist)
             else:
                 out = run_ours(args, dist)
         if out is not None:

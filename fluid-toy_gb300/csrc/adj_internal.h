@@ -42,8 +42,9 @@ cudaError_t launch_adj_step(const SceneView &v, const TapeView &t, const AdjView
                             const float4 *xbar_in, const float4 *vbar_in, float4 *xbar_out,
                             float4 *vbar_out, const float4 *dir_tab, int dir_half, uint32_t n,
                             int K, int lanes, int sm_count, cudaStream_t st);
+// partial: one double per 256 voxels
 cudaError_t launch_splat_mse(const SplatArgs &sa, const float *field, const float *target,
-                             float *gg, double *loss, cudaStream_t st);
+                             float *gg, double *partial, double *loss, cudaStream_t st);
 cudaError_t launch_reduce_params(const double2 *gpart, const uint32_t *scene_first,
                                  const uint32_t *scene_count, uint32_t scenes, double *gparam,
                                  cudaStream_t st);

@@ -652,10 +652,11 @@ __global__ void __launch_bounds__(256)
 
 // ---- the density-splat MSE loss ---------------------------------------------------------------
 // L = (1/V) sum_v (rho_v - target_v)^2 over the V voxels; gg_v = dL/drho_v /
-// gamma_v (0 for clipped voxels), loss partial sums in FP64.
+// gamma_v (0 for clipped voxels). The loss sums in FP64 in a fixed order:
+// a shared-memory tree per block, then k_sum_partials over the blocks.
 __global__ void __launch_bounds__(256)
     k_splat_mse(SplatArgs sa, const float *__restrict__ field, const float *__restrict__ target,
-                float *__restrict__ gg, double *__restrict__ loss) {
+                float *__restrict__ gg, double *__restrict__ partial) {
   const uint32_t gs = sa.mc.grid_size;
   const uint32_t nvox = gs * gs * gs;
   const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -683,10 +684,29 @@ __global__ void __launch_bounds__(256)
     gamma = fmaxf(gamma, 0.15f);
     gg[vx] = clipped ? 0.0f : (2.0f * d / float(nvox)) / gamma;
   }
-  l /= double(nvox);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-  if ((threadIdx.x & 31u) == 0u && l != 0.0) atomicAdd(loss, l);
+  __shared__ double part[256];
+  part[threadIdx.x] = l / double(nvox);
+  __syncthreads();
+  for (unsigned o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = part[0];
+}
+
+// out = sum of n partials, fixed order (one block).
+__global__ void __launch_bounds__(1024)
+    k_sum_partials(const double *__restrict__ partial, uint32_t n, double *__restrict__ out) {
+  __shared__ double part[1024];
+  double acc = 0.0;
+  for (uint32_t i = threadIdx.x; i < n; i += 1024u) acc += partial[i];
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (unsigned o = 512; o > 0; o >>= 1) {
+    if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = part[0];
 }
 
 // dL/dx_j = sum_v gg_v * 6 coeff (h^2 - r^2)^2 (w_v - x_j), over the voxels
@@ -853,11 +873,13 @@ cudaError_t launch_adj_step(const SceneView &v, const TapeView &t, const AdjView
 }
 
 cudaError_t launch_splat_mse(const SplatArgs &sa, const float *field, const float *target,
-                             float *gg, double *loss, cudaStream_t st) {
+                             float *gg, double *partial, double *loss, cudaStream_t st) {
   const uint32_t gs = sa.mc.grid_size;
   const uint32_t nvox = gs * gs * gs;
   if (nvox == 0) return cudaSuccess;
-  k_splat_mse<<<blocks_for(nvox, 256), 256, 0, st>>>(sa, field, target, gg, loss);
+  const unsigned blocks = blocks_for(nvox, 256);
+  k_splat_mse<<<blocks, 256, 0, st>>>(sa, field, target, gg, partial);
+  k_sum_partials<<<1, 1024, 0, st>>>(partial, blocks, loss);
   return cudaGetLastError();
 }
 

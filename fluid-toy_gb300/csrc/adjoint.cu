@@ -73,7 +73,7 @@ struct FsAdj {
   bool seeded = false;
   // loss scratch
   float *field = nullptr, *target = nullptr, *gg = nullptr;
-  double *loss = nullptr;
+  double *loss = nullptr, *partial = nullptr;
   size_t vox_cap = 0;
   int lanes = 0;  // lanes per particle of the reverse gathers (autotuned)
   uint32_t *scene_first = nullptr, *scene_count = nullptr;  // device, canonical ranges
@@ -388,6 +388,41 @@ int fs_adj_set_cotangents(FsAdj *a, const float *dl_dpos, const float *dl_dvel, 
   return FS_OK;
 }
 
+int fs_adj_final_splat(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
+                       const GpuContainerGeometry *geom, float *out, int out_on_device) {
+  CHECK_ADJ(a);
+  FsSim *s = a->sim;
+  if (!grid || !geom || !out) return fail(FS_E_INVALID_ARGUMENT, "fs_adj_final_splat: null argument");
+  if (scene >= s->scenes())
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_final_splat: scene %u of %u", scene, s->scenes());
+  if (grid->grid_size == 0 || grid->grid_size > 1024)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_final_splat: grid_size %u outside [1, 1024]",
+                grid->grid_size);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  const DevUniforms &u = s->hu[scene];
+  const SplatArgs sa = make_splat_args(*grid, *geom, u.grid);
+  if (sa.cell_radius < 1 || sa.cell_radius > 8)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_final_splat: splat radius spans %d cells",
+                sa.cell_radius);
+  if ((rc = enqueue_grid_build(s))) return rc;
+  const size_t vox = size_t(grid->grid_size) * grid->grid_size * grid->grid_size;
+  if (out_on_device) {
+    FS_CUDA(launch_density_splat(sa, s->d.s_pos, s->d.cell_begin + u.c_offset, out, s->stream),
+            "final splat");
+    return FS_OK;
+  }
+  float *tmp = nullptr;
+  FS_CUDA(cudaMallocAsync(reinterpret_cast<void **>(&tmp), sizeof(float) * vox, s->stream),
+          "final splat scratch");
+  cudaError_t e = launch_density_splat(sa, s->d.s_pos, s->d.cell_begin + u.c_offset, tmp, s->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, tmp, sizeof(float) * vox, cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(tmp, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "final splat");
+  return check_device_error(s);
+}
+
 int fs_adj_splat_mse_loss(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
                           const GpuContainerGeometry *geom, const float *target,
                           int target_on_device, double *loss_out) {
@@ -409,13 +444,14 @@ int fs_adj_splat_mse_loss(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
     FS_CUDA(cudaStreamSynchronize(s->stream), "loss scratch");
     if (a->field) cudaFree(a->field);
     a->field = nullptr;
-    const size_t bytes = a256(sizeof(float) * vox) * 3 + 256;
+    const size_t bytes = a256(sizeof(float) * vox) * 3 + 256 + a256(sizeof(double) * (vox / 256 + 1));
     char *p = nullptr;
     FS_CUDA(cudaMalloc(&p, bytes), "allocate loss scratch");
     a->field = reinterpret_cast<float *>(p);
     a->target = reinterpret_cast<float *>(p + a256(sizeof(float) * vox));
     a->gg = reinterpret_cast<float *>(p + 2 * a256(sizeof(float) * vox));
     a->loss = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox));
+    a->partial = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox) + 256);
     a->vox_cap = vox;
   }
   const DevUniforms &u = s->hu[scene];
@@ -432,8 +468,8 @@ int fs_adj_splat_mse_loss(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
                           target_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                           s->stream),
           "upload target");
-  FS_CUDA(cudaMemsetAsync(a->loss, 0, sizeof(double), s->stream), "clear loss");
-  FS_CUDA(launch_splat_mse(sa, a->field, a->target, a->gg, a->loss, s->stream), "loss");
+  FS_CUDA(launch_splat_mse(sa, a->field, a->target, a->gg, a->partial, a->loss, s->stream),
+          "loss");
   FS_CUDA(launch_splat_adjoint(sa, s->scene_n[scene], s->d.p_pos + u.p_offset, a->gg,
                                a->cot[a->cur][0] + u.p_offset, s->stream),
           "loss adjoint");

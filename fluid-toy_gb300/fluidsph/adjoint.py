@@ -27,6 +27,7 @@ class DifferentiableRollout:
         h = C.c_void_p()
         check(self._lib.fs_adj_create(sim._h, int(checkpoint_every), C.byref(h)))
         self._h = h
+        sim._register(self)
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -73,6 +74,14 @@ class DifferentiableRollout:
                                                   C.byref(container_geom), t.ctypes.data, 0,
                                                   C.byref(loss)))
         return loss.value
+
+    def final_splat(self, mc_params, container_geom, scene: int = 0) -> np.ndarray:
+        """Density splat of the recorded rollout's final positions, (gs, gs, gs)."""
+        gs = int(mc_params.grid_size)
+        out = np.empty((gs, gs, gs), np.float32)
+        check(self._lib.fs_adj_final_splat(self._h, int(scene), C.byref(mc_params),
+                                           C.byref(container_geom), out.ctypes.data, 0))
+        return out
 
     def backward(self, scenes: int = 1):
         n = self.sim.num_particles()

@@ -196,6 +196,37 @@ def reference_physics_rollout(nx: int = 16, ny: int = 8, nz: int = 16, steps: in
                  None, 4, steps, box)
 
 
+def config4(seed: int = 0, num_scenes: int = 64, lo: int = 8192, hi: int = 32768,
+            steps: int = 150) -> tuple[list, list]:
+    """Batched parameter identification: `num_scenes` scenes set up as the
+    batched ensemble (batch_scene) with counts log-uniform in [lo, hi], and per
+    scene a hidden target: viscosity U[5, 25] and stiffness U[20, 50] (the
+    surface tension keeps the scene's own value). Returns (scenes, hidden)."""
+    scs = [batch_scene(k, seed + 4_000, lo, hi, steps) for k in range(num_scenes)]
+    hidden = []
+    for k in range(num_scenes):
+        u = uniform01(seed * 1_000_003 + 104_729 * (k + 1), 2)
+        hidden.append({"viscosity": float(5.0 + 20.0 * u[0]), "stiffness": float(20.0 + 30.0 * u[1]),
+                       "surface_tension": float(scs[k].sph.surface_tension)})
+    return scs, hidden
+
+
+def reference_physics_batch(num_scenes: int = 64, steps: int = 20, seed: int = 0) -> tuple:
+    """Well-posed identification companion of config4: small rollouts with the
+    reference app's default physics (reference_physics_rollout), lattices of
+    8-12 x 6-8 x 8-12, each with a hidden viscosity U[0.35, 1.4] (the default
+    is 0.7). Returns (scenes, hidden)."""
+    scs, hidden = [], []
+    for k in range(num_scenes):
+        u = uniform01(seed * 1_000_003 + 31 * (k + 1), 4)
+        nx, ny, nz = 8 + int(5 * u[0]), 6 + int(3 * u[1]), 8 + int(5 * u[2])
+        sc = reference_physics_rollout(nx, ny, nz, steps, seed + k)
+        scs.append(sc)
+        hidden.append({"viscosity": float(0.35 + 1.05 * u[3]), "stiffness": float(sc.sph.stiffness),
+                       "surface_tension": float(sc.sph.surface_tension)})
+    return scs, hidden
+
+
 def loss_grid(scene: Scene, grid_size: int = 64):
     """The MC grid of the rollout loss: grid_size^3 voxels over the scene's
     box (cell = largest extent / grid_size), splat radius h."""

@@ -11,6 +11,7 @@ panics on wgpu validation errors; this library reports a status instead).
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -44,7 +45,19 @@ class SphSimulation3DGrid:
         check(self._lib.fs_grid_params(self._h, C.byref(self._grid)))
 
     # -- lifetime ---------------------------------------------------------------
+    def _register(self, dependent) -> None:
+        """Objects built on this simulation (rollouts, spray systems) are
+        closed before it: their C handles point into it."""
+        if not hasattr(self, "_dependents"):
+            self._dependents = []
+        self._dependents.append(weakref.ref(dependent))
+
     def close(self) -> None:
+        for ref in getattr(self, "_dependents", []):
+            dep = ref()
+            if dep is not None:
+                dep.close()
+        self._dependents = []
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.fs_destroy(self._h)
             self._h = C.c_void_p()

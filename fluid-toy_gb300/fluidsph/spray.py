@@ -39,6 +39,7 @@ class SpraySystem:
         check(self._lib.fs_spray_create(sim._h, int(scene), self.max_particles, C.byref(h)))
         self._h = h
         self.sim = sim
+        sim._register(self)
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -550,6 +550,7 @@ int fs_batch_upload_scene(FsSim *sim, uint32_t scene, const SphParticle3D *parti
  * iterations, every particle inside the SPH grid (else fs_adj_backward
  * returns FS_E_STATE). Works on plain simulations and batches. */
 typedef struct FsAdj FsAdj;
+/* An FsAdj (like an FsSpray) refers to its simulation: destroy it first. */
 int fs_adj_create(FsSim *sim, uint32_t checkpoint_every, FsAdj **out);
 int fs_adj_destroy(FsAdj *adj);
 /* Run nsteps steps from the simulation's current state, recording; the
@@ -567,6 +568,11 @@ int fs_adj_set_cotangents(FsAdj *adj, const float *dl_dpos, const float *dl_dvel
 int fs_adj_splat_mse_loss(FsAdj *adj, uint32_t scene, const GpuMcGridParams *grid,
                           const GpuContainerGeometry *geom, const float *target,
                           int target_on_device, double *loss);
+/* The density splat (fs_density_splat) of the scene's FINAL positions after
+ * fs_adj_forward, e.g. to build a target field from a hidden run: host or
+ * device memory, grid_size^3 floats. */
+int fs_adj_final_splat(FsAdj *adj, uint32_t scene, const GpuMcGridParams *grid,
+                       const GpuContainerGeometry *geom, float *out, int out_on_device);
 /* Reverse the recorded rollout: dL/dpos0 and dL/dvel0 as (N, 3) float rows
  * (host or device, either may be NULL) and, if dl_dparams is not NULL,
  * 3 doubles per scene (viscosity, stiffness, surface_tension). Leaves the

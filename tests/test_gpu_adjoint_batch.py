@@ -1,0 +1,57 @@
+"""The reverse pass on a batch: each scene's gradients (initial velocities,
+viscosity, surface tension) against the same scene's plain reverse pass, and
+each scene's loss against its plain loss. The reverse gathers may pick a
+different lanes-per-particle variant for the batch's particle count (a
+different fixed summation order), so gradients agree to a stated relative
+tolerance rather than bit for bit; the losses are bit-identical (the forward
+is)."""
+import numpy as np
+import pytest
+
+from helpers import gpu_sim_for_scene
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+
+
+def test_batch_gradients_match_plain(oracle_mod):
+    from fluidsph import scenes
+    from fluidsph.adjoint import DifferentiableRollout
+    from fluidsph.sim import SphBatch3DGrid
+    scs, hidden = scenes.reference_physics_batch(num_scenes=3, steps=8, seed=3)
+    grids = [scenes.loss_grid(s, 32) for s in scs]
+    # targets: each scene's hidden-viscosity run
+    targets = []
+    for s, hdn, mc in zip(scs, hidden, grids):
+        p = type(s.sph).from_buffer_copy(s.sph)
+        p.viscosity = hdn["viscosity"]
+        sim = gpu_sim_for_scene(s)
+        sim.update_sph_params(p)
+        r = DifferentiableRollout(sim, 4)
+        r.forward(s.steps)
+        targets.append(r.final_splat(mc, s.geom))
+    b = SphBatch3DGrid([s.particles for s in scs], [s.sph for s in scs], [s.geom for s in scs])
+    for k, s in enumerate(scs):
+        b.update_scene(k, gravity=s.gravity)
+    b.set_pcisph_iterations(scs[0].iterations)
+    rb = DifferentiableRollout(b, 4)
+    rb.forward(scs[0].steps)
+    losses = [rb.splat_mse_loss(grids[k], scs[k].geom, targets[k], scene=k) for k in range(3)]
+    dpos_b, dvel_b, dpar_b = rb.backward(scenes=3)
+    off = 0
+    for k, s in enumerate(scs):
+        sim = gpu_sim_for_scene(s)
+        r = DifferentiableRollout(sim, 4)
+        r.forward(s.steps)
+        loss = r.splat_mse_loss(grids[k], s.geom, targets[k])
+        _, dvel, dpar = r.backward()
+        assert loss == losses[k]
+        n = s.n
+        g_b = dvel_b[off:off + n].astype(np.float64)
+        scale = np.abs(dvel).max()
+        assert np.abs(g_b - dvel).max() <= RTOL * scale, k
+        for idx in (0, 2):
+            assert abs(dpar_b[k, idx] - dpar[0, idx]) <= RTOL * abs(dpar[0, idx]), (k, idx)
+        assert dpar_b[k, 1] == 0.0
+        off += n
