@@ -77,6 +77,9 @@ struct DevState {
   float2 *s_dens;   // density (boundary-corrected), near density
   float4 *s_nrm;    // Akinci normal, 0
   float4 *vel_x;    // post-XSPH velocity (the canonical velocity mid-step)
+  float4 *nb_pos;   // neighbour records (density pass): position, max(density, 1)
+  float4 *nb_vel;   //   pre-XSPH velocity, mass / max(density, 1)
+  float4 *nb_nrm;   //   Akinci normal, max(near density, 1)
   float4 *anp;      // non-pressure acceleration a_np
   float4 *pred_xp[2];  // predicted position, pressure (ping-pong)
   float *pred_rho[2];  // predicted density (ping-pong)

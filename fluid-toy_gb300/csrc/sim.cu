@@ -101,6 +101,9 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.s_dens = c.take<float2>(M);
   d.s_nrm = c.take<float4>(M);
   d.vel_x = c.take<float4>(M);
+  d.nb_pos = c.take<float4>(M);
+  d.nb_vel = c.take<float4>(M);
+  d.nb_nrm = c.take<float4>(M);
   d.anp = c.take<float4>(M);
   d.pred_xp[0] = c.take<float4>(M);
   d.pred_xp[1] = c.take<float4>(M);

@@ -45,12 +45,14 @@ __device__ __forceinline__ void for_each_hit(const Runs &R, Test &&test, Body &&
 }
 
 // ---- hit masks ----------------------------------------------------------------
-// The heavy per-hit bodies (force, XSPH, PCISPH pressure) run over a per-
-// particle bitmask of in-range neighbours: bit o is candidate o of the
-// particle's nine runs concatenated in visiting order. Walking the mask gives
-// every lane its own hits, one per loop iteration, in the shaders' order, so a
-// warp runs as long as its busiest lane (not as long as the union of its
-// lanes' candidate positions), and no candidate is tested twice.
+// The heavy per-hit bodies (force, XSPH) run over a per-particle bitmask of
+// in-range neighbours written by the density pass. Each run's candidates start
+// a new word: bit k of the run's word w is candidate lo + 32w + k, so a run of
+// length L owns ceil(L / 32) words and a particle R.words words in run order.
+// Walking the mask gives every lane its own hits, one per loop iteration, in
+// the shaders' order, so a warp runs as long as its busiest lane (not as long
+// as the union of its lanes' candidate positions), and no candidate is tested
+// twice.
 constexpr uint32_t MASK_NONE = 0xffffffffu;
 
 // Word offset of each particle's mask, allocated per warp from a bump counter.
@@ -75,32 +77,88 @@ __device__ __forceinline__ uint32_t alloc_mask(bool active, uint32_t nwords,
   return uint32_t(off);
 }
 
-// Walk a particle's mask: one hit per iteration, empty words skipped inside
-// the iteration, so lanes progress independently.
+// Cursor over a particle's mask: next() yields the hit slots in visiting
+// order, skipping empty words inside the call, so lanes progress
+// independently (one hit per call).
+struct MaskWalk {
+  const uint32_t *words;
+  uint32_t nwords;    // words of the particle
+  uint32_t w;         // index of the word held in `nxt`
+  uint32_t cur;       // bits left of the current word
+  uint32_t nxt;       // word w, loaded one ahead to hide its latency
+  uint32_t wbase;     // slot of bit 0 of the current word
+  uint32_t row_wend;  // first word index past the current run
+  int row;
+
+  __device__ __forceinline__ void init(const Runs &R, const uint32_t *wds) {
+    words = wds;
+    nwords = R.words;
+    w = 0u;
+    cur = 0u;
+    nxt = nwords ? wds[0] : 0u;
+    wbase = 0u;
+    row_wend = 0u;
+    row = -1;
+  }
+  __device__ __forceinline__ bool next(const Runs &R, uint32_t &j) {
+    while (cur == 0u) {
+      if (w == nwords) return false;
+      // runs shorter than one candidate own no word; w < nwords guarantees a
+      // later run that owns word w
+      while (w == row_wend) {
+        row++;
+        row_wend += (R.hi[row] - R.lo[row] + 31u) >> 5;
+        wbase = R.lo[row] - 32u;  // modulo 2^32: the += 32 below restores lo
+      }
+      wbase += 32u;
+      cur = nxt;
+      w++;
+      nxt = w < nwords ? words[w] : 0u;
+    }
+    j = wbase + uint32_t(__ffs(cur) - 1);
+    cur &= cur - 1u;
+    return true;
+  }
+};
+
 template <class Body>
 __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, Body &&body) {
-  const uint32_t nwords = (R.total + 31u) >> 5;
-  if (nwords == 0u) return;
-  // `nxt` holds word w+1, loaded one word ahead to hide its latency
-  uint32_t w = 0u, cur = words[0], nxt = nwords > 1u ? words[1] : 0u;
-  int row = 0;
-  uint32_t row_start = 0u, row_end = R.hi[0] - R.lo[0];
+  MaskWalk m;
+  m.init(R, words);
+  uint32_t j;
+  while (m.next(R, j)) body(j);
+}
+
+// The same walk with the neighbour records of the next hit loaded while the
+// current hit's body runs (software pipelining of the dependent gathers).
+template <class Load, class Body>
+__device__ __forceinline__ void walk_mask_pipelined(const Runs &R, const uint32_t *words,
+                                                    Load &&load, Body &&body) {
+  MaskWalk m;
+  m.init(R, words);
+  uint32_t j;
+  if (!m.next(R, j)) return;
+  auto rec = load(j);
   while (true) {
-    while (cur == 0u && ++w < nwords) {
-      cur = nxt;
-      nxt = w + 1u < nwords ? words[w + 1u] : 0u;
-    }
-    if (cur == 0u) break;
-    const uint32_t o = (w << 5) + uint32_t(__ffs(cur) - 1);
-    cur &= cur - 1u;
-    while (o >= row_end) {
-      row++;
-      row_start = row_end;
-      row_end += R.hi[row] - R.lo[row];
-    }
-    body(R.lo[row] + (o - row_start));
+    uint32_t jn = 0u;
+    const bool more = m.next(R, jn);
+    decltype(rec) recn{};
+    if (more) recn = load(jn);
+    body(j, rec);
+    if (!more) break;
+    j = jn;
+    rec = recn;
   }
 }
+
+// Per-particle neighbour records, written by the density pass for the later
+// gathers: pos = (position, max(density, 1)), vel = (pre-XSPH velocity,
+// mass / max(density, 1)), nrm = (Akinci normal, max(near density, 1)). Each
+// value is the exact expression the shaders evaluate per neighbour, computed
+// once per particle instead of once per pair.
+struct NbrRecords {
+  float4 *pos, *vel, *nrm;
+};
 
 __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int dir_half) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -112,11 +170,15 @@ __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int
 
 // sph_density_3d_grid.wgsl:111-194 (writes the sorted copy only). Besides the
 // density it records each particle's hit mask (1e-12 < r^2 < h^2, the XSPH and
-// force criterion) for the later passes.
+// force criterion) and its neighbour records for the later passes. The body
+// is evaluated for every candidate and the sums are updated with selects
+// (x = hit ? x + t : x, the same bits as the shader's branch), so lanes never
+// split inside the loop.
 __device__ __forceinline__ void density_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
+              const float4 *__restrict__ s_vel,
               const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
-              float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
+              float4 *__restrict__ s_nrm, NbrRecords nb, unsigned long long *__restrict__ stats,
               uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
               uint32_t *__restrict__ mask_hits, unsigned long long *__restrict__ mask_alloc,
               unsigned long long mask_cap) {
@@ -127,53 +189,56 @@ __device__ __forceinline__ void density_one(
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
   const float scale_n = 15.0f / (PI_F * P.kernel_radius_pow6);
   const float m_over_rho0 = mass / P.rest_density;
-  unsigned long long hits = 0, nonself = 0;
+  uint32_t hits = 0u, nonself = 0u;
   float3 pos_i = f3(0.f, 0.f, 0.f);
   Runs R;
   R.count = 0;
   R.total = 0;
+  R.words = 0;
   if (active) {
     pos_i = xyz(s_pos[s]);
     neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   }
-  const uint32_t off = alloc_mask(active, (R.total + 31u) >> 5, mask_alloc, mask_cap);
+  const uint32_t off = alloc_mask(active, R.words, mask_alloc, mask_cap);
   if (active) {
     mask_off[s] = off;
     uint32_t *words = mask_words + (off == MASK_NONE ? 0u : off);
     float density = 0.0f, near_density = 0.0f;
     float3 normal = f3(0.f, 0.f, 0.f);
-    uint32_t word = 0u, bit = 0u, widx = 0u;
+    uint32_t widx = 0u;
     for (int r = 0; r < R.count; r++) {
+      for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
+        const uint32_t cnt = min(32u, R.hi[r] - base);
+        uint32_t word = 0u, bit = 1u;
 #pragma unroll 4
-      for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
-        const float4 pj = __ldg(s_pos + j);
-        const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
-        const float r_sq = rx * rx + ry * ry + rz * rz;
-        if (r_sq < h2) {
-          hits++;
+        for (uint32_t k = 0; k < cnt; k++, bit <<= 1) {
+          const float4 pj = __ldg(s_pos + base + k);
+          const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+          const float r_sq = rx * rx + ry * ry + rz * rz;
+          const bool hit = r_sq < h2;
+          const bool ns = hit && r_sq > 1e-12f;
           const float rr = sqrtf(r_sq);
           const float diff = h2 - r_sq;
-          density += mass * (scale_d * diff * diff * diff);
+          const float td = mass * (scale_d * diff * diff * diff);
           const float dn = h - rr;
-          near_density += mass * (scale_n * dn * dn * dn);
-          if (r_sq > 1e-12f) {
-            nonself++;
-            word |= 1u << bit;
-            normal.x = normal.x + m_over_rho0 * rx * diff * diff;
-            normal.y = normal.y + m_over_rho0 * ry * diff * diff;
-            normal.z = normal.z + m_over_rho0 * rz * diff * diff;
-          }
+          const float tn = mass * (scale_n * dn * dn * dn);
+          density = hit ? density + td : density;
+          near_density = hit ? near_density + tn : near_density;
+          const float nx = normal.x + m_over_rho0 * rx * diff * diff;
+          const float ny = normal.y + m_over_rho0 * ry * diff * diff;
+          const float nz = normal.z + m_over_rho0 * rz * diff * diff;
+          normal.x = ns ? nx : normal.x;
+          normal.y = ns ? ny : normal.y;
+          normal.z = ns ? nz : normal.z;
+          hits += hit ? 1u : 0u;
+          word |= ns ? bit : 0u;
         }
-        if (++bit == 32u) {
-          if (off != MASK_NONE) words[widx] = word;
-          widx++;
-          word = 0u;
-          bit = 0u;
-        }
+        if (off != MASK_NONE) words[widx] = word;
+        widx++;
+        nonself += uint32_t(__popc(word));
       }
     }
-    if (bit && off != MASK_NONE) words[widx] = word;
-    mask_hits[s] = uint32_t(nonself);
+    mask_hits[s] = nonself;
     const float gamma = boundary_gamma(U->geom, h, pos_i);
     density = density / gamma;
     const float h8 = P.kernel_radius_pow6 * h * h;
@@ -181,24 +246,30 @@ __device__ __forceinline__ void density_one(
     normal = normal * normal_scale;
     s_dens[s] = make_float2(density, near_density);
     s_nrm[s] = make_float4(normal.x, normal.y, normal.z, 0.0f);
+    const float dmax = fmaxf(density, 1.0f);
+    const float4 vs = s_vel[s];
+    nb.pos[s] = make_float4(pos_i.x, pos_i.y, pos_i.z, dmax);
+    nb.vel[s] = make_float4(vs.x, vs.y, vs.z, mass / dmax);
+    nb.nrm[s] = make_float4(normal.x, normal.y, normal.z, fmaxf(near_density, 1.0f));
   }
   const unsigned long long cand = warp_sum_u64(R.total);
-  hits = warp_sum_u64(hits);
-  nonself = warp_sum_u64(nonself);
+  const unsigned long long hsum = warp_sum_u64(hits);
+  const unsigned long long nsum = warp_sum_u64(nonself);
   if ((threadIdx.x & 31) == 0 && cand) {
     atomicAdd(stats + STAT_CAND_DENSITY, cand);
-    atomicAdd(stats + STAT_HIT_DENSITY, hits);
-    atomicAdd(stats + STAT_HIT_NONSELF, nonself);
+    atomicAdd(stats + STAT_HIT_DENSITY, hsum);
+    atomicAdd(stats + STAT_HIT_NONSELF, nsum);
   }
 }
 
 // ---- XSPH -------------------------------------------------------------------
 // xsph.wgsl:81-138; the result is the post-XSPH velocity in sorted order (the
-// reference scatters it to the canonical array).
+// reference scatters it to the canonical array). mass / density_j comes from
+// the neighbour record (the same quotient, evaluated once per particle).
 __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
-                                              const float4 *__restrict__ s_pos,
                                               const float4 *__restrict__ s_vel,
-                                              const float2 *__restrict__ s_dens,
+                                              const float4 *__restrict__ nb_pos,
+                                              const float4 *__restrict__ nb_vel,
                                               const uint32_t *__restrict__ begin,
                                               const uint32_t *__restrict__ mask_words,
                                               const uint32_t *__restrict__ mask_off,
@@ -213,32 +284,37 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
     return;
   }
   const float3 vel_i = xyz(vi4);
-  const float h2 = P.kernel_radius_sq, mass = P.mass;
+  const float h2 = P.kernel_radius_sq;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
-  const float3 pos_i = xyz(s_pos[s]);
+  const float3 pos_i = xyz(nb_pos[s]);
   Runs R;
   neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   float3 corr = f3(0.f, 0.f, 0.f);
-  auto body = [&](uint32_t j, float r_sq) {
-    const float density_j = fmaxf(__ldg(&s_dens[j].x), 1.0f);
-    const float3 vel_j = xyz(__ldg(s_vel + j));
-    const float diff = h2 - r_sq;
-    const float w = scale_d * diff * diff * diff;
-    corr = corr + (mass / density_j) * (vel_j - vel_i) * w;
+  struct Rec {
+    float4 p, v;
   };
-  auto dist2 = [&](uint32_t j) {
-    const float4 pj = __ldg(s_pos + j);
+  auto dist2 = [&](float4 pj) {
     const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
     return rx * rx + ry * ry + rz * rz;
   };
+  auto body = [&](uint32_t, const Rec &q) {
+    const float r_sq = dist2(q.p);
+    const float diff = h2 - r_sq;
+    const float w = scale_d * diff * diff * diff;
+    corr = corr + q.v.w * (xyz(q.v) - vel_i) * w;
+  };
+  auto load = [&](uint32_t j) { return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j)}; };
   const uint32_t off = mask_off[s];
   if (off != MASK_NONE) {
-    walk_mask(R, mask_words + off, [&](uint32_t j) { body(j, dist2(j)); });
+    walk_mask_pipelined(R, mask_words + off, load, body);
   } else {
-    float r_sq = 0.f;
     for_each_hit(
-        R, [&](uint32_t j) { r_sq = dist2(j); return r_sq < h2 && r_sq > 1e-12f; },
-        [&](uint32_t j) { body(j, r_sq); });
+        R,
+        [&](uint32_t j) {
+          const float r_sq = dist2(__ldg(nb_pos + j));
+          return r_sq < h2 && r_sq > 1e-12f;
+        },
+        [&](uint32_t j) { body(j, load(j)); });
   }
   const float3 vn = vel_i + eps * corr;
   vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
@@ -249,7 +325,8 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
 // particle (sorted order).
 __device__ __forceinline__ void force_predict_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
-                    const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
+                    const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
+                    const float4 *__restrict__ nb_nrm, const float2 *__restrict__ s_dens,
                     const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
@@ -277,11 +354,16 @@ __device__ __forceinline__ void force_predict_one(
   // Every arm of the shader's branches is evaluated and the accumulators are
   // updated with selects (x = c ? x + t : x), which leaves their bits exactly
   // as the branches would: lanes of a warp then never split inside the body.
-  auto body = [&](uint32_t j) {
-    const float3 pos_j = xyz(__ldg(s_pos + j));
-    const float2 dj = __ldg(s_dens + j);
-    const float3 vel_j = xyz(__ldg(s_vel + j));
-    const float3 n_j = xyz(__ldg(s_nrm + j));
+  struct Rec {
+    float4 p, v, n;
+  };
+  auto load = [&](uint32_t j) {
+    return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j), __ldg(nb_nrm + j)};
+  };
+  auto body = [&](uint32_t j, const Rec &q) {
+    const float3 pos_j = xyz(q.p);
+    const float3 vel_j = xyz(q.v);
+    const float3 n_j = xyz(q.n);
     const float3 r_vec = pos_i - pos_j;
     const float r_sq = dot3(r_vec, r_vec);
     const float rr = sqrtf(r_sq);
@@ -299,8 +381,8 @@ __device__ __forceinline__ void force_predict_one(
     if (close && !tabulated)
       dir_close = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
     const float3 dir = close ? dir_close : dir_far;
-    const float density_j = fmaxf(dj.x, 1.0f);
-    const float near_density_j = fmaxf(dj.y, 1.0f);
+    const float density_j = q.p.w;       // max(density_j, 1)
+    const float near_density_j = q.n.w;  // max(near density_j, 1)
     const float near_pressure_j = near_k * near_density_j;
     const float dg = h - rr;
     const float grad = scale_g * dg * dg;
@@ -326,17 +408,17 @@ __device__ __forceinline__ void force_predict_one(
   };
   const uint32_t off = mask_off[s];
   if (off != MASK_NONE) {
-    walk_mask(R, mask_words + off, body);
+    walk_mask_pipelined(R, mask_words + off, load, body);
   } else {
     for_each_hit(
         R,
         [&](uint32_t j) {
-          const float4 pj = __ldg(s_pos + j);
+          const float4 pj = __ldg(nb_pos + j);
           const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
           const float r_sq = rx * rx + ry * ry + rz * rz;
           return r_sq < h2 && r_sq > 1e-12f;
         },
-        body);
+        [&](uint32_t j) { body(j, load(j)); });
   }
   a_c = a_c * P.surface_tension;
   const float3 a_g = xyz(U->gravity.direction);
@@ -373,10 +455,11 @@ __device__ __forceinline__ void solve_one(
   const float h = P.kernel_radius, h2 = P.kernel_radius_sq, mass = P.mass;
   const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
   const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
-  unsigned long long hits = 0;
+  uint32_t hits = 0u;
   Runs R;
   R.count = 0;
   R.total = 0;
+  R.words = 0;
   if (active) {
     const float4 self_xp = xp_in[s];
     const float3 pred_pos = xyz(self_xp);
@@ -447,10 +530,10 @@ __device__ __forceinline__ void solve_one(
     }
   }
   const unsigned long long cand = warp_sum_u64(R.total);
-  hits = warp_sum_u64(hits);
+  const unsigned long long hsum = warp_sum_u64(hits);
   if ((threadIdx.x & 31) == 0 && cand) {
     atomicAdd(stats + STAT_CAND_SOLVE, cand);
-    atomicAdd(stats + STAT_HIT_SOLVE, hits);
+    atomicAdd(stats + STAT_HIT_SOLVE, hsum);
   }
 }
 
@@ -458,11 +541,12 @@ __device__ __forceinline__ void solve_one(
 // The neighbour passes' cost per particle ranges over two orders of
 // magnitude (the clumps carry most of the pairs). Persistent warps take
 // 32-slot tasks from a queue ordered heaviest first (longest-processing-time
-// scheduling). Density, XSPH and solve take warps of 32 consecutive sorted
-// slots (neighbouring particles share their neighbours' loads in L1); the
-// force pass, whose per-hit body is long, takes 32 slots of similar hit
-// count from a permutation built by a counting sort on a log-linear work key,
-// so its lanes finish together. Which lane computes a particle does not
+// scheduling). Density and solve, which test every candidate, take warps of
+// 32 consecutive sorted slots (neighbouring particles share their
+// neighbours' loads in L1); the mask walks (XSPH, force), whose lanes run as
+// many iterations as they have hits, take 32 slots of similar hit count from
+// a permutation built by a counting sort on a log-linear work key, so their
+// lanes finish together. Which lane computes a particle does not
 // change its result.
 __device__ __forceinline__ uint32_t work_key(uint32_t c) {
   return c < 4096u ? c : 4096u + min((c - 4096u) >> 4, 4095u);
@@ -581,39 +665,39 @@ __global__ void __launch_bounds__(256)
 
 __global__ void __launch_bounds__(128)
     k_density(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
-              const uint32_t *__restrict__ begin, float2 *__restrict__ s_dens,
-              float4 *__restrict__ s_nrm, unsigned long long *__restrict__ stats,
-              uint32_t *__restrict__ mask_words, uint32_t *__restrict__ mask_off,
-              uint32_t *__restrict__ mask_hits, unsigned long long *__restrict__ mask_alloc,
-              unsigned long long mask_cap) {
+              const float4 *__restrict__ s_vel, const uint32_t *__restrict__ begin,
+              float2 *__restrict__ s_dens, float4 *__restrict__ s_nrm, NbrRecords nb,
+              unsigned long long *__restrict__ stats, uint32_t *__restrict__ mask_words,
+              uint32_t *__restrict__ mask_off, uint32_t *__restrict__ mask_hits,
+              unsigned long long *__restrict__ mask_alloc, unsigned long long mask_cap) {
   for_warp_tasks(q, [&](uint32_t s) {
-    density_one(s, v, s_pos, begin, s_dens, s_nrm, stats, mask_words, mask_off, mask_hits,
-                mask_alloc, mask_cap);
+    density_one(s, v, s_pos, s_vel, begin, s_dens, s_nrm, nb, stats, mask_words, mask_off,
+                mask_hits, mask_alloc, mask_cap);
   });
 }
 
 __global__ void __launch_bounds__(128)
-    k_xsph(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
-           const float4 *__restrict__ s_vel, const float2 *__restrict__ s_dens,
+    k_xsph(TaskQueue q, SceneView v, const float4 *__restrict__ s_vel,
+           const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
            const uint32_t *__restrict__ begin, const uint32_t *__restrict__ mask_words,
            const uint32_t *__restrict__ mask_off, float4 *__restrict__ vel_x) {
   for_warp_tasks(q, [&](uint32_t s) {
-    xsph_one(s, v, s_pos, s_vel, s_dens, begin, mask_words, mask_off, vel_x);
+    xsph_one(s, v, s_vel, nb_pos, nb_vel, begin, mask_words, mask_off, vel_x);
   });
 }
 
 __global__ void __launch_bounds__(128, 4)
-    k_force_predict(TaskQueue q, SceneView v,
-                    const float4 *__restrict__ s_pos, const float4 *__restrict__ s_vel,
-                    const float2 *__restrict__ s_dens, const float4 *__restrict__ s_nrm,
-                    const float4 *__restrict__ vel_x, const uint32_t *__restrict__ begin,
-                    const float4 *__restrict__ dir_tab, int dir_half,
-                    const uint32_t *__restrict__ mask_words, const uint32_t *__restrict__ mask_off,
-                    float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
-                    float *__restrict__ pred_rho) {
+    k_force_predict(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
+                    const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
+                    const float4 *__restrict__ nb_nrm, const float2 *__restrict__ s_dens,
+                    const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
+                    const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
+                    int dir_half, const uint32_t *__restrict__ mask_words,
+                    const uint32_t *__restrict__ mask_off, float4 *__restrict__ anp,
+                    float4 *__restrict__ pred_xp, float *__restrict__ pred_rho) {
   for_warp_tasks(q, [&](uint32_t s) {
-    force_predict_one(s, v, s_pos, s_vel, s_dens, s_nrm, vel_x, begin, dir_tab, dir_half,
-                      mask_words, mask_off, anp, pred_xp, pred_rho);
+    force_predict_one(s, v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm, vel_x, begin, dir_tab,
+                      dir_half, mask_words, mask_off, anp, pred_xp, pred_rho);
   });
 }
 
@@ -959,21 +1043,22 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_density, d.sm_count);
-  k_density<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.cell_begin, d.s_dens, d.s_nrm, d.stats,
-                                    d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc,
-                                    d.mask_cap);
+  const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm};
+  k_density<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm,
+                                    nb, d.stats, d.mask_words, d.mask_off, d.mask_hits,
+                                    d.mask_alloc, d.mask_cap);
   return cudaGetLastError();
 }
 
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   TaskQueue q;
-  cudaError_t e = prepare_queue(d, d.warp_order, false, n, 0, st, &q);
+  cudaError_t e = prepare_queue(d, d.perm_hit, true, n, 0, st, &q);
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_xsph, d.sm_count);
-  k_xsph<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.s_dens, d.cell_begin, d.mask_words,
-                                 d.mask_off, d.vel_x);
+  k_xsph<<<blocks, 128, 0, st>>>(q, d.view(), d.s_vel, d.nb_pos, d.nb_vel, d.cell_begin,
+                                 d.mask_words, d.mask_off, d.vel_x);
   return cudaGetLastError();
 }
 
@@ -986,7 +1071,8 @@ cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st)
   if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count);
   float4 *xp_out = d.rec_xp ? d.rec_xp[0] : d.pred_xp[0];
   float *rho_out = d.rec_rho ? d.rec_rho[0] : d.pred_rho[0];
-  k_force_predict<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.s_dens, d.s_nrm, d.vel_x,
+  k_force_predict<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm,
+                                          d.s_dens, d.s_nrm, d.vel_x,
                                           d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
                                           d.mask_off, d.anp, xp_out, rho_out);
   return cudaGetLastError();
