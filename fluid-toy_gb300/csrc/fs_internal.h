@@ -80,6 +80,7 @@ struct DevState {
   float4 *nb_pos;   // neighbour records (density pass): position, max(density, 1)
   float4 *nb_vel;   //   pre-XSPH velocity, mass / max(density, 1)
   float4 *nb_nrm;   //   Akinci normal, max(near density, 1)
+  float *pterm[2];  // solve: p / max(rho, 1)^2 per particle, ping-pong with pred_xp
   float4 *anp;      // non-pressure acceleration a_np
   float4 *pred_xp[2];  // predicted position, pressure (ping-pong)
   float *pred_rho[2];  // predicted density (ping-pong)

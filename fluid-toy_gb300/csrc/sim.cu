@@ -109,6 +109,8 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.pred_xp[1] = c.take<float4>(M);
   d.pred_rho[0] = c.take<float>(M);
   d.pred_rho[1] = c.take<float>(M);
+  d.pterm[0] = c.take<float>(M);
+  d.pterm[1] = c.take<float>(M);
   d.pred_v = c.take<float4>(M);
   d.cell_of = c.take<uint32_t>(M);
   d.rank_of = c.take<uint32_t>(M);

@@ -129,25 +129,37 @@ __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, 
   while (m.next(R, j)) body(j);
 }
 
-// The same walk with the neighbour records of the next hit loaded while the
-// current hit's body runs (software pipelining of the dependent gathers).
-template <class Load, class Body>
-__device__ __forceinline__ void walk_mask_pipelined(const Runs &R, const uint32_t *words,
-                                                    Load &&load, Body &&body) {
+// The walk with a ring of D hits in flight: slot i holds hit k and, once
+// its body has run, is refilled with hit k + D, so the gathers of the next
+// D - 1 hits overlap each body. Hits are processed in visiting order.
+template <int D, class Load, class Body>
+__device__ __forceinline__ void walk_mask_ring(const Runs &R, const uint32_t *words, Load &&load,
+                                               Body &&body) {
   MaskWalk m;
   m.init(R, words);
-  uint32_t j;
-  if (!m.next(R, j)) return;
-  auto rec = load(j);
-  while (true) {
-    uint32_t jn = 0u;
-    const bool more = m.next(R, jn);
-    decltype(rec) recn{};
-    if (more) recn = load(jn);
-    body(j, rec);
-    if (!more) break;
-    j = jn;
-    rec = recn;
+  uint32_t jq[D];
+  bool vq[D];
+  using Rec = decltype(load(0u));
+  Rec rq[D];
+#pragma unroll
+  for (int i = 0; i < D; i++) {
+    vq[i] = m.next(R, jq[i]);
+    rq[i] = vq[i] ? load(jq[i]) : Rec{};
+  }
+  bool more = vq[0];
+  while (more) {
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      if (more) {
+        if (!vq[i]) {
+          more = false;
+        } else {
+          body(jq[i], rq[i]);
+          vq[i] = m.next(R, jq[i]);
+          if (vq[i]) rq[i] = load(jq[i]);
+        }
+      }
+    }
   }
 }
 
@@ -210,7 +222,7 @@ __device__ __forceinline__ void density_one(
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
         uint32_t word = 0u, bit = 1u;
-#pragma unroll 4
+#pragma unroll 8
         for (uint32_t k = 0; k < cnt; k++, bit <<= 1) {
           const float4 pj = __ldg(s_pos + base + k);
           const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
@@ -306,7 +318,7 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
   auto load = [&](uint32_t j) { return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j)}; };
   const uint32_t off = mask_off[s];
   if (off != MASK_NONE) {
-    walk_mask_pipelined(R, mask_words + off, load, body);
+    walk_mask_ring<3>(R, mask_words + off, load, body);
   } else {
     for_each_hit(
         R,
@@ -377,7 +389,8 @@ __device__ __forceinline__ void force_predict_one(
                               div_by_rcp(dv.z, rr, y_rr));
     const int d = int(s) - int(j);
     const bool tabulated = d >= -dir_half && d <= dir_half;
-    float3 dir_close = tabulated ? xyz(__ldg(dir_tab + (tabulated ? d + dir_half : 0))) : dir_far;
+    float3 dir_close = dir_far;
+    if (close && tabulated) dir_close = xyz(__ldg(dir_tab + (d + dir_half)));
     if (close && !tabulated)
       dir_close = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
     const float3 dir = close ? dir_close : dir_far;
@@ -408,7 +421,9 @@ __device__ __forceinline__ void force_predict_one(
   };
   const uint32_t off = mask_off[s];
   if (off != MASK_NONE) {
-    walk_mask_pipelined(R, mask_words + off, load, body);
+    // the loads are not pipelined here: the body is long enough to cover
+    // them, and the ring's registers would cost occupancy
+    walk_mask(R, mask_words + off, [&](uint32_t j) { body(j, load(j)); });
   } else {
     for_each_hit(
         R,
@@ -439,16 +454,19 @@ __device__ __forceinline__ void force_predict_one(
 // it. Iteration 0 reads the predict output, where every pressure is 0: the
 // pressure sum is +0 exactly, so it is skipped (HAS_PRESSURE=false) with
 // bit-identical results. The last iteration only produces the corrected
-// velocity.
+// velocity. Each other iteration also writes every particle's pressure term
+// p / max(rho, 1)^2 (the shader's per-neighbour quotient, which depends on
+// the neighbour only), so the next iteration reads it instead of dividing per
+// pair.
 template <bool HAS_PRESSURE, bool LAST>
 __device__ __forceinline__ void solve_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
-            const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
-            const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
-            float *__restrict__ rho_out, float4 *__restrict__ v_out,
-            unsigned long long *__restrict__ stats, float4 *__restrict__ ap_out) {
+            const float *__restrict__ pterm_in, float4 *__restrict__ xp_out,
+            float *__restrict__ rho_out, float *__restrict__ pterm_out,
+            float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
+            float4 *__restrict__ ap_out) {
   const bool active = s < v.b->n_sorted;
   const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
@@ -464,22 +482,23 @@ __device__ __forceinline__ void solve_one(
     const float4 self_xp = xp_in[s];
     const float3 pred_pos = xyz(self_xp);
     const float old_p = self_xp.w;
-    const float sd = fmaxf(rho_in[s], 1.0f);
     const float3 pos_i = xyz(s_pos[s]);  // current position decides the cells
     neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
     float pred_density = 0.0f;
     float3 a_p = f3(0.f, 0.f, 0.f);
-    const float self_term = old_p / (sd * sd);
-    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq, float np) {
+    // old_p / (sd * sd) with sd = max(rho_in[s], 1), written by the previous
+    // iteration (read only when there is pressure)
+    const float self_term = HAS_PRESSURE ? pterm_in[s] : 0.0f;
+    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
       const float rr = sqrtf(r_sq);
-      const float nd = fmaxf(__ldg(rho_in + j), 1.0f);
+      const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
       const float y_rr = __frcp_rn(rr);
       const float3 nr = -r_vec;
       const float3 dir = f3(div_by_rcp(nr.x, rr, y_rr), div_by_rcp(nr.y, rr, y_rr),
                             div_by_rcp(nr.z, rr, y_rr));
       const float dg = h - rr;
       const float grad = scale_g * dg * dg;
-      a_p = a_p + (-mass * (self_term + np / (nd * nd)) * grad) * dir;
+      a_p = a_p + (-mass * (self_term + pt) * grad) * dir;
     };
     // candidates in chunks of up to 32: the predicted density is summed while
     // testing; the pressure hits of the chunk go to a per-lane bitmask that
@@ -488,7 +507,7 @@ __device__ __forceinline__ void solve_one(
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
         uint32_t chunk = 0u;
-#pragma unroll 4
+#pragma unroll 8
         for (uint32_t k = 0; k < cnt; k++) {
           const float4 nb = __ldg(xp_in + base + k);
           const float3 r_vec = pred_pos - xyz(nb);
@@ -506,7 +525,7 @@ __device__ __forceinline__ void solve_one(
             chunk &= chunk - 1u;
             const float4 nb = __ldg(xp_in + j);
             const float3 r_vec = pred_pos - xyz(nb);
-            pressure(j, r_vec, dot3(r_vec, r_vec), nb.w);
+            pressure(j, r_vec, dot3(r_vec, r_vec));
           }
         }
       }
@@ -527,6 +546,8 @@ __device__ __forceinline__ void solve_one(
       const float3 x_star = pos_i + dt * v_star;
       xp_out[s] = make_float4(x_star.x, x_star.y, x_star.z, new_p);
       rho_out[s] = pred_density;
+      const float nd = fmaxf(pred_density, 1.0f);
+      pterm_out[s] = new_p / (nd * nd);
     }
   }
   const unsigned long long cand = warp_sum_u64(R.total);
@@ -706,13 +727,13 @@ __global__ void __launch_bounds__(128)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
-            const float *__restrict__ rho_in, uint32_t *__restrict__ mask_words,
-            const uint32_t *__restrict__ mask_off, float4 *__restrict__ xp_out,
-            float *__restrict__ rho_out, float4 *__restrict__ v_out,
-            unsigned long long *__restrict__ stats, float4 *__restrict__ ap_out) {
+            const float *__restrict__ pterm_in, float4 *__restrict__ xp_out,
+            float *__restrict__ rho_out, float *__restrict__ pterm_out,
+            float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
+            float4 *__restrict__ ap_out) {
   for_warp_tasks(q, [&](uint32_t s) {
-    solve_one<HAS_PRESSURE, LAST>(s, v, s_pos, vel_x, anp, begin, xp_in, rho_in, mask_words,
-                                  mask_off, xp_out, rho_out, v_out, stats, ap_out);
+    solve_one<HAS_PRESSURE, LAST>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
+                                  rho_out, pterm_out, v_out, stats, ap_out);
   });
 }
 
@@ -1083,7 +1104,6 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   const int in = iter & 1, out = in ^ 1;
   // ping-pong, or the recorded levels iter -> iter + 1 when recording
   const float4 *xp_in = d.rec_xp ? d.rec_xp[iter] : d.pred_xp[in];
-  const float *rho_in = d.rec_rho ? d.rec_rho[iter] : d.pred_rho[in];
   float4 *xp_out = d.rec_xp ? d.rec_xp[iter + 1] : d.pred_xp[out];
   float *rho_out = d.rec_rho ? d.rec_rho[iter + 1] : d.pred_rho[out];
   float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
@@ -1095,8 +1115,8 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     static unsigned blocks = 0;                                                               \
     if (!blocks) blocks = persistent_blocks(k_solve<P_, L_>, d.sm_count);                    \
     k_solve<P_, L_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp, d.cell_begin,    \
-                                            xp_in, rho_in, d.mask_words, d.mask_off, xp_out,  \
-                                            rho_out, d.pred_v, d.stats, ap_out);              \
+                                            xp_in, d.pterm[in], xp_out, rho_out, d.pterm[out], \
+                                            d.pred_v, d.stats, ap_out);                       \
   } while (0)
   if (iter == 0 && last) FS_SOLVE(false, true);
   else if (iter == 0) FS_SOLVE(false, false);
