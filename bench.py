@@ -373,7 +373,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                 "d2h_bytes_per_step": d2h,
                 "pattern": "per step: upload sph/geometry/gravity/rigid-body structs, "
                            "fs_step(1), read rigid-body accumulator (sync)"},
-        "gpu_launches": K * (10 + scene.iterations),
+        "gpu_launches": K * (13 + scene.iterations),
         "clocks": clk,
     }
     if forms is not None:
@@ -473,7 +473,7 @@ def run_batch(args, dist: Dist) -> dict | None:
                          "pattern": "one SphSimulation3DGrid per scene on one stream, "
                                     "each fs_step(k) graph-replayed, scene after scene"},
         "batched_over_looped": round(value / loop_value, 3) if loop_value else None,
-        "gpu_launches": K * (10 + scenes[0].iterations),
+        "gpu_launches": K * (13 + scenes[0].iterations),
         "clocks": clk,
     }
 

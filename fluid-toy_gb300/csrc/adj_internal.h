@@ -20,6 +20,9 @@ struct TapeView {
   const float *rho[kMaxAdjIters + 1];  // predicted densities per level
   const float4 *ap[kMaxAdjIters];      // pressure acceleration before the clamp
   const uint32_t *order;               // the step's task order (warp ids, heaviest first)
+  const uint32_t *mask_words;          // the step's hit masks (density pass)
+  const uint32_t *mask_off;            // word offset of each slot's mask, or MASK_NONE
+  const uint32_t *perm_hit;            // slots ordered by hit count, heaviest first
 };
 
 // Reverse accumulators, grid-sorted order.

@@ -84,6 +84,8 @@ __device__ __forceinline__ float3 group_sum3(float3 x) {
 // recorded task order (heaviest first) split L ways, so a heavy warp's
 // particles spread over L concurrently running warps and the critical path
 // (the heaviest particle's candidate list) shrinks L-fold.
+// With a slot permutation (q.slots) the 32 slots of task group t / L are
+// perm[32 (t / L) .. 32 (t / L) + 31] (0xffffffff past the end).
 template <int L, class F>
 __device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
   const unsigned lane = threadIdx.x & 31u;
@@ -93,7 +95,44 @@ __device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
     if (lane == 0u) t = atomicAdd(q.counter, 1u);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= ntasks) break;
-    f(__ldg(q.perm + t / L) * 32u + (t % L) * (32u / L) + lane / L, lane % L);
+    const uint32_t within = (t % L) * (32u / L) + lane / L;
+    uint32_t slot;
+    if (q.slots) {
+      const uint32_t idx = (t / L) * 32u + within;
+      slot = idx < q.n ? __ldg(q.perm + idx) : 0xffffffffu;
+    } else {
+      slot = __ldg(q.perm + t / L) * 32u + within;
+    }
+    f(slot, lane % L);
+  }
+}
+
+// q's in-range neighbours j (1e-12 < r^2 < h^2, the force / XSPH / normal
+// criterion): walked from the recorded step's hit mask when q has one (the
+// forward's own decisions, no candidate tests), else found by testing the
+// candidates. Lane `sub` of q's L lanes takes every L-th hit.
+template <int L, class InRange, class Body>
+__device__ __forceinline__ void for_hits_sub(const Runs &R, const TapeView &t, uint32_t q,
+                                             uint32_t sub, InRange &&in_range, Body &&body) {
+  const uint32_t off = t.mask_off[q];
+  if (off != MASK_NONE) {
+    MaskWalk m;
+    m.init(R, t.mask_words + off);
+    uint32_t j = 0u, skip = sub;
+    while (true) {
+      bool ok = m.next(R, j);
+      while (ok && skip) {
+        skip--;
+        ok = m.next(R, j);
+      }
+      if (!ok) break;
+      body(j);
+      skip = L - 1;
+    }
+  } else {
+    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
+      if (in_range(j)) body(j);
+    });
   }
 }
 
@@ -361,11 +400,14 @@ template <bool JSIDE>
 __device__ __forceinline__ void force_half(const ForceSide &I, const ForceSide &J,
                                            const PairGeom &g, float3 w, float3 e_close,
                                            const ForceConst &c, ForceAcc &acc) {
+  // every branch of the forward is evaluated and the sums are updated with
+  // selects, so the lanes of a warp stay together through the pair
+  const float3 zero = f3(0.f, 0.f, 0.f);
   const float3 r_ij = JSIDE ? -g.r : g.r;
   const float3 u_ij = JSIDE ? -g.u : g.u;
   const float3 e = g.close ? e_close : -u_ij;
   const float we = dot3(w, e);
-  const float3 dwe = g.close ? f3(0.f, 0.f, 0.f) : (w - e * we) * (-g.inv_rr);
+  const float3 dwe = g.close ? zero : (w - e * we) * (-g.inv_rr);
   // near pressure: alpha G e
   const float Pn_i = c.near_k * I.rnb, Pn_j = c.near_k * J.rnb;
   const float inv2 = 1.0f / (2.0f * I.rb * J.rnb);
@@ -373,38 +415,38 @@ __device__ __forceinline__ void force_half(const ForceSide &I, const ForceSide &
   float3 g_r = (u_ij * (g.Gp * we) + dwe * g.G) * alpha;
   const float Gwe = g.G * we;
   if (!JSIDE) {
-    if (I.m) acc.grho += (-alpha / I.rb) * Gwe;
-    if (I.mn) acc.grhon += (-c.mass * c.near_k * inv2) * Gwe;
+    acc.grho += I.m ? (-alpha / I.rb) * Gwe : 0.0f;
+    acc.grhon += I.mn ? (-c.mass * c.near_k * inv2) * Gwe : 0.0f;
   } else {
-    if (J.mn) acc.grhon += (c.mass * Pn_i * inv2 / J.rnb) * Gwe;
+    acc.grhon += J.mn ? (c.mass * Pn_i * inv2 / J.rnb) * Gwe : 0.0f;
   }
   // separation (close pairs): -200 (1 - r / min_dist) e
-  if (g.close) g_r = g_r + u_ij * (c.sep_k * we);
+  g_r = g_r + (g.close ? u_ij * (c.sep_k * we) : zero);
   // viscosity where v_ij . x_ij < 0: beta G e, beta = m visc h vdx / (D avg)
   const float3 vij = I.vhat - J.vpre;
   const float vdx = dot3(vij, r_ij);
-  if (vdx < 0.0f) {
-    const float avg = (I.rb + J.rb) * 0.5f;
-    const float inv_Davg = 1.0f / (g.D * avg);
-    const float bG = c.mass * c.h * vdx * inv_Davg;
-    const float beta = c.visc * bG * g.G;
-    const float dbdv = c.visc * c.mass * c.h * g.G * inv_Davg;
-    g_r = g_r + (vij * dbdv + u_ij * (c.visc * bG * g.Gp) - r_ij * (2.0f * beta / g.D)) * we +
-          dwe * beta;
-    const float drho = -beta / (2.0f * avg) * we;
-    if (!JSIDE) {
-      acc.gvh = acc.gvh + r_ij * (we * dbdv);
-      if (I.m) acc.grho += drho;
-      acc.sv += bG * Gwe;
-    } else {
-      acc.gv = acc.gv + r_ij * (-we * dbdv);
-      if (J.m) acc.grho += drho;
-    }
+  const bool vis = vdx < 0.0f;
+  const float avg = (I.rb + J.rb) * 0.5f;
+  const float inv_Davg = 1.0f / (g.D * avg);
+  const float bG = c.mass * c.h * vdx * inv_Davg;
+  const float beta = c.visc * bG * g.G;
+  const float dbdv = c.visc * c.mass * c.h * g.G * inv_Davg;
+  const float3 g_vis = (vij * dbdv + u_ij * (c.visc * bG * g.Gp) - r_ij * (2.0f * beta / g.D)) * we +
+                       dwe * beta;
+  g_r = g_r + (vis ? g_vis : zero);
+  const float drho = -beta / (2.0f * avg) * we;
+  if (!JSIDE) {
+    acc.gvh = acc.gvh + (vis ? r_ij * (we * dbdv) : zero);
+    acc.grho += (vis && I.m) ? drho : 0.0f;
+    acc.sv += vis ? bG * Gwe : 0.0f;
+  } else {
+    acc.gv = acc.gv + (vis ? r_ij * (-we * dbdv) : zero);
+    acc.grho += (vis && J.m) ? drho : 0.0f;
   }
   // cohesion, scaled by st: m K C e - m K (n_i - n_j)
   const float3 wc = w * c.st;
   const float wce = dot3(wc, e);
-  const float3 dwce = g.close ? f3(0.f, 0.f, 0.f) : (wc - e * wce) * (-g.inv_rr);
+  const float3 dwce = g.close ? zero : (wc - e * wce) * (-g.inv_rr);
   const float rs = I.rb + J.rb;
   const float Kij = 2.0f * c.rho0 / rs;
   const float mK = c.mass * Kij;
@@ -413,12 +455,12 @@ __device__ __forceinline__ void force_half(const ForceSide &I, const ForceSide &
   const float dKterm = (-Kij / rs) * (c.mass * g.C * wce - c.mass * dot3(wc, nij));
   if (!JSIDE) {
     acc.gn = acc.gn + wc * (-mK);
-    if (I.m) acc.grho += dKterm;
+    acc.grho += I.m ? dKterm : 0.0f;
     acc.ss += mK * g.C * we - mK * dot3(w, nij);
     acc.gx = acc.gx + g_r;
   } else {
     acc.gn = acc.gn + wc * mK;
-    if (J.m) acc.grho += dKterm;
+    acc.grho += J.m ? dKterm : 0.0f;
     acc.gx = acc.gx - g_r;
   }
 }
@@ -430,9 +472,9 @@ __device__ __forceinline__ float3 close_dir(const float4 *dir_tab, int dir_half,
   return fallback_dir_eval(float(si - s_off) - float(sj - s_off));
 }
 
-__device__ __forceinline__ ForceSide force_side(const TapeView &t, uint32_t i) {
+__device__ __forceinline__ ForceSide force_side(const TapeView &t, uint32_t i, float3 x) {
   ForceSide S;
-  S.x = f3of(__ldg(t.pos + i));
+  S.x = x;
   S.vhat = f3of(__ldg(t.vhat + i));
   S.vpre = f3of(__ldg(t.vel + i));
   S.n = f3of(__ldg(t.nrm + i));
@@ -458,23 +500,32 @@ __device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const Sc
     const DevUniforms *U = v.u + scene;
     const ForceConst c = force_const(U->sph);
     const float h2 = U->sph.kernel_radius_sq;
-    const ForceSide Q = force_side(t, q);
+    const ForceSide Q = force_side(t, q, f3of(t.pos[q]));
     const float3 wq = f3of(a.ga[q]);
     Runs R;
     flag_outside(a.err, runs_checked(Q.x, U->grid, t.cell_begin + U->c_offset, R));
-    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
-      const float3 xj = f3of(__ldg(t.pos + j));
-      const float3 r = Q.x - xj;
-      const float r2 = dot3(r, r);
-      if (!(r2 < h2 && r2 > MIN_R2)) return;
-      const ForceSide Jn = force_side(t, j);
-      const PairGeom g = pair_geom(r, r2, c);
-      const float3 wj = f3of(__ldg(a.ga + j));
-      const float3 ec_qj = g.close ? close_dir(dir_tab, dir_half, q, j, U->s_offset) : f3(0.f, 0.f, 0.f);
-      const float3 ec_jq = g.close ? close_dir(dir_tab, dir_half, j, q, U->s_offset) : f3(0.f, 0.f, 0.f);
-      force_half<false>(Q, Jn, g, wq, ec_qj, c, acc);
-      force_half<true>(Jn, Q, g, wj, ec_jq, c, acc);
-    });
+    for_hits_sub<L>(
+        R, t, q, sub,
+        [&](uint32_t j) {
+          const float3 r = Q.x - f3of(__ldg(t.pos + j));
+          const float r2 = dot3(r, r);
+          return r2 < h2 && r2 > MIN_R2;
+        },
+        [&](uint32_t j) {
+          const float3 xj = f3of(__ldg(t.pos + j));
+          const float3 r = Q.x - xj;
+          const float r2 = dot3(r, r);
+          const ForceSide Jn = force_side(t, j, xj);
+          const PairGeom g = pair_geom(r, r2, c);
+          const float3 wj = f3of(__ldg(a.ga + j));
+          float3 ec_qj = f3(0.f, 0.f, 0.f), ec_jq = f3(0.f, 0.f, 0.f);
+          if (g.close) {
+            ec_qj = close_dir(dir_tab, dir_half, q, j, U->s_offset);
+            ec_jq = close_dir(dir_tab, dir_half, j, q, U->s_offset);
+          }
+          force_half<false>(Q, Jn, g, wq, ec_qj, c, acc);
+          force_half<true>(Jn, Q, g, wj, ec_jq, c, acc);
+        });
   }
   acc.sv = group_sum<L>(acc.sv);
   acc.ss = group_sum<L>(acc.ss);
@@ -527,11 +578,15 @@ __device__ __forceinline__ void adj_xsph_one(uint32_t q, uint32_t sub, const Sce
     const float grho_k = rho_q > 1.0f ? -eps * mass / (rb_q * rb_q) : 0.0f;
     Runs R;
     flag_outside(a.err, runs_checked(xq, U->grid, t.cell_begin + U->c_offset, R));
-    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
+    auto in_range = [&](uint32_t j) {
+      const float3 r = xq - f3of(__ldg(t.pos + j));
+      const float r2 = dot3(r, r);
+      return r2 < h2 && r2 > MIN_R2;
+    };
+    for_hits_sub<L>(R, t, q, sub, in_range, [&](uint32_t j) {
       const float3 xj = f3of(__ldg(t.pos + j));
       const float3 r = xq - xj;  // r_qj
       const float r2 = dot3(r, r);
-      if (!(r2 < h2 && r2 > MIN_R2)) return;
       const float diff = h2 - r2;
       const float W = scale_d * diff * diff * diff;
       const float dWs = -6.0f * scale_d * diff * diff;  // dW/dr = dWs * r
@@ -610,11 +665,15 @@ __device__ __forceinline__ void adj_density_one(uint32_t q, uint32_t sub, const 
     const float3 nq = f3of(a.gn[q]);
     Runs R;
     flag_outside(a.err, runs_checked(xq, U->grid, t.cell_begin + U->c_offset, R));
-    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
+    auto in_range = [&](uint32_t j) {
+      const float3 r = xq - f3of(__ldg(t.pos + j));
+      const float r2 = dot3(r, r);
+      return r2 < h2 && r2 > MIN_R2;
+    };
+    for_hits_sub<L>(R, t, q, sub, in_range, [&](uint32_t j) {
       const float3 xj = f3of(__ldg(t.pos + j));
       const float3 r = xq - xj;  // r_qj; the pair (j, q) has r_jq = -r
       const float r2 = dot3(r, r);
-      if (!(r2 < h2 && r2 > MIN_R2)) return;
       const float2 gj = __ldg(a.grho + j);
       const float3 nj = f3of(__ldg(a.gn + j));
       const float diff = h2 - r2;
@@ -840,14 +899,19 @@ cudaError_t adj_gathers(const SceneView &v, const TapeView &t, const AdjView &a,
     b.density = resident_blocks(k_adj_density<L>, sm_count);
   }
   const uint32_t nwarps = (n + 31u) / 32u;
+  // the solve levels test their candidates (predicted positions) and take
+  // the recorded warp order; the mask walks take the hit-sorted slots
   auto queue = [&](int slot) { return TaskQueue{t.order, a.counters + slot, n, nwarps, false}; };
+  auto hit_queue = [&](int slot) {
+    return TaskQueue{t.perm_hit, a.counters + slot, n, nwarps, true};
+  };
   for (int k = K - 1; k >= 0; k--)
     k_adj_solve<L><<<b.solve, 128, 0, st>>>(queue(k), v, t, a, t.xp[k], t.rho[k],
                                             k >= 1 ? t.ap[k - 1] : nullptr, a.gu[k & 1],
                                             a.gu[(k + 1) & 1], k, K);
-  k_adj_force<L><<<b.force, 128, 0, st>>>(queue(K), v, t, a, dir_tab, dir_half);
-  k_adj_xsph<L><<<b.xsph, 128, 0, st>>>(queue(K + 1), v, t, a);
-  k_adj_density<L><<<b.density, 128, 0, st>>>(queue(K + 2), v, t, a);
+  k_adj_force<L><<<b.force, 128, 0, st>>>(hit_queue(K), v, t, a, dir_tab, dir_half);
+  k_adj_xsph<L><<<b.xsph, 128, 0, st>>>(hit_queue(K + 1), v, t, a);
+  k_adj_density<L><<<b.density, 128, 0, st>>>(hit_queue(K + 2), v, t, a);
   return cudaGetLastError();
 }
 }  // namespace

@@ -34,7 +34,14 @@ struct TapeSlot {
   float *rho[kMaxAdjIters + 1];
   float4 *ap[kMaxAdjIters];
   uint32_t *order;
+  uint32_t *mask_words, *mask_off, *perm_hit;
+  size_t mask_cap;
 };
+
+// Hit-mask words a tape slot holds: 96 per particle on average (3,072
+// candidates) plus a floor; particles beyond the capacity fall back to
+// testing their candidates, in the forward and in the reverse pass alike.
+size_t tape_mask_cap(size_t n) { return 96 * n + (size_t(1) << 16); }
 
 size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -76,6 +83,7 @@ struct FsAdj {
   double *loss = nullptr, *partial = nullptr;
   size_t vox_cap = 0;
   int lanes = 0;  // lanes per particle of the reverse gathers (autotuned)
+  int64_t tape_seg = -1;  // checkpoint segment the tape holds (-1: none)
   uint32_t *scene_first = nullptr, *scene_count = nullptr;  // device, canonical ranges
 };
 
@@ -113,6 +121,10 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
     }
     for (uint32_t k = 0; k < a->K; k++) t.ap[k] = c.take<float4>(N);
     t.order = c.take<uint32_t>((N + 31) / 32);
+    t.mask_cap = tape_mask_cap(N);
+    t.mask_words = c.take<uint32_t>(t.mask_cap);
+    t.mask_off = c.take<uint32_t>(N);
+    t.perm_hit = c.take<uint32_t>(N);
   }
   AdjView &v = a->av;
   v.gx = c.take<float4>(N);
@@ -175,6 +187,10 @@ DevState recording_state(const FsAdj *a, const TapeSlot &t) {
   dv.rec_rho = t.rho;
   dv.rec_ap = t.ap;
   dv.warp_order = t.order;
+  dv.mask_words = t.mask_words;
+  dv.mask_off = t.mask_off;
+  dv.mask_cap = t.mask_cap;
+  dv.perm_hit = t.perm_hit;
   return dv;
 }
 
@@ -196,6 +212,9 @@ TapeView tape_view(const TapeSlot &t, uint32_t K) {
   }
   for (uint32_t k = 0; k < K; k++) v.ap[k] = t.ap[k];
   v.order = t.order;
+  v.mask_words = t.mask_words;
+  v.mask_off = t.mask_off;
+  v.perm_hit = t.perm_hit;
   return v;
 }
 
@@ -345,11 +364,22 @@ int fs_adj_forward(FsAdj *a, uint32_t nsteps) {
     FS_CUDA(cudaMalloc(&a->final_state, sizeof(float4) * 2 * std::max<size_t>(a->N, 1)),
             "allocate final state");
   if ((rc = ensure_work(a))) return rc;
+  a->tape_seg = -1;
   for (uint32_t c = 0; c < nck; c++) {
     float4 *ck = a->ck + size_t(c) * 2 * a->N;
     if ((rc = copy_state(s, ck, ck + a->N, s->d.p_pos, s->d.p_vel, a->N))) return rc;
     const uint32_t len = std::min(a->every, nsteps - c * a->every);
-    if ((rc = fs_step(s, len))) return rc;
+    if (c + 1 < nck) {
+      if ((rc = fs_step(s, len))) return rc;
+    } else {
+      // the reverse pass starts with the last segment: record its tape now
+      // instead of re-running it there
+      for (uint32_t t = 0; t < len; t++) {
+        const DevState dv = recording_state(a, a->tape[t]);
+        if ((rc = enqueue_step(s, false, &dv))) return rc;
+      }
+      a->tape_seg = int64_t(c);
+    }
   }
   if ((rc = copy_state(s, a->final_state, a->final_state + a->N, s->d.p_pos, s->d.p_vel, a->N)))
     return rc;
@@ -514,12 +544,17 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
   const uint32_t nck = (a->steps + a->every - 1) / a->every;
   const SceneView base = s->d.view();
   for (uint32_t seg = nck; seg-- > 0;) {
-    const float4 *ck = a->ck + size_t(seg) * 2 * N;
-    if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, ck, ck + N, N))) return rc;
     const uint32_t len = std::min(a->every, a->steps - seg * a->every);
-    for (uint32_t t = 0; t < len; t++) {
-      const DevState dv = recording_state(a, a->tape[t]);
-      if ((rc = enqueue_step(s, false, &dv))) return rc;
+    if (a->tape_seg != int64_t(seg)) {
+      // restore the segment's checkpoint and re-run it, recording
+      a->tape_seg = -1;
+      const float4 *ck = a->ck + size_t(seg) * 2 * N;
+      if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, ck, ck + N, N))) return rc;
+      for (uint32_t t = 0; t < len; t++) {
+        const DevState dv = recording_state(a, a->tape[t]);
+        if ((rc = enqueue_step(s, false, &dv))) return rc;
+      }
+      a->tape_seg = int64_t(seg);
     }
     for (uint32_t t = len; t-- > 0;) {
       const TapeSlot &slot = a->tape[t];

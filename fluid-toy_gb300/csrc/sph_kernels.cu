@@ -53,7 +53,6 @@ __device__ __forceinline__ void for_each_hit(const Runs &R, Test &&test, Body &&
 // the shaders' order, so a warp runs as long as its busiest lane (not as long
 // as the union of its lanes' candidate positions), and no candidate is tested
 // twice.
-constexpr uint32_t MASK_NONE = 0xffffffffu;
 
 // Word offset of each particle's mask, allocated per warp from a bump counter.
 // Particles that do not fit the capacity get MASK_NONE and use the tested
@@ -76,50 +75,6 @@ __device__ __forceinline__ uint32_t alloc_mask(bool active, uint32_t nwords,
   if (!active || off + nwords > capacity || off >= MASK_NONE) return MASK_NONE;
   return uint32_t(off);
 }
-
-// Cursor over a particle's mask: next() yields the hit slots in visiting
-// order, skipping empty words inside the call, so lanes progress
-// independently (one hit per call).
-struct MaskWalk {
-  const uint32_t *words;
-  uint32_t nwords;    // words of the particle
-  uint32_t w;         // index of the word held in `nxt`
-  uint32_t cur;       // bits left of the current word
-  uint32_t nxt;       // word w, loaded one ahead to hide its latency
-  uint32_t wbase;     // slot of bit 0 of the current word
-  uint32_t row_wend;  // first word index past the current run
-  int row;
-
-  __device__ __forceinline__ void init(const Runs &R, const uint32_t *wds) {
-    words = wds;
-    nwords = R.words;
-    w = 0u;
-    cur = 0u;
-    nxt = nwords ? wds[0] : 0u;
-    wbase = 0u;
-    row_wend = 0u;
-    row = -1;
-  }
-  __device__ __forceinline__ bool next(const Runs &R, uint32_t &j) {
-    while (cur == 0u) {
-      if (w == nwords) return false;
-      // runs shorter than one candidate own no word; w < nwords guarantees a
-      // later run that owns word w
-      while (w == row_wend) {
-        row++;
-        row_wend += (R.hi[row] - R.lo[row] + 31u) >> 5;
-        wbase = R.lo[row] - 32u;  // modulo 2^32: the += 32 below restores lo
-      }
-      wbase += 32u;
-      cur = nxt;
-      w++;
-      nxt = w < nwords ? words[w] : 0u;
-    }
-    j = wbase + uint32_t(__ffs(cur) - 1);
-    cur &= cur - 1u;
-    return true;
-  }
-};
 
 template <class Body>
 __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, Body &&body) {
@@ -333,6 +288,8 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
 }
 
 // ---- force + PCISPH predict ---------------------------------------------------
+// Two hits per walk iteration: their terms are computed side by side.
+constexpr bool kForceHitPairs = true;
 // sph_force_3d_grid.wgsl:105-227, then pcisph_predict.wgsl:61-72 for the same
 // particle (sorted order).
 __device__ __forceinline__ void force_predict_one(
@@ -366,20 +323,32 @@ __device__ __forceinline__ void force_predict_one(
   // Every arm of the shader's branches is evaluated and the accumulators are
   // updated with selects (x = c ? x + t : x), which leaves their bits exactly
   // as the branches would: lanes of a warp then never split inside the body.
+  // Each hit's terms are computed first (they depend on the hit only) and
+  // then added in the shader's order, so the terms of consecutive hits can
+  // overlap while the sums keep their order.
   struct Rec {
     float4 p, v, n;
+  };
+  struct Terms {
+    float3 p;    // near-pressure term
+    float3 sep;  // close-pair separation term
+    float3 v;    // viscosity term
+    float3 c1;   // cohesion term
+    float3 c2;   // normal-difference term
+    bool close, visc;
   };
   auto load = [&](uint32_t j) {
     return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j), __ldg(nb_nrm + j)};
   };
-  auto body = [&](uint32_t j, const Rec &q) {
+  auto terms = [&](uint32_t j, const Rec &q) {
+    Terms t;
     const float3 pos_j = xyz(q.p);
     const float3 vel_j = xyz(q.v);
     const float3 n_j = xyz(q.n);
     const float3 r_vec = pos_i - pos_j;
     const float r_sq = dot3(r_vec, r_vec);
     const float rr = sqrtf(r_sq);
-    const bool close = rr < min_dist;
+    t.close = rr < min_dist;
     // normalize(pos_j - pos_i): its length is sqrt(dot(-r, -r)) == rr bit for
     // bit, so dividing by rr is the same operation sequence
     // (pos_j - pos_i) / rr with one shared reciprocal, bit-identical
@@ -390,40 +359,64 @@ __device__ __forceinline__ void force_predict_one(
     const int d = int(s) - int(j);
     const bool tabulated = d >= -dir_half && d <= dir_half;
     float3 dir_close = dir_far;
-    if (close && tabulated) dir_close = xyz(__ldg(dir_tab + (d + dir_half)));
-    if (close && !tabulated)
+    if (t.close && tabulated) dir_close = xyz(__ldg(dir_tab + (d + dir_half)));
+    if (t.close && !tabulated)
       dir_close = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
-    const float3 dir = close ? dir_close : dir_far;
+    const float3 dir = t.close ? dir_close : dir_far;
     const float density_j = q.p.w;       // max(density_j, 1)
     const float near_density_j = q.n.w;  // max(near density_j, 1)
     const float near_pressure_j = near_k * near_density_j;
     const float dg = h - rr;
     const float grad = scale_g * dg * dg;
-    a_p = a_p + (-mass * (near_pressure_i + near_pressure_j) /
-                 (2.0f * density_i * near_density_j)) * dir * grad;
+    t.p = (-mass * (near_pressure_i + near_pressure_j) /
+           (2.0f * density_i * near_density_j)) * dir * grad;
     const float sep = 200.0f * (1.0f - div_by_rcp(rr, min_dist, y_min_dist));
-    const float3 a_p_sep = a_p + (-sep) * dir;
-    a_p = close ? a_p_sep : a_p;
+    t.sep = (-sep) * dir;
     const float3 v_ij = vel_i - vel_j;
     const float v_dot_x = dot3(v_ij, r_vec);
     const float mu = h * v_dot_x / (r_sq + 0.01f * h2);
     const float avg_density = (density_i + density_j) * 0.5f;
     const float pi_visc = -visc * mu / avg_density;
-    const float3 a_v_new = a_v + (-mass * pi_visc * grad) * dir;
-    a_v = v_dot_x < 0.0f ? a_v_new : a_v;
+    t.v = (-mass * pi_visc * grad) * dir;
+    t.visc = v_dot_x < 0.0f;
     const float K_ij = 2.0f * rho0 / (density_i + density_j);
     const float r3 = rr * rr * rr;
     const float coh_far = scale_c * dg * dg * dg * r3;
     const float coh_near = scale_c * (2.0f * dg * dg * dg * r3 - P.kernel_radius_pow6 / 64.0f);
     const float coh = rr >= h * 0.5f ? coh_far : coh_near;
-    a_c = a_c + (mass * K_ij * coh) * dir;
-    a_c = a_c - (mass * K_ij) * (n_i - n_j);
+    t.c1 = (mass * K_ij * coh) * dir;
+    t.c2 = (mass * K_ij) * (n_i - n_j);
+    return t;
   };
+  auto add = [&](const Terms &t) {
+    a_p = a_p + t.p;
+    const float3 a_p_sep = a_p + t.sep;
+    a_p = t.close ? a_p_sep : a_p;
+    const float3 a_v_new = a_v + t.v;
+    a_v = t.visc ? a_v_new : a_v;
+    a_c = a_c + t.c1;
+    a_c = a_c - t.c2;
+  };
+  auto body = [&](uint32_t j) { add(terms(j, load(j))); };
   const uint32_t off = mask_off[s];
   if (off != MASK_NONE) {
-    // the loads are not pipelined here: the body is long enough to cover
-    // them, and the ring's registers would cost occupancy
-    walk_mask(R, mask_words + off, [&](uint32_t j) { body(j, load(j)); });
+    if (kForceHitPairs) {
+      MaskWalk m;
+      m.init(R, mask_words + off);
+      uint32_t j0, j1;
+      while (m.next(R, j0)) {
+        if (!m.next(R, j1)) {
+          body(j0);
+          break;
+        }
+        const Terms t0 = terms(j0, load(j0));
+        const Terms t1 = terms(j1, load(j1));
+        add(t0);
+        add(t1);
+      }
+    } else {
+      walk_mask(R, mask_words + off, body);
+    }
   } else {
     for_each_hit(
         R,
@@ -433,7 +426,7 @@ __device__ __forceinline__ void force_predict_one(
           const float r_sq = rx * rx + ry * ry + rz * rz;
           return r_sq < h2 && r_sq > 1e-12f;
         },
-        [&](uint32_t j) { body(j, load(j)); });
+        body);
   }
   a_c = a_c * P.surface_tension;
   const float3 a_g = xyz(U->gravity.direction);
