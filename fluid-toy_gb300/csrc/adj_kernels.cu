@@ -113,11 +113,12 @@ __device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
 // candidates. Lane `sub` of q's L lanes takes every L-th hit.
 template <int L, class InRange, class Body>
 __device__ __forceinline__ void for_hits_sub(const Runs &R, const TapeView &t, uint32_t q,
-                                             uint32_t sub, InRange &&in_range, Body &&body) {
+                                             uint32_t sub, InRange &&in_range, Body &&body,
+                                             const uint32_t *words = nullptr) {
   const uint32_t off = t.mask_off[q];
   if (off != MASK_NONE) {
     MaskWalk m;
-    m.init(R, t.mask_words + off);
+    m.init(R, (words ? words : t.mask_words) + off);
     uint32_t j = 0u, skip = sub;
     while (true) {
       bool ok = m.next(R, j);
@@ -269,33 +270,44 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
     Runs R;
     flag_outside(a.err, runs_checked(f3of(t.pos[q]), U->grid, t.cell_begin + U->c_offset, R));
     const float c_rho = -6.0f * mass * scale_d;
-    for_candidates_sub<L>(R, sub, [&](uint32_t j) {
-      const float4 xj4 = __ldg(xpk + j);
-      const float3 r = xq - f3of(xj4);
-      const float r2 = dot3(r, r);
-      if (!(r2 < h2)) return;
-      const float4 uj4 = __ldg(gu_in + j);
-      if (has_rho) {
-        const float diff = h2 - r2;
-        xsb = mad3(xsb, c_rho * diff * diff * (rhat_q + uj4.w), r);
-      }
-      if (has_p && r2 > MIN_R2) {
-        const float rt_j = fmaxf(__ldg(rhok + j), 1.0f);
-        const float cij = cq + xj4.w / (rt_j * rt_j);
-        const float rr = sqrtf(r2);
-        const float inv_rr = 1.0f / rr;
-        const float3 e = r * inv_rr;
-        const float dg = h - rr;
-        const float g = scale_g * dg * dg;
-        const float gp = -2.0f * scale_g * dg;
-        const float3 du = uq - f3of(uj4);
-        const float edu = dot3(e, du);
-        // J du = g' (e.du) e + (g / r)(du - (e.du) e)
-        const float3 Jdu = e * (gp * edu) + (du - e * edu) * (g * inv_rr);
-        xsb = mad3(xsb, mass * cij, Jdu);
-        phisum += mass * g * edu;
-      }
-    });
+    // the level's in-range pairs (r^2 < h^2 at the predicted positions),
+    // walked from the mask the forward iteration recorded
+    for_hits_sub<L>(
+        R, t, q, sub,
+        [&](uint32_t j) {
+          const float3 r = xq - f3of(__ldg(xpk + j));
+          return dot3(r, r) < h2;
+        },
+        [&](uint32_t j) {
+          const float4 xj4 = __ldg(xpk + j);
+          const float3 r = xq - f3of(xj4);
+          const float r2 = dot3(r, r);
+          const float4 uj4 = __ldg(gu_in + j);
+          if (has_rho) {
+            const float diff = h2 - r2;
+            xsb = mad3(xsb, c_rho * diff * diff * (rhat_q + uj4.w), r);
+          }
+          if (has_p) {
+            // evaluated for every hit, kept for r^2 > 1e-12 (selects keep the
+            // lanes together)
+            const bool ns = r2 > MIN_R2;
+            const float rt_j = fmaxf(__ldg(rhok + j), 1.0f);
+            const float cij = cq + xj4.w / (rt_j * rt_j);
+            const float rr = sqrtf(ns ? r2 : 1.0f);
+            const float inv_rr = 1.0f / rr;
+            const float3 e = r * inv_rr;
+            const float dg = h - rr;
+            const float g = scale_g * dg * dg;
+            const float gp = -2.0f * scale_g * dg;
+            const float3 du = uq - f3of(uj4);
+            const float edu = dot3(e, du);
+            // J du = g' (e.du) e + (g / r)(du - (e.du) e)
+            const float3 Jdu = e * (gp * edu) + (du - e * edu) * (g * inv_rr);
+            xsb = ns ? mad3(xsb, mass * cij, Jdu) : xsb;
+            phisum += ns ? mass * g * edu : 0.0f;
+          }
+        },
+        t.hits[k]);
   }
   xsb = group_sum3<L>(xsb);
   phisum = group_sum<L>(phisum);

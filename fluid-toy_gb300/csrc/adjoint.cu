@@ -35,6 +35,7 @@ struct TapeSlot {
   float4 *ap[kMaxAdjIters];
   uint32_t *order;
   uint32_t *mask_words, *mask_off, *perm_hit;
+  uint32_t *hits[kMaxAdjIters];  // per PCISPH level, same layout as mask_words
   size_t mask_cap;
 };
 
@@ -125,6 +126,7 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
     t.mask_words = c.take<uint32_t>(t.mask_cap);
     t.mask_off = c.take<uint32_t>(N);
     t.perm_hit = c.take<uint32_t>(N);
+    for (uint32_t k = 0; k < a->K; k++) t.hits[k] = c.take<uint32_t>(t.mask_cap);
   }
   AdjView &v = a->av;
   v.gx = c.take<float4>(N);
@@ -191,6 +193,7 @@ DevState recording_state(const FsAdj *a, const TapeSlot &t) {
   dv.mask_off = t.mask_off;
   dv.mask_cap = t.mask_cap;
   dv.perm_hit = t.perm_hit;
+  dv.rec_hits = t.hits;
   return dv;
 }
 
@@ -215,6 +218,7 @@ TapeView tape_view(const TapeSlot &t, uint32_t K) {
   v.mask_words = t.mask_words;
   v.mask_off = t.mask_off;
   v.perm_hit = t.perm_hit;
+  for (uint32_t k = 0; k < K; k++) v.hits[k] = t.hits[k];
   return v;
 }
 

@@ -450,8 +450,10 @@ __device__ __forceinline__ void force_predict_one(
 // velocity. Each other iteration also writes every particle's pressure term
 // p / max(rho, 1)^2 (the shader's per-neighbour quotient, which depends on
 // the neighbour only), so the next iteration reads it instead of dividing per
-// pair.
-template <bool HAS_PRESSURE, bool LAST>
+// pair. When recording (hit_out), the iteration also writes each particle's
+// in-range candidates (r^2 < h^2 at the predicted positions) as a hit mask in
+// the density mask's layout and offsets (same runs), for the reverse pass.
+template <bool HAS_PRESSURE, bool LAST, bool RECORD>
 __device__ __forceinline__ void solve_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
@@ -459,7 +461,8 @@ __device__ __forceinline__ void solve_one(
             const float *__restrict__ pterm_in, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
-            float4 *__restrict__ ap_out) {
+            float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
+            uint32_t *__restrict__ hit_out) {
   const bool active = s < v.b->n_sorted;
   const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
@@ -493,13 +496,19 @@ __device__ __forceinline__ void solve_one(
       const float grad = scale_g * dg * dg;
       a_p = a_p + (-mass * (self_term + pt) * grad) * dir;
     };
+    uint32_t *hit_words = nullptr;
+    if (RECORD) {
+      const uint32_t off = mask_off[s];
+      hit_words = off == MASK_NONE ? nullptr : hit_out + off;
+    }
+    uint32_t widx = 0u;
     // candidates in chunks of up to 32: the predicted density is summed while
     // testing; the pressure hits of the chunk go to a per-lane bitmask that
     // each lane then walks (its own hits only, ascending)
     for (int r = 0; r < R.count; r++) {
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
-        uint32_t chunk = 0u;
+        uint32_t chunk = 0u, hitw = 0u;
 #pragma unroll 8
         for (uint32_t k = 0; k < cnt; k++) {
           const float4 nb = __ldg(xp_in + base + k);
@@ -510,7 +519,12 @@ __device__ __forceinline__ void solve_one(
             const float diff = h2 - r_sq;
             pred_density += mass * (scale_d * diff * diff * diff);
             if (HAS_PRESSURE && r_sq > 1e-12f) chunk |= 1u << k;
+            if (RECORD) hitw |= 1u << k;
           }
+        }
+        if (RECORD) {
+          if (hit_words) hit_words[widx] = hitw;
+          widx++;
         }
         if (HAS_PRESSURE) {
           while (chunk) {
@@ -715,7 +729,7 @@ __global__ void __launch_bounds__(128, 4)
   });
 }
 
-template <bool HAS_PRESSURE, bool LAST>
+template <bool HAS_PRESSURE, bool LAST, bool RECORD>
 __global__ void __launch_bounds__(128)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
@@ -723,10 +737,12 @@ __global__ void __launch_bounds__(128)
             const float *__restrict__ pterm_in, float4 *__restrict__ xp_out,
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
-            float4 *__restrict__ ap_out) {
+            float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
+            uint32_t *__restrict__ hit_out) {
   for_warp_tasks(q, [&](uint32_t s) {
-    solve_one<HAS_PRESSURE, LAST>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
-                                  rho_out, pterm_out, v_out, stats, ap_out);
+    solve_one<HAS_PRESSURE, LAST, RECORD>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
+                                          rho_out, pterm_out, v_out, stats, ap_out, mask_off,
+                                          hit_out);
   });
 }
 
@@ -1100,21 +1116,29 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   float4 *xp_out = d.rec_xp ? d.rec_xp[iter + 1] : d.pred_xp[out];
   float *rho_out = d.rec_rho ? d.rec_rho[iter + 1] : d.pred_rho[out];
   float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
+  uint32_t *hit_out = d.rec_hits ? d.rec_hits[iter] : nullptr;
   TaskQueue q;
   cudaError_t e = prepare_queue(d, d.warp_order, false, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
-#define FS_SOLVE(P_, L_)                                                                      \
+#define FS_SOLVE(P_, L_, R_)                                                                  \
   do {                                                                                        \
     static unsigned blocks = 0;                                                               \
-    if (!blocks) blocks = persistent_blocks(k_solve<P_, L_>, d.sm_count);                    \
-    k_solve<P_, L_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp, d.cell_begin,    \
-                                            xp_in, d.pterm[in], xp_out, rho_out, d.pterm[out], \
-                                            d.pred_v, d.stats, ap_out);                       \
+    if (!blocks) blocks = persistent_blocks(k_solve<P_, L_, R_>, d.sm_count);                \
+    k_solve<P_, L_, R_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp,          \
+                                                d.cell_begin, xp_in, d.pterm[in], xp_out,     \
+                                                rho_out, d.pterm[out], d.pred_v, d.stats,     \
+                                                ap_out, d.mask_off, hit_out);                 \
   } while (0)
-  if (iter == 0 && last) FS_SOLVE(false, true);
-  else if (iter == 0) FS_SOLVE(false, false);
-  else if (last) FS_SOLVE(true, true);
-  else FS_SOLVE(true, false);
+#define FS_SOLVE_R(P_, L_)            \
+  do {                                \
+    if (hit_out) FS_SOLVE(P_, L_, true); \
+    else FS_SOLVE(P_, L_, false);     \
+  } while (0)
+  if (iter == 0 && last) FS_SOLVE_R(false, true);
+  else if (iter == 0) FS_SOLVE_R(false, false);
+  else if (last) FS_SOLVE_R(true, true);
+  else FS_SOLVE_R(true, false);
+#undef FS_SOLVE_R
 #undef FS_SOLVE
   return cudaGetLastError();
 }
