@@ -911,8 +911,9 @@ cudaError_t adj_gathers(const SceneView &v, const TapeView &t, const AdjView &a,
     b.density = resident_blocks(k_adj_density<L>, sm_count);
   }
   const uint32_t nwarps = (n + 31u) / 32u;
-  // the solve levels test their candidates (predicted positions) and take
-  // the recorded warp order; the mask walks take the hit-sorted slots
+  // the force reverse (long per-hit body) takes the hit-sorted slots, so its
+  // lanes finish together; the others (short bodies) keep the recorded warp
+  // order, whose neighbouring particles share their neighbours' loads in L1
   auto queue = [&](int slot) { return TaskQueue{t.order, a.counters + slot, n, nwarps, false}; };
   auto hit_queue = [&](int slot) {
     return TaskQueue{t.perm_hit, a.counters + slot, n, nwarps, true};
@@ -922,8 +923,8 @@ cudaError_t adj_gathers(const SceneView &v, const TapeView &t, const AdjView &a,
                                             k >= 1 ? t.ap[k - 1] : nullptr, a.gu[k & 1],
                                             a.gu[(k + 1) & 1], k, K);
   k_adj_force<L><<<b.force, 128, 0, st>>>(hit_queue(K), v, t, a, dir_tab, dir_half);
-  k_adj_xsph<L><<<b.xsph, 128, 0, st>>>(hit_queue(K + 1), v, t, a);
-  k_adj_density<L><<<b.density, 128, 0, st>>>(hit_queue(K + 2), v, t, a);
+  k_adj_xsph<L><<<b.xsph, 128, 0, st>>>(queue(K + 1), v, t, a);
+  k_adj_density<L><<<b.density, 128, 0, st>>>(queue(K + 2), v, t, a);
   return cudaGetLastError();
 }
 }  // namespace
