@@ -45,7 +45,7 @@ __device__ __forceinline__ void for_each_hit(const Runs &R, Test &&test, Body &&
 }
 
 // ---- hit masks ----------------------------------------------------------------
-// The heavy per-hit bodies (force, XSPH) run over a per-particle bitmask of
+// The heavy per-hit body (force) runs over a per-particle bitmask of
 // in-range neighbours written by the density pass. Each run's candidates start
 // a new word: bit k of the run's word w is candidate lo + 32w + k, so a run of
 // length L owns ceil(L / 32) words and a particle R.words words in run order.
@@ -82,40 +82,6 @@ __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, 
   m.init(R, words);
   uint32_t j;
   while (m.next(R, j)) body(j);
-}
-
-// The walk with a ring of D hits in flight: slot i holds hit k and, once
-// its body has run, is refilled with hit k + D, so the gathers of the next
-// D - 1 hits overlap each body. Hits are processed in visiting order.
-template <int D, class Load, class Body>
-__device__ __forceinline__ void walk_mask_ring(const Runs &R, const uint32_t *words, Load &&load,
-                                               Body &&body) {
-  MaskWalk m;
-  m.init(R, words);
-  uint32_t jq[D];
-  bool vq[D];
-  using Rec = decltype(load(0u));
-  Rec rq[D];
-#pragma unroll
-  for (int i = 0; i < D; i++) {
-    vq[i] = m.next(R, jq[i]);
-    rq[i] = vq[i] ? load(jq[i]) : Rec{};
-  }
-  bool more = vq[0];
-  while (more) {
-#pragma unroll
-    for (int i = 0; i < D; i++) {
-      if (more) {
-        if (!vq[i]) {
-          more = false;
-        } else {
-          body(jq[i], rq[i]);
-          vq[i] = m.next(R, jq[i]);
-          if (vq[i]) rq[i] = load(jq[i]);
-        }
-      }
-    }
-  }
 }
 
 // Per-particle neighbour records, written by the density pass for the later
@@ -232,14 +198,16 @@ __device__ __forceinline__ void density_one(
 // ---- XSPH -------------------------------------------------------------------
 // xsph.wgsl:81-138; the result is the post-XSPH velocity in sorted order (the
 // reference scatters it to the canonical array). mass / density_j comes from
-// the neighbour record (the same quotient, evaluated once per particle).
+// the neighbour record (the same quotient, evaluated once per particle). The
+// per-neighbour body is short, so every candidate is tested in a branch-free
+// loop (the term is added where 1e-12 < r^2 < h^2, in the shader's order):
+// faster here than walking the hit mask, whose per-hit cost is the walk and
+// two dependent gathers.
 __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
                                               const float4 *__restrict__ s_vel,
                                               const float4 *__restrict__ nb_pos,
                                               const float4 *__restrict__ nb_vel,
                                               const uint32_t *__restrict__ begin,
-                                              const uint32_t *__restrict__ mask_words,
-                                              const uint32_t *__restrict__ mask_off,
                                               float4 *__restrict__ vel_x) {
   if (s >= v.b->n_sorted) return;
   const DevUniforms *U = v.u + v.scene_of_slot[s];
@@ -257,38 +225,27 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
   Runs R;
   neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   float3 corr = f3(0.f, 0.f, 0.f);
-  struct Rec {
-    float4 p, v;
-  };
-  auto dist2 = [&](float4 pj) {
-    const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
-    return rx * rx + ry * ry + rz * rz;
-  };
-  auto body = [&](uint32_t, const Rec &q) {
-    const float r_sq = dist2(q.p);
-    const float diff = h2 - r_sq;
-    const float w = scale_d * diff * diff * diff;
-    corr = corr + q.v.w * (xyz(q.v) - vel_i) * w;
-  };
-  auto load = [&](uint32_t j) { return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j)}; };
-  const uint32_t off = mask_off[s];
-  if (off != MASK_NONE) {
-    walk_mask_ring<3>(R, mask_words + off, load, body);
-  } else {
-    for_each_hit(
-        R,
-        [&](uint32_t j) {
-          const float r_sq = dist2(__ldg(nb_pos + j));
-          return r_sq < h2 && r_sq > 1e-12f;
-        },
-        [&](uint32_t j) { body(j, load(j)); });
+  for (int r = 0; r < R.count; r++) {
+#pragma unroll 8
+    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
+      const float4 pj = __ldg(nb_pos + j);
+      const float4 vj = __ldg(nb_vel + j);
+      const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+      const float r_sq = rx * rx + ry * ry + rz * rz;
+      const bool hit = r_sq < h2 && r_sq > 1e-12f;
+      const float diff = h2 - r_sq;
+      const float w = scale_d * diff * diff * diff;
+      const float3 c = corr + vj.w * (xyz(vj) - vel_i) * w;
+      corr = hit ? c : corr;
+    }
   }
   const float3 vn = vel_i + eps * corr;
   vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
 }
 
 // ---- force + PCISPH predict ---------------------------------------------------
-// Two hits per walk iteration: their terms are computed side by side.
+// Two hits per walk iteration: their terms are computed side by side (three
+// measured no faster).
 constexpr bool kForceHitPairs = true;
 // sph_force_3d_grid.wgsl:105-227, then pcisph_predict.wgsl:61-72 for the same
 // particle (sorted order).
@@ -569,12 +526,12 @@ __device__ __forceinline__ void solve_one(
 // The neighbour passes' cost per particle ranges over two orders of
 // magnitude (the clumps carry most of the pairs). Persistent warps take
 // 32-slot tasks from a queue ordered heaviest first (longest-processing-time
-// scheduling). Density and solve, which test every candidate, take warps of
-// 32 consecutive sorted slots (neighbouring particles share their
-// neighbours' loads in L1); the mask walks (XSPH, force), whose lanes run as
-// many iterations as they have hits, take 32 slots of similar hit count from
-// a permutation built by a counting sort on a log-linear work key, so their
-// lanes finish together. Which lane computes a particle does not
+// scheduling). Density, XSPH and solve, which test every candidate, take
+// warps of 32 consecutive sorted slots (neighbouring particles share their
+// neighbours' loads in L1); the force pass, which walks the hit mask (its
+// lanes run as many iterations as they have hits), takes 32 slots of similar
+// hit count from a permutation built by a counting sort on a log-linear work
+// key, so its lanes finish together. Which lane computes a particle does not
 // change its result.
 __device__ __forceinline__ uint32_t work_key(uint32_t c) {
   return c < 4096u ? c : 4096u + min((c - 4096u) >> 4, 4095u);
@@ -707,11 +664,8 @@ __global__ void __launch_bounds__(128)
 __global__ void __launch_bounds__(128)
     k_xsph(TaskQueue q, SceneView v, const float4 *__restrict__ s_vel,
            const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
-           const uint32_t *__restrict__ begin, const uint32_t *__restrict__ mask_words,
-           const uint32_t *__restrict__ mask_off, float4 *__restrict__ vel_x) {
-  for_warp_tasks(q, [&](uint32_t s) {
-    xsph_one(s, v, s_vel, nb_pos, nb_vel, begin, mask_words, mask_off, vel_x);
-  });
+           const uint32_t *__restrict__ begin, float4 *__restrict__ vel_x) {
+  for_warp_tasks(q, [&](uint32_t s) { xsph_one(s, v, s_vel, nb_pos, nb_vel, begin, vel_x); });
 }
 
 __global__ void __launch_bounds__(128, 4)
@@ -1083,12 +1037,11 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
 cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   TaskQueue q;
-  cudaError_t e = prepare_queue(d, d.perm_hit, true, n, 0, st, &q);
+  cudaError_t e = prepare_queue(d, d.warp_order, false, n, 0, st, &q);
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
   if (!blocks) blocks = persistent_blocks(k_xsph, d.sm_count);
-  k_xsph<<<blocks, 128, 0, st>>>(q, d.view(), d.s_vel, d.nb_pos, d.nb_vel, d.cell_begin,
-                                 d.mask_words, d.mask_off, d.vel_x);
+  k_xsph<<<blocks, 128, 0, st>>>(q, d.view(), d.s_vel, d.nb_pos, d.nb_vel, d.cell_begin, d.vel_x);
   return cudaGetLastError();
 }
 

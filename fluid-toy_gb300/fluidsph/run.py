@@ -1,10 +1,17 @@
 """Headless runner: step one of the seeded workloads through the C ABI.
 
     python fluid-toy_gb300/fluidsph/run.py --config 1 --steps 12 [--graph]
+    python fluid-toy_gb300/fluidsph/run.py --identify --iterations 2
 
 Each step is one fs_step(sim, 1) call (one launch per kernel, the form that
 profilers can address launch by launch) unless --graph replays them as one
 captured graph. Prints the particle count, steps and wall time.
+
+--identify runs the batched parameter-identification workload instead (the
+64 scenes of scenes.config4 as one batch, 150 steps, checkpoint every 15):
+per iteration a DifferentiableRollout forward, an MSE splat loss per scene
+against zero targets and the backward, inside NVTX ranges named fwd<i> and
+bwd<i> (when torch is importable) so a profiler can select one phase.
 """
 from __future__ import annotations
 
@@ -20,13 +27,81 @@ from fluidsph import scenes  # noqa: E402
 from fluidsph.sim import SphSimulation3DGrid  # noqa: E402
 
 
+class _Ranges:
+    """NVTX push/pop through torch when available, else no-ops."""
+
+    def __init__(self):
+        try:
+            import torch
+            self._nvtx = torch.cuda.nvtx
+        except Exception:  # torch absent: no ranges
+            self._nvtx = None
+
+    def push(self, name: str) -> None:
+        if self._nvtx is not None:
+            self._nvtx.range_push(name)
+
+    def pop(self) -> None:
+        if self._nvtx is not None:
+            self._nvtx.range_pop()
+
+
+def identify(iterations: int, steps: int = 150, every: int = 15, device: int = 0) -> None:
+    import numpy as np
+
+    from fluidsph.adjoint import DifferentiableRollout
+    from fluidsph.sim import SphBatch3DGrid
+
+    scs, _ = scenes.config4(steps=steps)
+    b = SphBatch3DGrid([s.particles for s in scs], [s.sph for s in scs], [s.geom for s in scs],
+                       device=device)
+    for k, s in enumerate(scs):
+        b.update_scene(k, gravity=s.gravity)
+    b.set_pcisph_iterations(scs[0].iterations)
+    grids = [scenes.loss_grid(s, 64) for s in scs]
+    r = DifferentiableRollout(b, every)
+    nv = _Ranges()
+    targets = None
+    for it in range(iterations):
+        for k, s in enumerate(scs):
+            b.upload_scene_particles(k, s.particles)
+        b.sync()
+        t0 = time.perf_counter()
+        nv.push(f"fwd{it}")
+        r.forward(steps)
+        b.sync()
+        nv.pop()
+        t1 = time.perf_counter()
+        if targets is None:
+            targets = [np.zeros_like(r.final_splat(grids[k], scs[k].geom, scene=k))
+                       for k in range(len(scs))]
+        for k in range(len(scs)):
+            r.splat_mse_loss(grids[k], scs[k].geom, targets[k], scene=k)
+        t2 = time.perf_counter()
+        nv.push(f"bwd{it}")
+        r.backward(scenes=len(scs))
+        b.sync()
+        nv.pop()
+        t3 = time.perf_counter()
+        print(f"identification iteration {it}: {sum(s.n for s in scs)} particles, forward "
+              f"{1e3 * (t1 - t0) / steps:.3f} ms/step, loss {1e3 * (t2 - t1):.1f} ms, backward "
+              f"{1e3 * (t3 - t2) / steps:.3f} ms/step", flush=True)
+    r.close()
+    b.close()
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", type=int, default=0, choices=sorted(scenes.CONFIGS))
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--identify", action="store_true")
+    ap.add_argument("--iterations", type=int, default=2)
     a = ap.parse_args(argv)
+    if a.identify:
+        identify(a.iterations, device=a.device)
+        return 0
     sc = scenes.CONFIGS[a.config]()
     sim = SphSimulation3DGrid(sc.particles, sc.sph, sc.geom, device=a.device)
     sim.update_gravity(sc.gravity)
