@@ -172,6 +172,9 @@ cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uin
                                      cudaStream_t st);
 cudaError_t launch_scatter(const DevState &d, uint32_t n_canon, cudaStream_t st);
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_t st);
+// 64-byte AoS records of canonical particles or sorted slots [first, first + count)
+cudaError_t launch_export_aos(const DevState &d, bool sorted, uint32_t first, uint32_t count,
+                              void *out, cudaStream_t st);
 cudaError_t launch_dir_table(const DevState &d, cudaStream_t st);
 cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st);
 constexpr int TASK_COUNTERS = 16;

@@ -287,6 +287,62 @@ cudaError_t launch_scatter(const DevState &d, uint32_t n_canon, cudaStream_t st)
   return cudaGetLastError();
 }
 
+namespace {
+// 64-byte SphParticle3D records (particle.rs:8-17) packed from the SoA
+// arrays into caller device memory: position + pad, velocity + pad,
+// force + density, near density + normal. Four threads per record, one
+// 16-byte quarter each, so consecutive threads store consecutive quarters.
+__global__ void __launch_bounds__(256)
+    k_export_aos(uint32_t count, bool sorted, const float4 *__restrict__ pos,
+                 const float4 *__restrict__ vel, const float4 *__restrict__ frc,
+                 const float4 *__restrict__ aux, const float2 *__restrict__ dens,
+                 const float4 *__restrict__ nrm, float4 *__restrict__ out) {
+  const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= uint64_t(count) * 4u) return;
+  const uint32_t i = uint32_t(t >> 2), q = uint32_t(t & 3u);
+  float4 v;
+  if (q == 0u) {
+    v = pos[i];
+  } else if (q == 1u) {
+    v = vel[i];
+  } else if (sorted) {
+    const float2 d = dens[i];
+    if (q == 2u) {
+      const float4 f = frc[i];
+      v = make_float4(f.x, f.y, f.z, d.x);
+    } else {
+      const float4 n = nrm[i];
+      v = make_float4(d.y, n.x, n.y, n.z);
+    }
+  } else {
+    const float4 a0 = aux[2 * size_t(i)];
+    if (q == 2u) {
+      const float4 f = frc[i];
+      v = make_float4(f.x, f.y, f.z, a0.x);
+    } else {
+      v = make_float4(a0.y, a0.z, a0.w, aux[2 * size_t(i) + 1].x);
+    }
+  }
+  out[t] = v;
+}
+}  // namespace
+
+cudaError_t launch_export_aos(const DevState &d, bool sorted, uint32_t first, uint32_t count,
+                              void *out, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  const uint64_t threads = uint64_t(count) * 4u;
+  const unsigned blocks = unsigned((threads + 255u) / 256u);
+  if (sorted)
+    k_export_aos<<<blocks, 256, 0, st>>>(count, true, d.s_pos + first, d.s_vel + first,
+                                         d.s_frc + first, nullptr, d.s_dens + first,
+                                         d.s_nrm + first, static_cast<float4 *>(out));
+  else
+    k_export_aos<<<blocks, 256, 0, st>>>(count, false, d.p_pos + first, d.p_vel + first,
+                                         d.p_force + first, d.p_aux + 2 * size_t(first), nullptr,
+                                         nullptr, static_cast<float4 *>(out));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_t st) {
   if (n_sorted == 0) return cudaSuccess;
   k_sort_gather<<<blocks_for(n_sorted, 256), 256, 0, st>>>(

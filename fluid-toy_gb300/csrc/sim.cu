@@ -1065,6 +1065,36 @@ int fs_batch_download_scene(FsSim *s, uint32_t scene, SphParticle3D *out, uint32
   return read_canonical(s, s->hu[scene].p_offset, out, count);
 }
 
+int fs_export_particles_aos(FsSim *s, uint32_t scene, int sorted, SphParticle3D *device_out,
+                            uint32_t count) {
+  CHECK_SIM(s);
+  CHECK_SCENE(s, scene);
+  const uint32_t avail = sorted ? s->hu[scene].n : s->scene_n[scene];
+  if (count > avail)
+    return fail(FS_E_CAPACITY, "%s: %u > %u particles", __func__, count, avail);
+  if (count == 0) return FS_OK;
+  if (!device_out) return fail(FS_E_INVALID_ARGUMENT, "%s: null device_out", __func__);
+  if (reinterpret_cast<uintptr_t>(device_out) % 16 != 0)
+    return fail(FS_E_INVALID_ARGUMENT, "%s: device_out must be 16-byte aligned", __func__);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, device_out) != cudaSuccess ||
+      (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)) {
+    cudaGetLastError();  // clear the query's error state
+    return fail(FS_E_INVALID_ARGUMENT, "%s: device_out is not CUDA device or managed memory",
+                __func__);
+  }
+  if (attr.type == cudaMemoryTypeDevice && attr.device != s->device)
+    return fail(FS_E_INVALID_ARGUMENT, "%s: device_out is on device %d, the simulation on %d",
+                __func__, attr.device, s->device);
+  const DevUniforms &u = s->hu[scene];
+  FS_CUDA(launch_export_aos(s->d, sorted != 0, sorted ? u.s_offset : u.p_offset, count,
+                            device_out, s->stream),
+          "AoS export");
+  return FS_OK;
+}
+
 int fs_batch_download_scene_sorted(FsSim *s, uint32_t scene, SphParticle3D *out, uint32_t count) {
   CHECK_SIM(s);
   CHECK_SCENE(s, scene);

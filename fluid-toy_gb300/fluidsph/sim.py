@@ -141,6 +141,14 @@ class SphSimulation3DGrid:
         check(self._lib.fs_download_particles(self._h, out.ctypes.data, n))
         return out
 
+    def export_particles_aos(self, device_ptr: int, count: int, sorted: bool = False,
+                             scene: int = 0) -> None:
+        """Write `count` 64-byte SphParticle3D records (canonical, or sorted
+        slots) into device memory at `device_ptr`, asynchronously on the
+        simulation's stream (fs_export_particles_aos)."""
+        check(self._lib.fs_export_particles_aos(self._h, int(scene), 1 if sorted else 0,
+                                                C.c_void_p(int(device_ptr)), int(count)))
+
     def upload_particles(self, particles: np.ndarray) -> None:
         p = abi.as_particles(particles)
         check(self._lib.fs_upload_particles(self._h, p.ctypes.data, len(p)))

@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010050u
+#define FS_ABI_VERSION 0x00010051u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -420,6 +420,16 @@ int fs_download_cells(FsSim *sim, uint32_t *counts, uint32_t *starts,
  * sorted_to_orig. Either pointer may be NULL. */
 int fs_download_index_maps(FsSim *sim, uint32_t *cell_indices,
                            uint32_t *sorted_to_orig, uint32_t count);
+/* The same 64-byte records written into DEVICE memory, asynchronously on the
+ * simulation's stream (the AoS vertex buffer a renderer instances from,
+ * particle_renderer_3d.rs:144-160: position at offset 0, velocity at 16):
+ * scene `scene`'s canonical particles [0, count) (sorted = 0, the
+ * particle_buffer view) or its sorted slots [0, count) (sorted != 0, the
+ * sorted_particle_buffer view). device_out is CUDA device (on the
+ * simulation's GPU) or managed memory, 16-byte aligned, count * 64 bytes;
+ * anything else returns FS_E_INVALID_ARGUMENT. */
+int fs_export_particles_aos(FsSim *sim, uint32_t scene, int sorted, SphParticle3D *device_out,
+                            uint32_t count);
 /* Overwrite the canonical particle records (all fields) of [0, count). */
 int fs_upload_particles(FsSim *sim, const SphParticle3D *particles,
                         uint32_t count);
