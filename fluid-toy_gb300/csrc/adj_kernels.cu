@@ -110,7 +110,8 @@ __device__ __forceinline__ void for_warp_tasks_sub(const TaskQueue &q, F &&f) {
 // q's in-range neighbours j (1e-12 < r^2 < h^2, the force / XSPH / normal
 // criterion): walked from the recorded step's hit mask when q has one (the
 // forward's own decisions, no candidate tests), else found by testing the
-// candidates. Lane `sub` of q's L lanes takes every L-th hit.
+// candidates. Lane `sub` of q's L lanes takes every L-th mask word (every
+// L-th candidate when testing).
 template <int L, class InRange, class Body>
 __device__ __forceinline__ void for_hits_sub(const Runs &R, const TapeView &t, uint32_t q,
                                              uint32_t sub, InRange &&in_range, Body &&body,
@@ -118,18 +119,9 @@ __device__ __forceinline__ void for_hits_sub(const Runs &R, const TapeView &t, u
   const uint32_t off = t.mask_off[q];
   if (off != MASK_NONE) {
     MaskWalk m;
-    m.init(R, (words ? words : t.mask_words) + off);
-    uint32_t j = 0u, skip = sub;
-    while (true) {
-      bool ok = m.next(R, j);
-      while (ok && skip) {
-        skip--;
-        ok = m.next(R, j);
-      }
-      if (!ok) break;
-      body(j);
-      skip = L - 1;
-    }
+    m.init(R, (words ? words : t.mask_words) + off, sub, uint32_t(L));
+    uint32_t j = 0u;
+    while (m.next(R, j)) body(j);
   } else {
     for_candidates_sub<L>(R, sub, [&](uint32_t j) {
       if (in_range(j)) body(j);

@@ -8,7 +8,8 @@ profilers can address launch by launch) unless --graph replays them as one
 captured graph. Prints the particle count, steps and wall time.
 
 --identify runs the batched parameter-identification workload instead (the
-64 scenes of scenes.config4 as one batch, 150 steps, checkpoint every 15):
+64 scenes of scenes.config4 as one batch, 150 steps, checkpoint every 15;
+--scenes / --rollout-steps / --every shrink it for profiling):
 per iteration a DifferentiableRollout forward, an MSE splat loss per scene
 against zero targets and the backward, inside NVTX ranges named fwd<i> and
 bwd<i> (when torch is importable) so a profiler can select one phase.
@@ -46,13 +47,14 @@ class _Ranges:
             self._nvtx.range_pop()
 
 
-def identify(iterations: int, steps: int = 150, every: int = 15, device: int = 0) -> None:
+def identify(iterations: int, steps: int = 150, every: int = 15, num_scenes: int = 64,
+             device: int = 0) -> None:
     import numpy as np
 
     from fluidsph.adjoint import DifferentiableRollout
     from fluidsph.sim import SphBatch3DGrid
 
-    scs, _ = scenes.config4(steps=steps)
+    scs, _ = scenes.config4(num_scenes=num_scenes, steps=steps)
     b = SphBatch3DGrid([s.particles for s in scs], [s.sph for s in scs], [s.geom for s in scs],
                        device=device)
     for k, s in enumerate(scs):
@@ -98,9 +100,12 @@ def main(argv=None) -> int:
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--identify", action="store_true")
     ap.add_argument("--iterations", type=int, default=2)
+    ap.add_argument("--scenes", type=int, default=64, help="--identify: scenes (the first n)")
+    ap.add_argument("--rollout-steps", type=int, default=150, help="--identify: steps")
+    ap.add_argument("--every", type=int, default=15, help="--identify: checkpoint interval")
     a = ap.parse_args(argv)
     if a.identify:
-        identify(a.iterations, device=a.device)
+        identify(a.iterations, a.rollout_steps, a.every, a.scenes, device=a.device)
         return 0
     sc = scenes.CONFIGS[a.config]()
     sim = SphSimulation3DGrid(sc.particles, sc.sph, sc.geom, device=a.device)
