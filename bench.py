@@ -557,7 +557,7 @@ def run_adjoint(args, dist: Dist) -> dict | None:
     }
 
 
-def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False):
+def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, tape_budget=0):
     """Batched gradient descent on per-scene viscosity and surface tension
     (and stiffness, whose gradient is 0) against hidden-parameter targets.
     Steps are sign steps scaled by a decaying rate relative to each
@@ -591,7 +591,7 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False):
     hb.close()
     params = [with_(s.sph) for s in scenes]
     b = batch(params)
-    r = DifferentiableRollout(b, every)
+    r = DifferentiableRollout(b, every, tape_budget_bytes=tape_budget)
     names = ("viscosity", "stiffness", "surface_tension")
     init = np.array([[getattr(p, n) for n in names] for p in params], np.float64)
     cur = init.copy()
@@ -617,6 +617,7 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False):
         rate = 0.25 * (0.9 ** it)
         step = np.where(np.isfinite(g) & (g != 0), -np.sign(np.nan_to_num(g)), 0.0) * rate * span
         cur = cur + step
+    tape_segments, segment_bytes = r.tape_info()
     r.close()
     b.close()
     err = np.abs(cur - truth) / np.abs(truth)
@@ -625,7 +626,8 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False):
             "relative_error_final": {n: float(np.mean(err[:, i])) for i, n in enumerate(names)},
             "loss_first": losses[0] if losses else None, "loss_last": losses[-1] if losses else None,
             "gradient_finite": bool(np.isfinite(g).all()) if iters else None,
-            "fwd_adjoint_ms_per_step": float(np.median(ms)) if ms else None}
+            "fwd_adjoint_ms_per_step": float(np.median(ms)) if ms else None,
+            "tape_segments": tape_segments, "tape_segment_gb": round(segment_bytes / 1e9, 3)}
 
 
 def run_identify(args, dist: Dist) -> dict | None:
@@ -652,6 +654,9 @@ def run_identify(args, dist: Dist) -> dict | None:
     stream = torch.cuda.Stream(device=dev)  # events and steps on one stream
     b.set_stream(stream.cuda_stream)
     b.prepare_steps(150)
+    b.step(5)  # warm-up, then back to the initial state
+    for k, s in enumerate(scs):
+        b.upload_scene_particles(k, s.particles)
     torch.cuda.synchronize(dev)
     e0.record(stream)
     b.step(150)
@@ -660,6 +665,12 @@ def run_identify(args, dist: Dist) -> dict | None:
     fwd_ms = e0.elapsed_time(e1) / 150
     b.close()
     spec = _identify(scs, hidden, 150, 15, args.gd_iters, 64, dev)
+    # the same with a tape budget of half the free device memory: the forward
+    # records as many checkpoint segments as fit and the backward re-runs only
+    # the others (timing only: two iterations)
+    free, _ = torch.cuda.mem_get_info(dev)
+    budget = int(free * 0.5)
+    budgeted = _identify(scs, hidden, 150, 15, 2, 64, dev, tape_budget=budget)
     well = _identify(*S.reference_physics_batch(64, 20), 20, 5, 50, 32, dev)
     if dist.rank != 0:
         return None
@@ -675,6 +686,12 @@ def run_identify(args, dist: Dist) -> dict | None:
         "forward_ms_per_step": round(fwd_ms, 4),
         "fwd_adjoint_over_forward": round(v / fwd_ms, 3),
         "identification": spec,
+        "with_tape_budget": {
+            "tape_budget_gb": round(budget / 1e9, 1),
+            "tape_segments": budgeted["tape_segments"],
+            "checkpoint_segments": 10,
+            "fwd_adjoint_ms_per_step": round(budgeted["fwd_adjoint_ms_per_step"], 4),
+            "fwd_adjoint_over_forward": round(budgeted["fwd_adjoint_ms_per_step"] / fwd_ms, 3)},
         "identification_reference_physics": well,
     }
 

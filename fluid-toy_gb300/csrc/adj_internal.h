@@ -23,7 +23,7 @@ struct TapeView {
   const uint32_t *mask_words;          // the step's hit masks (density pass)
   const uint32_t *mask_off;            // word offset of each slot's mask, or MASK_NONE
   const uint32_t *perm_hit;            // slots ordered by hit count, heaviest first
-  const uint32_t *hits[kMaxAdjIters];  // per level: in-range masks at the predicted positions
+  const uint32_t *hits;                // union over the levels of the in-range masks at x*
 };
 
 // Reverse accumulators, grid-sorted order.

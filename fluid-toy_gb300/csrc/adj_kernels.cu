@@ -262,8 +262,9 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
     Runs R;
     flag_outside(a.err, runs_checked(f3of(t.pos[q]), U->grid, t.cell_begin + U->c_offset, R));
     const float c_rho = -6.0f * mass * scale_d;
-    // the level's in-range pairs (r^2 < h^2 at the predicted positions),
-    // walked from the mask the forward iteration recorded
+    // the level's in-range pairs (r^2 < h^2 at the predicted positions):
+    // walked from the union of the levels' recorded masks, each pair kept
+    // where it is in range at this level (selects keep the lanes together)
     for_hits_sub<L>(
         R, t, q, sub,
         [&](uint32_t j) {
@@ -274,15 +275,15 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
           const float4 xj4 = __ldg(xpk + j);
           const float3 r = xq - f3of(xj4);
           const float r2 = dot3(r, r);
+          const bool in = r2 < h2;
           const float4 uj4 = __ldg(gu_in + j);
           if (has_rho) {
             const float diff = h2 - r2;
-            xsb = mad3(xsb, c_rho * diff * diff * (rhat_q + uj4.w), r);
+            xsb = in ? mad3(xsb, c_rho * diff * diff * (rhat_q + uj4.w), r) : xsb;
           }
           if (has_p) {
-            // evaluated for every hit, kept for r^2 > 1e-12 (selects keep the
-            // lanes together)
-            const bool ns = r2 > MIN_R2;
+            // evaluated for every hit, kept for 1e-12 < r^2 < h^2
+            const bool ns = in && r2 > MIN_R2;
             const float rt_j = fmaxf(__ldg(rhok + j), 1.0f);
             const float cij = cq + xj4.w / (rt_j * rt_j);
             const float rr = sqrtf(ns ? r2 : 1.0f);
@@ -299,7 +300,7 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
             phisum += ns ? mass * g * edu : 0.0f;
           }
         },
-        t.hits[k]);
+        t.hits);
   }
   xsb = group_sum3<L>(xsb);
   phisum = group_sum<L>(phisum);

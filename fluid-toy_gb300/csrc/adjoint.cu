@@ -35,7 +35,7 @@ struct TapeSlot {
   float4 *ap[kMaxAdjIters];
   uint32_t *order;
   uint32_t *mask_words, *mask_off, *perm_hit;
-  uint32_t *hits[kMaxAdjIters];  // per PCISPH level, same layout as mask_words
+  uint32_t *hits;  // union of the PCISPH levels' hit masks, same layout as mask_words
   size_t mask_cap;
 };
 
@@ -73,8 +73,13 @@ struct FsAdj {
   // one segment of tape + reverse accumulators + cotangents
   void *work = nullptr;
   size_t work_bytes = 0;
-  uint32_t work_N = 0, work_G = 0, work_K = 0, work_every = 0, work_scenes = 0;
+  uint32_t work_N = 0, work_G = 0, work_K = 0, work_every = 0, work_scenes = 0, work_segs = 0;
+  // tape buffers: segs segments of `every` recorded steps, slot b * every + t
   std::vector<TapeSlot> tape;
+  uint32_t segs = 1;             // segment buffers (the forward records the last segs segments)
+  uint64_t tape_budget = 0;      // bytes the caller allows for tape buffers (0: one segment)
+  uint32_t seg_limit = ~0u;      // 1 after the budget's buffers failed to allocate
+  std::vector<int64_t> buf_seg;  // checkpoint segment each buffer holds (-1: none)
   AdjView av{};
   float4 *cot[2][2] = {};  // [buffer][0 = d/d pos, 1 = d/d vel], canonical
   int cur = 0;
@@ -84,7 +89,6 @@ struct FsAdj {
   double *loss = nullptr, *partial = nullptr;
   size_t vox_cap = 0;
   int lanes = 0;  // lanes per particle of the reverse gathers (autotuned)
-  int64_t tape_seg = -1;  // checkpoint segment the tape holds (-1: none)
   uint32_t *scene_first = nullptr, *scene_count = nullptr;  // device, canonical ranges
 };
 
@@ -100,12 +104,9 @@ void free_adj(FsAdj *a) {
   a->field = nullptr;
 }
 
-// Lay out (or size, when base == nullptr) the tape, accumulators and cotangents.
-void carve_work(FsAdj *a, char *base, size_t *bytes) {
-  Carve c{base};
-  const size_t N = a->N, G = a->G;
-  a->tape.assign(a->every, TapeSlot{});
-  for (TapeSlot &t : a->tape) {
+// One recorded step's buffers.
+void carve_slot(Carve &c, TapeSlot &t, size_t N, size_t G, uint32_t K) {
+  {
     t.s2o = c.take<uint32_t>(N);
     t.sos = c.take<uint16_t>(N);
     t.cell_begin = c.take<uint32_t>(G + 1);
@@ -116,18 +117,34 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
     t.anp = c.take<float4>(N);
     t.vfin = c.take<float4>(N);
     t.dens = c.take<float2>(N);
-    for (uint32_t k = 0; k <= a->K; k++) {
+    for (uint32_t k = 0; k <= K; k++) {
       t.xp[k] = c.take<float4>(N);
       t.rho[k] = c.take<float>(N);
     }
-    for (uint32_t k = 0; k < a->K; k++) t.ap[k] = c.take<float4>(N);
+    for (uint32_t k = 0; k < K; k++) t.ap[k] = c.take<float4>(N);
     t.order = c.take<uint32_t>((N + 31) / 32);
     t.mask_cap = tape_mask_cap(N);
     t.mask_words = c.take<uint32_t>(t.mask_cap);
     t.mask_off = c.take<uint32_t>(N);
     t.perm_hit = c.take<uint32_t>(N);
-    for (uint32_t k = 0; k < a->K; k++) t.hits[k] = c.take<uint32_t>(t.mask_cap);
+    t.hits = c.take<uint32_t>(t.mask_cap);
   }
+}
+
+// Bytes of one checkpoint segment's tape (`every` recorded steps).
+uint64_t segment_bytes(const FsAdj *a) {
+  Carve c{nullptr};
+  TapeSlot t{};
+  carve_slot(c, t, a->N, a->G, a->K);
+  return uint64_t(c.off) * a->every;
+}
+
+// Lay out (or size, when base == nullptr) the tape, accumulators and cotangents.
+void carve_work(FsAdj *a, char *base, size_t *bytes) {
+  Carve c{base};
+  const size_t N = a->N, G = a->G;
+  a->tape.assign(size_t(a->segs) * a->every, TapeSlot{});
+  for (TapeSlot &t : a->tape) carve_slot(c, t, N, G, a->K);
   AdjView &v = a->av;
   v.gx = c.take<float4>(N);
   v.gvhat = c.take<float4>(N);
@@ -150,7 +167,7 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
 
 int ensure_work(FsAdj *a) {
   if (a->work && a->work_N == a->N && a->work_G == a->G && a->work_K == a->K &&
-      a->work_every == a->every && a->work_scenes == a->scenes)
+      a->work_every == a->every && a->work_scenes == a->scenes && a->work_segs == a->segs)
     return FS_OK;
   FsSim *s = a->sim;
   if (a->work) {
@@ -159,7 +176,16 @@ int ensure_work(FsAdj *a) {
     a->work = nullptr;
   }
   carve_work(a, nullptr, &a->work_bytes);
-  FS_CUDA(cudaMalloc(&a->work, a->work_bytes), "allocate adjoint workspace");
+  if (cudaMalloc(&a->work, a->work_bytes) != cudaSuccess && a->segs > 1) {
+    // the budget's extra tape segments do not fit: fall back to one (until
+    // the budget changes)
+    cudaGetLastError();
+    a->work = nullptr;
+    a->segs = 1;
+    a->seg_limit = 1;
+    carve_work(a, nullptr, &a->work_bytes);
+  }
+  if (!a->work) FS_CUDA(cudaMalloc(&a->work, a->work_bytes), "allocate adjoint workspace");
   carve_work(a, static_cast<char *>(a->work), &a->work_bytes);
   // cell_begin[0] of every slot must read 0 (the scan writes from index 1)
   FS_CUDA(cudaMemsetAsync(a->work, 0, a->work_bytes, s->stream), "clear adjoint workspace");
@@ -168,6 +194,8 @@ int ensure_work(FsAdj *a) {
   a->work_G = a->G;
   a->work_K = a->K;
   a->work_every = a->every;
+  a->work_segs = a->segs;
+  a->buf_seg.assign(a->segs, -1);
   a->work_scenes = a->scenes;
   return FS_OK;
 }
@@ -218,7 +246,7 @@ TapeView tape_view(const TapeSlot &t, uint32_t K) {
   v.mask_words = t.mask_words;
   v.mask_off = t.mask_off;
   v.perm_hit = t.perm_hit;
-  for (uint32_t k = 0; k < K; k++) v.hits[k] = t.hits[k];
+  v.hits = t.hits;
   return v;
 }
 
@@ -326,6 +354,20 @@ int fs_adj_create(FsSim *sim, uint32_t checkpoint_every, FsAdj **out) {
   return FS_OK;
 }
 
+int fs_adj_set_tape_budget(FsAdj *a, uint64_t bytes) {
+  CHECK_ADJ(a);
+  a->tape_budget = bytes;
+  a->seg_limit = ~0u;
+  return FS_OK;
+}
+
+int fs_adj_tape_info(FsAdj *a, uint32_t *segments, uint64_t *segment_bytes_out) {
+  CHECK_ADJ(a);
+  if (segments) *segments = a->work ? a->segs : 0u;
+  if (segment_bytes_out) *segment_bytes_out = a->work ? segment_bytes(a) : 0u;
+  return FS_OK;
+}
+
 int fs_adj_destroy(FsAdj *a) {
   if (!a) return FS_OK;
   if (a->sim) {
@@ -367,22 +409,33 @@ int fs_adj_forward(FsAdj *a, uint32_t nsteps) {
   if (!a->final_state)
     FS_CUDA(cudaMalloc(&a->final_state, sizeof(float4) * 2 * std::max<size_t>(a->N, 1)),
             "allocate final state");
+  // tape segment buffers: one, or as many as the caller's budget holds (up
+  // to the rollout's segments)
+  {
+    const uint64_t seg = segment_bytes(a);
+    uint64_t want = seg ? a->tape_budget / seg : 1;
+    want = std::max<uint64_t>(1, std::min<uint64_t>({want, uint64_t(std::max<uint32_t>(nck, 1)),
+                                                      uint64_t(a->seg_limit)}));
+    a->segs = uint32_t(want);
+  }
   if ((rc = ensure_work(a))) return rc;
-  a->tape_seg = -1;
+  a->buf_seg.assign(a->segs, -1);
+  // the reverse pass starts with the last segments: the last `segs` record
+  // their tapes on the way instead of being re-run there
+  const uint32_t first_rec = nck > a->segs ? nck - a->segs : 0u;
   for (uint32_t c = 0; c < nck; c++) {
     float4 *ck = a->ck + size_t(c) * 2 * a->N;
     if ((rc = copy_state(s, ck, ck + a->N, s->d.p_pos, s->d.p_vel, a->N))) return rc;
     const uint32_t len = std::min(a->every, nsteps - c * a->every);
-    if (c + 1 < nck) {
+    if (c < first_rec) {
       if ((rc = fs_step(s, len))) return rc;
     } else {
-      // the reverse pass starts with the last segment: record its tape now
-      // instead of re-running it there
+      const uint32_t b = c - first_rec;
       for (uint32_t t = 0; t < len; t++) {
-        const DevState dv = recording_state(a, a->tape[t]);
+        const DevState dv = recording_state(a, a->tape[size_t(b) * a->every + t]);
         if ((rc = enqueue_step(s, false, &dv))) return rc;
       }
-      a->tape_seg = int64_t(c);
+      a->buf_seg[b] = int64_t(c);
     }
   }
   if ((rc = copy_state(s, a->final_state, a->final_state + a->N, s->d.p_pos, s->d.p_vel, a->N)))
@@ -549,19 +602,24 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
   const SceneView base = s->d.view();
   for (uint32_t seg = nck; seg-- > 0;) {
     const uint32_t len = std::min(a->every, a->steps - seg * a->every);
-    if (a->tape_seg != int64_t(seg)) {
-      // restore the segment's checkpoint and re-run it, recording
-      a->tape_seg = -1;
+    uint32_t b = 0;
+    while (b < a->segs && a->buf_seg[b] != int64_t(seg)) b++;
+    if (b == a->segs) {
+      // restore the segment's checkpoint and re-run it, recording into
+      // buffer 0 (whose segment, if any, has been reversed already)
+      b = 0;
+      a->buf_seg[0] = -1;
       const float4 *ck = a->ck + size_t(seg) * 2 * N;
       if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, ck, ck + N, N))) return rc;
       for (uint32_t t = 0; t < len; t++) {
         const DevState dv = recording_state(a, a->tape[t]);
         if ((rc = enqueue_step(s, false, &dv))) return rc;
       }
-      a->tape_seg = int64_t(seg);
+      a->buf_seg[0] = int64_t(seg);
     }
+    const TapeSlot *seg_tape = a->tape.data() + size_t(b) * a->every;
     for (uint32_t t = len; t-- > 0;) {
-      const TapeSlot &slot = a->tape[t];
+      const TapeSlot &slot = seg_tape[t];
       SceneView v = base;
       v.scene_of_slot = slot.sos;
       if (a->lanes == 0) {

@@ -129,7 +129,7 @@ struct DevState {
   float4 *const *rec_xp = nullptr;   // [iterations + 1]
   float *const *rec_rho = nullptr;   // [iterations + 1]
   float4 *const *rec_ap = nullptr;   // [iterations] pressure acceleration before the clamp
-  uint32_t *const *rec_hits = nullptr;  // [iterations] per-level hit masks (density mask layout)
+  uint32_t *rec_hits = nullptr;  // union over the PCISPH levels of their hit masks (density mask layout)
 };
 
 // Set the thread-local text fs_last_error() returns (sim.cu).

@@ -407,9 +407,10 @@ __device__ __forceinline__ void force_predict_one(
 // velocity. Each other iteration also writes every particle's pressure term
 // p / max(rho, 1)^2 (the shader's per-neighbour quotient, which depends on
 // the neighbour only), so the next iteration reads it instead of dividing per
-// pair. When recording (hit_out), the iteration also writes each particle's
-// in-range candidates (r^2 < h^2 at the predicted positions) as a hit mask in
-// the density mask's layout and offsets (same runs), for the reverse pass.
+// pair. When recording (hit_out), the iteration also records each particle's
+// in-range candidates (r^2 < h^2 at the predicted positions) in a hit mask in
+// the density mask's layout and offsets (same runs), for the reverse pass:
+// iteration 0 writes it, later iterations OR theirs in (one union mask).
 template <bool HAS_PRESSURE, bool LAST, bool RECORD>
 __device__ __forceinline__ void solve_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
@@ -419,7 +420,7 @@ __device__ __forceinline__ void solve_one(
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
-            uint32_t *__restrict__ hit_out) {
+            uint32_t *__restrict__ hit_out, bool hit_or) {
   const bool active = s < v.b->n_sorted;
   const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
@@ -480,7 +481,7 @@ __device__ __forceinline__ void solve_one(
           }
         }
         if (RECORD) {
-          if (hit_words) hit_words[widx] = hitw;
+          if (hit_words) hit_words[widx] = hit_or ? (hit_words[widx] | hitw) : hitw;
           widx++;
         }
         if (HAS_PRESSURE) {
@@ -692,11 +693,11 @@ __global__ void __launch_bounds__(128)
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
-            uint32_t *__restrict__ hit_out) {
+            uint32_t *__restrict__ hit_out, bool hit_or) {
   for_warp_tasks(q, [&](uint32_t s) {
     solve_one<HAS_PRESSURE, LAST, RECORD>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
                                           rho_out, pterm_out, v_out, stats, ap_out, mask_off,
-                                          hit_out);
+                                          hit_out, hit_or);
   });
 }
 
@@ -1069,7 +1070,8 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   float4 *xp_out = d.rec_xp ? d.rec_xp[iter + 1] : d.pred_xp[out];
   float *rho_out = d.rec_rho ? d.rec_rho[iter + 1] : d.pred_rho[out];
   float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
-  uint32_t *hit_out = d.rec_hits ? d.rec_hits[iter] : nullptr;
+  uint32_t *hit_out = d.rec_hits;
+  const bool hit_or = iter > 0;
   TaskQueue q;
   cudaError_t e = prepare_queue(d, d.warp_order, false, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
@@ -1080,7 +1082,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     k_solve<P_, L_, R_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp,          \
                                                 d.cell_begin, xp_in, d.pterm[in], xp_out,     \
                                                 rho_out, d.pterm[out], d.pred_v, d.stats,     \
-                                                ap_out, d.mask_off, hit_out);                 \
+                                                ap_out, d.mask_off, hit_out, hit_or);         \
   } while (0)
 #define FS_SOLVE_R(P_, L_)            \
   do {                                \

@@ -15,7 +15,7 @@ import numpy as np
 
 from .build import LIB_PATH
 
-FS_ABI_VERSION = 0x00010051
+FS_ABI_VERSION = 0x00010052
 FS_OK = 0
 FS_STAGE_COUNT = 10
 FS_STAT_COUNT = 5
@@ -225,6 +225,8 @@ SIGNATURES = {
     "fs_adj_create": (C.c_int, [_vp, _u32, _P(_vp)]),
     "fs_adj_destroy": (C.c_int, [_vp]),
     "fs_adj_forward": (C.c_int, [_vp, _u32]),
+    "fs_adj_set_tape_budget": (C.c_int, [_vp, C.c_uint64]),
+    "fs_adj_tape_info": (C.c_int, [_vp, _P(_u32), _P(C.c_uint64)]),
     "fs_adj_set_cotangents": (C.c_int, [_vp, _vp, _vp, C.c_int]),
     "fs_adj_splat_mse_loss": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),
                                         _vp, C.c_int, _P(C.c_double)]),

@@ -21,13 +21,27 @@ from .abi import check
 
 
 class DifferentiableRollout:
-    def __init__(self, sim, checkpoint_every: int = 20):
+    def __init__(self, sim, checkpoint_every: int = 20, tape_budget_bytes: int = 0):
         self._lib = abi.load()
         self.sim = sim
         h = C.c_void_p()
         check(self._lib.fs_adj_create(sim._h, int(checkpoint_every), C.byref(h)))
         self._h = h
         sim._register(self)
+        if tape_budget_bytes:
+            self.set_tape_budget(tape_budget_bytes)
+
+    def set_tape_budget(self, nbytes: int) -> None:
+        """Device memory the tape may take (fs_adj_set_tape_budget): segments
+        that fit are recorded during forward() and not re-run by backward()."""
+        check(self._lib.fs_adj_set_tape_budget(self._h, int(nbytes)))
+
+    def tape_info(self) -> tuple[int, int]:
+        """(tape segments of the last forward, bytes per segment)."""
+        n = C.c_uint32()
+        b = C.c_uint64()
+        check(self._lib.fs_adj_tape_info(self._h, C.byref(n), C.byref(b)))
+        return n.value, b.value
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

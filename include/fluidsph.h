@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010051u
+#define FS_ABI_VERSION 0x00010052u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -553,7 +553,8 @@ int fs_batch_upload_scene(FsSim *sim, uint32_t scene, const SphParticle3D *parti
  * piecewise constant (taken from the recorded steps, not differentiated); the
  * r < 0.1h fallback direction is constant. The forward keeps the state every
  * `checkpoint_every` steps; the backward recomputes each segment from its
- * checkpoint, recording the step intermediates, and reverses it. Per-particle
+ * checkpoint, recording the step intermediates, and reverses it (segments
+ * whose tape the forward recorded are reversed directly). Per-particle
  * adjoints are FP32; the parameter gradients are reduced in FP64 (stiffness
  * is read by no stage of the step: its gradient is 0). Supported: every
  * particle active, mouse force and rigid body inactive, at most 16 PCISPH
@@ -565,8 +566,21 @@ int fs_adj_create(FsSim *sim, uint32_t checkpoint_every, FsAdj **out);
 int fs_adj_destroy(FsAdj *adj);
 /* Run nsteps steps from the simulation's current state, recording; the
  * cotangents are cleared. The parameters must not change until the
- * backward. */
+ * backward. The last checkpoint segment's tape is recorded on the way (and,
+ * with a tape budget, the last S segments'), so the backward re-runs only
+ * the other segments. */
 int fs_adj_forward(FsAdj *adj, uint32_t nsteps);
+/* Device memory the tape may take, in bytes (default 0: one segment of
+ * `checkpoint_every` steps). From the next fs_adj_forward on, the tape
+ * holds S = min(budget / segment bytes, segments of the rollout) segments
+ * (at least 1), recorded during the forward and reversed without re-running
+ * them; checkpoints are still kept every `checkpoint_every` steps and the
+ * earlier segments re-run from them. If the S buffers cannot be allocated
+ * the tape falls back to one segment until the budget is set again. */
+int fs_adj_set_tape_budget(FsAdj *adj, uint64_t bytes);
+/* Tape segments allocated by the last fs_adj_forward (0 before any) and the
+ * bytes one segment takes. Either pointer may be NULL. */
+int fs_adj_tape_info(FsAdj *adj, uint32_t *segments, uint64_t *segment_bytes);
 /* Cotangents dL/dpos and dL/dvel of the final canonical state, (N, 3) float
  * rows (N = fs_num_particles), host or device memory; NULL = zero. */
 int fs_adj_set_cotangents(FsAdj *adj, const float *dl_dpos, const float *dl_dvel,

@@ -68,13 +68,15 @@ def _oracle_loss(oracle_mod, sc, mc, target, steps, visc=None, st=None, vel=None
     return float(np.mean((f - target.astype(np.float64)) ** 2))
 
 
-def _gpu_grad(sc, mc, target, steps, every=6):
+def _gpu_grad(sc, mc, target, steps, every=6, tape_budget=0, info=None):
     from fluidsph.adjoint import DifferentiableRollout
     sim = gpu_sim_for_scene(sc)
-    r = DifferentiableRollout(sim, every)
+    r = DifferentiableRollout(sim, every, tape_budget_bytes=tape_budget)
     r.forward(steps)
     loss = r.splat_mse_loss(mc, sc.geom, target)
     dpos, dvel, dpar = r.backward()
+    if info is not None:
+        info.append(r.tape_info())
     return loss, dpos.astype(np.float64), dvel.astype(np.float64), dpar
 
 
@@ -182,3 +184,23 @@ def test_backward_deterministic_and_checkpoint_independent(smooth):
     assert np.array_equal(dpar, dpar2)
     _, dpos3, dvel3, dpar3 = _gpu_grad(sc, mc, target, sc.steps, every=20)
     assert np.array_equal(dvel, dvel3) and np.array_equal(dpar, dpar3)
+
+
+def test_tape_budget_keeps_gradients(smooth):
+    """With a tape budget the forward records several segments and the
+    backward reverses them without re-running them: same bits."""
+    sc, mc, target, (loss, dpos, dvel, dpar) = smooth
+    info = []
+    loss2, dpos2, dvel2, dpar2 = _gpu_grad(sc, mc, target, sc.steps, every=6, info=info)
+    assert info[-1][0] == 1 and info[-1][1] > 0  # default: one segment
+    segs = -(-sc.steps // 6)
+    loss3, dpos3, dvel3, dpar3 = _gpu_grad(sc, mc, target, sc.steps, every=6,
+                                           tape_budget=info[-1][1] * segs, info=info)
+    assert info[-1][0] == segs
+    assert loss3 == loss and np.array_equal(dpos, dpos3) and np.array_equal(dvel, dvel3)
+    assert np.array_equal(dpar, dpar3)
+    # a budget of two segments: the last two recorded, the others re-run
+    loss4, dpos4, dvel4, dpar4 = _gpu_grad(sc, mc, target, sc.steps, every=6,
+                                           tape_budget=info[-1][1] * 2, info=info)
+    assert info[-1][0] == min(2, segs)
+    assert np.array_equal(dpos, dpos4) and np.array_equal(dpar, dpar4)
