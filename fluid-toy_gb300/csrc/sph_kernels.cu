@@ -669,7 +669,11 @@ __global__ void __launch_bounds__(128)
   for_warp_tasks(q, [&](uint32_t s) { xsph_one(s, v, s_vel, nb_pos, nb_vel, begin, vel_x); });
 }
 
-__global__ void __launch_bounds__(128, 4)
+// Threads per block of the force pass: its registers fit 19 warps per SM,
+// which blocks of 128 threads round down to 16.
+constexpr int kForceThreads = 128;
+
+__global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
     k_force_predict(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
                     const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
                     const float4 *__restrict__ nb_nrm, const float2 *__restrict__ s_dens,
@@ -972,9 +976,9 @@ cudaError_t launch_dir_table(const DevState &d, cudaStream_t st) {
 namespace {
 // Persistent grid: as many resident blocks as the kernel's occupancy allows.
 template <class K>
-unsigned persistent_blocks(K kernel, int sm_count) {
+unsigned persistent_blocks(K kernel, int sm_count, int threads = 128) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
   return unsigned(per_sm * sm_count);
@@ -1052,10 +1056,10 @@ cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st)
   cudaError_t e = prepare_queue(d, d.perm_hit, true, n, 1, st, &q);
   if (e != cudaSuccess) return e;
   static unsigned blocks = 0;
-  if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count);
+  if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count, kForceThreads);
   float4 *xp_out = d.rec_xp ? d.rec_xp[0] : d.pred_xp[0];
   float *rho_out = d.rec_rho ? d.rec_rho[0] : d.pred_rho[0];
-  k_force_predict<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm,
+  k_force_predict<<<blocks, kForceThreads, 0, st>>>(q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm,
                                           d.s_dens, d.s_nrm, d.vel_x,
                                           d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
                                           d.mask_off, d.anp, xp_out, rho_out);
