@@ -130,6 +130,9 @@ struct DevState {
   float *const *rec_rho = nullptr;   // [iterations + 1]
   float4 *const *rec_ap = nullptr;   // [iterations] pressure acceleration before the clamp
   uint32_t *rec_hits = nullptr;  // union over the PCISPH levels of their hit masks (density mask layout)
+  // density and solve: the instantiation with batched candidate loads (true)
+  // or the plain loop (false); the same results, chosen per workload by speed
+  bool batched_loads = false;
 };
 
 // Set the thread-local text fs_last_error() returns (sim.cu).

@@ -28,6 +28,7 @@ constexpr int kGraphSlots = 4;
 struct StepGraph {
   cudaGraphExec_t exec = nullptr;
   uint32_t steps = 0, n_canon = 0, n_sorted = 0, iters = 0;
+  bool batched_loads = false;
   cudaStream_t stream = nullptr;
   uint64_t last_use = 0;
 };
@@ -55,6 +56,16 @@ struct FsSim {
   std::vector<uint8_t> coupled;  // scenes whose rigid body is device-coupled
   float *splat_buf = nullptr;  // device staging of host-bound density fields
   size_t splat_cap = 0;
+  // Load-batching choice of the density and solve passes (DevState::
+  // batched_loads, the same results either way): once the simulation has run
+  // 8 steps, its next four steps run as plain / batched / batched / plain,
+  // each between two events, whatever the fs_step call sizes; the next call
+  // waits for them once and keeps the faster instantiation.
+  bool batched_loads = false;
+  int tune_state = 0;  // 0 measuring (phase), 1 measured (events pending), 2 decided
+  int tune_phase = 0;  // measured steps so far
+  cudaEvent_t tune_ev[8] = {};
+  uint64_t steps_done = 0;
   // stage timing
   bool timing = false;
   cudaEvent_t ev[FS_STAGE_COUNT + 1] = {};
@@ -75,8 +86,9 @@ namespace fs {
 int set_device(FsSim *s);
 // Synchronise the stream and report a device-side error word, if set.
 int check_device_error(FsSim *s);
-// Enqueue one step on the simulation's stream (on `dv`'s buffers if given).
-int enqueue_step(FsSim *s, bool timed, const DevState *dv = nullptr);
+// Enqueue one step on the simulation's stream (on `dv`'s buffers if given;
+// batched loads as decided for the simulation, or as `batched` when 0 / 1).
+int enqueue_step(FsSim *s, bool timed, const DevState *dv = nullptr, int batched = -1);
 // Enqueue only the grid build (clear, hash, scan, reorder) of the current state.
 int enqueue_grid_build(FsSim *s);
 

@@ -262,12 +262,13 @@ int write_particles(FsSim *s, const SphParticle3D *parts, uint32_t offset, uint3
 // One step: the stage sequence of step(), sph_3d_grid.rs:1261-1444, over all
 // scenes at once, on the simulation's buffers or on `dv` (the same buffers
 // with some replaced, e.g. by a recording for the reverse pass).
-int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv) {
+int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv, int batched) {
   const uint32_t n = s->hb.n_sorted;
   const uint32_t n_canon = s->hb.n_canon;
   const uint32_t G = s->cells_total;
   cudaStream_t st = s->stream;
-  const DevState &d = dv ? *dv : s->d;
+  DevState d = dv ? *dv : s->d;
+  d.batched_loads = batched < 0 ? s->batched_loads : batched != 0;
   auto mark = [&](int i) -> int {
     if (timed) FS_CUDA(cudaEventRecord(s->ev[i], st), "record stage event");
     return FS_OK;
@@ -316,11 +317,53 @@ namespace {
 
 // The graph of `steps` back-to-back steps for the current counts, captured
 // on first use (least recently used slot replaced).
+// The load-batching choice (FsSim::batched_loads): measured once the
+// simulation has run this many steps (the clumps of an over-compressed start
+// have formed by then).
+constexpr uint64_t kTuneAfterSteps = 8;
+
+bool capturing(FsSim *s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+}
+
+constexpr int kTuneSteps = 4;
+
+// Wait for the four measured steps and keep the faster instantiation.
+int tune_decide(FsSim *s) {
+  if (s->tune_state != 1 || capturing(s)) return FS_OK;
+  FS_CUDA(cudaEventSynchronize(s->tune_ev[2 * kTuneSteps - 1]), "load-batching measurement");
+  float t[kTuneSteps];
+  for (int p = 0; p < kTuneSteps; p++)
+    FS_CUDA(cudaEventElapsedTime(&t[p], s->tune_ev[2 * p], s->tune_ev[2 * p + 1]),
+            "load-batching measurement");
+  s->batched_loads = t[1] + t[2] < t[0] + t[3];
+  s->tune_state = 2;
+  return FS_OK;
+}
+
+// Run the measured steps that are due (plain / batched / batched / plain),
+// consuming them from nsteps.
+int tune_steps(FsSim *s, uint32_t &nsteps) {
+  while (nsteps > 0 && s->tune_state == 0 && s->steps_done >= kTuneAfterSteps) {
+    const int p = s->tune_phase;
+    FS_CUDA(cudaEventRecord(s->tune_ev[2 * p], s->stream), "load-batching measurement");
+    const int rc = enqueue_step(s, false, nullptr, (p == 1 || p == 2) ? 1 : 0);
+    if (rc) return rc;
+    FS_CUDA(cudaEventRecord(s->tune_ev[2 * p + 1], s->stream), "load-batching measurement");
+    s->steps_done++;
+    nsteps--;
+    if (++s->tune_phase == kTuneSteps) s->tune_state = 1;
+  }
+  return FS_OK;
+}
+
 int graph_for(FsSim *s, uint32_t steps, cudaGraphExec_t *out) {
   StepGraph *slot = nullptr;
   for (StepGraph &g : s->graphs) {
     if (g.exec && g.steps == steps && g.n_canon == s->hb.n_canon &&
-        g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream) {
+        g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream &&
+        g.batched_loads == s->batched_loads) {
       g.last_use = ++s->graph_clock;
       *out = g.exec;
       return FS_OK;
@@ -355,6 +398,7 @@ int graph_for(FsSim *s, uint32_t steps, cudaGraphExec_t *out) {
   slot->n_sorted = s->hb.n_sorted;
   slot->iters = s->iterations;
   slot->stream = s->stream;
+  slot->batched_loads = s->batched_loads;
   slot->last_use = ++s->graph_clock;
   *out = exec;
   return FS_OK;
@@ -461,6 +505,8 @@ int create_sim(const char *who, const SphParticle3D *particles, const uint32_t *
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     for (auto &e : s->ev)
       if (e) cudaEventDestroy(e);
+    for (auto &e : s->tune_ev)
+      if (e) cudaEventDestroy(e);
     delete s;
     return code;
   };
@@ -470,6 +516,10 @@ int create_sim(const char *who, const SphParticle3D *particles, const uint32_t *
   if (e != cudaSuccess) return bail(cuda_fail(e, "create stream"));
   s->stream = s->own_stream;
   for (auto &ev : s->ev) {
+    e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "create event"));
+  }
+  for (auto &ev : s->tune_ev) {
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return bail(cuda_fail(e, "create event"));
   }
@@ -612,6 +662,8 @@ int fs_destroy(FsSim *s) {
   if (s->frame_graph.exec) cudaGraphExecDestroy(s->frame_graph.exec);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
+  for (auto &e : s->tune_ev)
+    if (e) cudaEventDestroy(e);
   if (s->splat_buf) cudaFree(s->splat_buf);
   if (s->arena) cudaFree(s->arena);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -619,11 +671,37 @@ int fs_destroy(FsSim *s) {
   return FS_OK;
 }
 
+namespace {
+int run_steps(FsSim *s, uint32_t nsteps);
+}
+
 int fs_step(FsSim *s, uint32_t nsteps) {
   CHECK_SIM(s);
   int rc;
   if ((rc = set_device(s))) return rc;
   if (nsteps == 0) return FS_OK;
+  if (!capturing(s)) {
+    if ((rc = tune_decide(s))) return rc;
+    // stage-timed steps are never measurement steps
+    if (!s->timing && s->tune_state == 0 && s->steps_done < kTuneAfterSteps &&
+        s->steps_done + nsteps > kTuneAfterSteps) {
+      const uint32_t pre = uint32_t(kTuneAfterSteps - s->steps_done);
+      if ((rc = run_steps(s, pre))) return rc;
+      s->steps_done += pre;
+      nsteps -= pre;
+    }
+    if (!s->timing && (rc = tune_steps(s, nsteps))) return rc;
+    if (nsteps == 0) return FS_OK;
+  }
+  s->steps_done += nsteps;
+  return run_steps(s, nsteps);
+}
+
+namespace {
+// The step loop: stage-timed steps, one step, or graphs of up to
+// kMaxGraphSteps steps.
+int run_steps(FsSim *s, uint32_t nsteps) {
+  int rc;
   if (s->timing) {
     for (uint32_t k = 0; k < nsteps; k++) {
       if ((rc = enqueue_step(s, true))) return rc;
@@ -656,11 +734,13 @@ int fs_step(FsSim *s, uint32_t nsteps) {
   }
   return FS_OK;
 }
+}  // namespace
 
 int fs_prepare_steps(FsSim *s, uint32_t nsteps) {
   CHECK_SIM(s);
   int rc;
   if ((rc = set_device(s))) return rc;
+  if ((rc = tune_decide(s))) return rc;  // capture with the final choice
   if (nsteps < 2 || s->timing) return FS_OK;
   const uint32_t chunks = (nsteps + kMaxGraphSteps - 1) / kMaxGraphSteps;
   const uint32_t chunk = nsteps / chunks;
@@ -838,9 +918,12 @@ int fs_frames(FsSim *s, uint32_t substeps, uint32_t frames) {
   int rc;
   if ((rc = set_device(s))) return rc;
   if (frames == 0) return FS_OK;
+  if ((rc = tune_decide(s))) return rc;
+  s->steps_done += uint64_t(substeps) * frames;
   StepGraph &g = s->frame_graph;
   if (!(g.exec && g.steps == substeps && g.n_canon == s->hb.n_canon &&
-        g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream)) {
+        g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream &&
+        g.batched_loads == s->batched_loads)) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = StepGraph{};
     cudaGraph_t graph = nullptr;
@@ -870,6 +953,7 @@ int fs_frames(FsSim *s, uint32_t substeps, uint32_t frames) {
     g.n_sorted = s->hb.n_sorted;
     g.iters = s->iterations;
     g.stream = s->stream;
+    g.batched_loads = s->batched_loads;
   }
   for (uint32_t f = 0; f < frames; f++)
     FS_CUDA(cudaGraphLaunch(g.exec, s->stream), "launch frame graph");

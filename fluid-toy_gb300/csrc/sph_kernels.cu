@@ -26,6 +26,20 @@
 namespace fs {
 namespace {
 
+// Candidate records loaded ahead per lane (batched_loop; <= 1: plain loop).
+// Density and solve have two instantiations: kBatchedLoads records in flight
+// per lane (105 registers), or the plain loop at the higher occupancy its
+// fewer registers allow. Which is faster depends on the workload: on the
+// 1M-particle dam break (clumps of ~10,000) B = 16 takes density 4.11 -> 3.22
+// ms and the four solve iterations 7.22 -> 4.92 ms, on the 256-scene ensemble
+// the plain loop is faster (step 29.3 ms against 33.5). The simulation picks
+// per workload by timing both (DevState::batched_loads, set by fs_step); the
+// results are the same bits either way. XSPH (two records per candidate)
+// uses B = 4.
+constexpr int kBatchedLoads = 16;
+constexpr int kPlainLoads = 0;
+constexpr int kXsphBatch = 4;
+
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -107,6 +121,7 @@ __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int
 // is evaluated for every candidate and the sums are updated with selects
 // (x = hit ? x + t : x, the same bits as the shader's branch), so lanes never
 // split inside the loop.
+template <int B>
 __device__ __forceinline__ void density_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
               const float4 *__restrict__ s_vel,
@@ -142,10 +157,10 @@ __device__ __forceinline__ void density_one(
     for (int r = 0; r < R.count; r++) {
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
-        uint32_t word = 0u, bit = 1u;
-#pragma unroll 8
-        for (uint32_t k = 0; k < cnt; k++, bit <<= 1) {
-          const float4 pj = __ldg(s_pos + base + k);
+        uint32_t word = 0u;
+        batched_loop<B>(
+            cnt, [&](uint32_t k) { return __ldg(s_pos + base + k); },
+            [&](uint32_t k, const float4 pj) {
           const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
           const float r_sq = rx * rx + ry * ry + rz * rz;
           const bool hit = r_sq < h2;
@@ -164,8 +179,8 @@ __device__ __forceinline__ void density_one(
           normal.y = ns ? ny : normal.y;
           normal.z = ns ? nz : normal.z;
           hits += hit ? 1u : 0u;
-          word |= ns ? bit : 0u;
-        }
+          word |= ns ? (1u << k) : 0u;
+        });
         if (off != MASK_NONE) words[widx] = word;
         widx++;
         nonself += uint32_t(__popc(word));
@@ -225,11 +240,16 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
   Runs R;
   neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
   float3 corr = f3(0.f, 0.f, 0.f);
+  struct PV {
+    float4 p, v;
+  };
   for (int r = 0; r < R.count; r++) {
-#pragma unroll 8
-    for (uint32_t j = R.lo[r]; j < R.hi[r]; j++) {
-      const float4 pj = __ldg(nb_pos + j);
-      const float4 vj = __ldg(nb_vel + j);
+    const uint32_t lo = R.lo[r];
+    batched_loop<kXsphBatch>(
+        R.hi[r] - lo, [&](uint32_t k) { return PV{__ldg(nb_pos + lo + k), __ldg(nb_vel + lo + k)}; },
+        [&](uint32_t, const PV &q) {
+      const float4 pj = q.p;
+      const float4 vj = q.v;
       const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
       const float r_sq = rx * rx + ry * ry + rz * rz;
       const bool hit = r_sq < h2 && r_sq > 1e-12f;
@@ -237,7 +257,7 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
       const float w = scale_d * diff * diff * diff;
       const float3 c = corr + vj.w * (xyz(vj) - vel_i) * w;
       corr = hit ? c : corr;
-    }
+    });
   }
   const float3 vn = vel_i + eps * corr;
   vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
@@ -411,7 +431,7 @@ __device__ __forceinline__ void force_predict_one(
 // in-range candidates (r^2 < h^2 at the predicted positions) in a hit mask in
 // the density mask's layout and offsets (same runs), for the reverse pass:
 // iteration 0 writes it, later iterations OR theirs in (one union mask).
-template <bool HAS_PRESSURE, bool LAST, bool RECORD>
+template <bool HAS_PRESSURE, bool LAST, bool RECORD, int B>
 __device__ __forceinline__ void solve_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
@@ -467,19 +487,19 @@ __device__ __forceinline__ void solve_one(
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
         uint32_t chunk = 0u, hitw = 0u;
-#pragma unroll 8
-        for (uint32_t k = 0; k < cnt; k++) {
-          const float4 nb = __ldg(xp_in + base + k);
-          const float3 r_vec = pred_pos - xyz(nb);
-          const float r_sq = dot3(r_vec, r_vec);
-          if (r_sq < h2) {
-            hits++;
-            const float diff = h2 - r_sq;
-            pred_density += mass * (scale_d * diff * diff * diff);
-            if (HAS_PRESSURE && r_sq > 1e-12f) chunk |= 1u << k;
-            if (RECORD) hitw |= 1u << k;
-          }
-        }
+        batched_loop<B>(
+            cnt, [&](uint32_t k) { return __ldg(xp_in + base + k); },
+            [&](uint32_t k, const float4 nb) {
+              const float3 r_vec = pred_pos - xyz(nb);
+              const float r_sq = dot3(r_vec, r_vec);
+              if (r_sq < h2) {
+                hits++;
+                const float diff = h2 - r_sq;
+                pred_density += mass * (scale_d * diff * diff * diff);
+                if (HAS_PRESSURE && r_sq > 1e-12f) chunk |= 1u << k;
+                if (RECORD) hitw |= 1u << k;
+              }
+            });
         if (RECORD) {
           if (hit_words) hit_words[widx] = hit_or ? (hit_words[widx] | hitw) : hitw;
           widx++;
@@ -649,6 +669,7 @@ __global__ void __launch_bounds__(256)
   perm[base[k] + pos + uint32_t(__popc(peers & ((1u << lane) - 1u)))] = s;
 }
 
+template <int B>
 __global__ void __launch_bounds__(128)
     k_density(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
               const float4 *__restrict__ s_vel, const uint32_t *__restrict__ begin,
@@ -657,8 +678,8 @@ __global__ void __launch_bounds__(128)
               uint32_t *__restrict__ mask_off, uint32_t *__restrict__ mask_hits,
               unsigned long long *__restrict__ mask_alloc, unsigned long long mask_cap) {
   for_warp_tasks(q, [&](uint32_t s) {
-    density_one(s, v, s_pos, s_vel, begin, s_dens, s_nrm, nb, stats, mask_words, mask_off,
-                mask_hits, mask_alloc, mask_cap);
+    density_one<B>(s, v, s_pos, s_vel, begin, s_dens, s_nrm, nb, stats, mask_words, mask_off,
+                   mask_hits, mask_alloc, mask_cap);
   });
 }
 
@@ -688,7 +709,7 @@ __global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
   });
 }
 
-template <bool HAS_PRESSURE, bool LAST, bool RECORD>
+template <bool HAS_PRESSURE, bool LAST, bool RECORD, int B>
 __global__ void __launch_bounds__(128)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
@@ -699,7 +720,7 @@ __global__ void __launch_bounds__(128)
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
             uint32_t *__restrict__ hit_out, bool hit_or) {
   for_warp_tasks(q, [&](uint32_t s) {
-    solve_one<HAS_PRESSURE, LAST, RECORD>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
+    solve_one<HAS_PRESSURE, LAST, RECORD, B>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
                                           rho_out, pterm_out, v_out, stats, ap_out, mask_off,
                                           hit_out, hit_or);
   });
@@ -1030,12 +1051,20 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   TaskQueue q;
   e = prepare_queue(d, d.warp_order, false, n, TASK_COUNTERS - 1, st, &q);
   if (e != cudaSuccess) return e;
-  static unsigned blocks = 0;
-  if (!blocks) blocks = persistent_blocks(k_density, d.sm_count);
   const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm};
-  k_density<<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm,
-                                    nb, d.stats, d.mask_words, d.mask_off, d.mask_hits,
-                                    d.mask_alloc, d.mask_cap);
+  if (d.batched_loads) {
+    static unsigned blocks = 0;
+    if (!blocks) blocks = persistent_blocks(k_density<kBatchedLoads>, d.sm_count);
+    k_density<kBatchedLoads><<<blocks, 128, 0, st>>>(
+        q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm, nb, d.stats,
+        d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc, d.mask_cap);
+  } else {
+    static unsigned blocks = 0;
+    if (!blocks) blocks = persistent_blocks(k_density<kPlainLoads>, d.sm_count);
+    k_density<kPlainLoads><<<blocks, 128, 0, st>>>(
+        q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm, nb, d.stats,
+        d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc, d.mask_cap);
+  }
   return cudaGetLastError();
 }
 
@@ -1079,14 +1108,19 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   TaskQueue q;
   cudaError_t e = prepare_queue(d, d.warp_order, false, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
-#define FS_SOLVE(P_, L_, R_)                                                                  \
+#define FS_SOLVE_B(P_, L_, R_, B_, Q_)                                                        \
   do {                                                                                        \
     static unsigned blocks = 0;                                                               \
-    if (!blocks) blocks = persistent_blocks(k_solve<P_, L_, R_>, d.sm_count);                \
-    k_solve<P_, L_, R_><<<blocks, 128, 0, st>>>(q, d.view(), d.s_pos, d.vel_x, d.anp,          \
-                                                d.cell_begin, xp_in, d.pterm[in], xp_out,     \
-                                                rho_out, d.pterm[out], d.pred_v, d.stats,     \
-                                                ap_out, d.mask_off, hit_out, hit_or);         \
+    if (!blocks) blocks = persistent_blocks(k_solve<P_, L_, R_, B_>, d.sm_count);            \
+    k_solve<P_, L_, R_, B_><<<blocks, 128, 0, st>>>(Q_, d.view(), d.s_pos, d.vel_x, d.anp,     \
+                                                    d.cell_begin, xp_in, d.pterm[in], xp_out, \
+                                                    rho_out, d.pterm[out], d.pred_v, d.stats, \
+                                                    ap_out, d.mask_off, hit_out, hit_or);     \
+  } while (0)
+#define FS_SOLVE(P_, L_, R_)                                 \
+  do {                                                       \
+    if (d.batched_loads) FS_SOLVE_B(P_, L_, R_, kBatchedLoads, q); \
+    else FS_SOLVE_B(P_, L_, R_, kPlainLoads, q);             \
   } while (0)
 #define FS_SOLVE_R(P_, L_)            \
   do {                                \
@@ -1099,6 +1133,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   else FS_SOLVE_R(true, false);
 #undef FS_SOLVE_R
 #undef FS_SOLVE
+#undef FS_SOLVE_B
   return cudaGetLastError();
 }
 
