@@ -736,6 +736,16 @@ int run_steps(FsSim *s, uint32_t nsteps) {
 }
 }  // namespace
 
+int fs_load_batching(FsSim *s, int *batched, int *decided) {
+  CHECK_SIM(s);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if ((rc = tune_decide(s))) return rc;
+  if (batched) *batched = s->batched_loads ? 1 : 0;
+  if (decided) *decided = s->tune_state == 2 ? 1 : 0;
+  return FS_OK;
+}
+
 int fs_prepare_steps(FsSim *s, uint32_t nsteps) {
   CHECK_SIM(s);
   int rc;

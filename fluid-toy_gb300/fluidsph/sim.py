@@ -141,6 +141,13 @@ class SphSimulation3DGrid:
         check(self._lib.fs_download_particles(self._h, out.ctypes.data, n))
         return out
 
+    def load_batching(self) -> tuple[bool, bool]:
+        """(batched candidate loads in use, choice measured yet): the density
+        and solve kernel form the simulation picked (fs_load_batching)."""
+        b, d = C.c_int(), C.c_int()
+        check(self._lib.fs_load_batching(self._h, C.byref(b), C.byref(d)))
+        return bool(b.value), bool(d.value)
+
     def export_particles_aos(self, device_ptr: int, count: int, sorted: bool = False,
                              scene: int = 0) -> None:
         """Write `count` 64-byte SphParticle3D records (canonical, or sorted

@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010052u
+#define FS_ABI_VERSION 0x00010053u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -327,6 +327,14 @@ int fs_step(FsSim *sim, uint32_t nsteps);
 /* No counterpart in the reference. Capture now the graphs a later
  * fs_step(sim, nsteps) uses, so that call only launches. */
 int fs_prepare_steps(FsSim *sim, uint32_t nsteps);
+/* Which form of the density and PCISPH-solve kernels the simulation runs:
+ * batched candidate loads (16 records in flight per lane) or the plain loop
+ * at higher occupancy. Both give the same bits; their speed depends on the
+ * workload, so once the simulation has run 8 steps its next four steps run
+ * both forms between events (whatever the fs_step call sizes), the next
+ * fs_step / fs_prepare_steps / fs_frames call waits for them once and the
+ * faster form is kept. decided = 0 until then (the plain form runs). */
+int fs_load_batching(FsSim *sim, int *batched, int *decided);
 
 /* update_* uploads, sph_3d_grid.rs:1446-1473. Ordered before later steps. */
 int fs_update_sph_params(FsSim *sim, const GpuSphParams3D *params);
