@@ -287,6 +287,7 @@ __device__ __forceinline__ void force_predict_one(
   const float near_k = P.near_stiffness, visc = P.viscosity, rho0 = P.rest_density;
   const float min_dist = h * 0.1f;
   const float y_min_dist = __frcp_rn(min_dist);
+  const bool min_dist_ok = rcp_den_ok(min_dist);
   const float3 pos_i = xyz(s_pos[s]);
   const float3 vel_i = xyz(vel_x[s]);
   const float2 di = s_dens[s];
@@ -328,11 +329,19 @@ __device__ __forceinline__ void force_predict_one(
     t.close = rr < min_dist;
     // normalize(pos_j - pos_i): its length is sqrt(dot(-r, -r)) == rr bit for
     // bit, so dividing by rr is the same operation sequence
-    // (pos_j - pos_i) / rr with one shared reciprocal, bit-identical
-    const float3 dv = pos_j - pos_i;
+    // (pos_j - pos_i) / rr with one shared reciprocal, bit-identical; and
+    // pos_j - pos_i is -r_vec exactly (IEEE subtraction is sign-symmetric).
+    // The three components and r / min_dist share one range check.
+    const float dvx = -r_vec.x, dvy = -r_vec.y, dvz = -r_vec.z;
     const float y_rr = __frcp_rn(rr);
-    const float3 dir_far = f3(div_by_rcp(dv.x, rr, y_rr), div_by_rcp(dv.y, rr, y_rr),
-                              div_by_rcp(dv.z, rr, y_rr));
+    float3 dir_far = f3(markstein(dvx, rr, y_rr), markstein(dvy, rr, y_rr),
+                        markstein(dvz, rr, y_rr));
+    float q_sep = markstein(rr, min_dist, y_min_dist);
+    if (!(min_dist_ok && rcp_den_ok(rr) && rcp_num_ok(rr) && rcp_num_ok(dvx) &&
+          rcp_num_ok(dvy) && rcp_num_ok(dvz))) {
+      dir_far = f3(dvx / rr, dvy / rr, dvz / rr);
+      q_sep = rr / min_dist;
+    }
     const int d = int(s) - int(j);
     const bool tabulated = d >= -dir_half && d <= dir_half;
     float3 dir_close = dir_far;
@@ -347,7 +356,7 @@ __device__ __forceinline__ void force_predict_one(
     const float grad = scale_g * dg * dg;
     t.p = (-mass * (near_pressure_i + near_pressure_j) /
            (2.0f * density_i * near_density_j)) * dir * grad;
-    const float sep = 200.0f * (1.0f - div_by_rcp(rr, min_dist, y_min_dist));
+    const float sep = 200.0f * (1.0f - q_sep);
     t.sep = (-sep) * dir;
     const float3 v_ij = vel_i - vel_j;
     const float v_dot_x = dot3(v_ij, r_vec);
@@ -468,8 +477,10 @@ __device__ __forceinline__ void solve_one(
       const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
       const float y_rr = __frcp_rn(rr);
       const float3 nr = -r_vec;
-      const float3 dir = f3(div_by_rcp(nr.x, rr, y_rr), div_by_rcp(nr.y, rr, y_rr),
-                            div_by_rcp(nr.z, rr, y_rr));
+      float3 dir = f3(markstein(nr.x, rr, y_rr), markstein(nr.y, rr, y_rr),
+                      markstein(nr.z, rr, y_rr));
+      if (!(rcp_den_ok(rr) && rcp_num_ok(nr.x) && rcp_num_ok(nr.y) && rcp_num_ok(nr.z)))
+        dir = f3(nr.x / rr, nr.y / rr, nr.z / rr);
       const float dg = h - rr;
       const float grad = scale_g * dg * dg;
       a_p = a_p + (-mass * (self_term + pt) * grad) * dir;
