@@ -21,6 +21,8 @@
 // three dx cells of a (dy,dz) row form ONE contiguous slot range
 // [begin[row+x0], begin[row+x1+1]): nine contiguous runs per particle, visited
 // in exactly the shaders' order.
+#include <type_traits>
+
 #include "sph_device.cuh"
 
 namespace fs {
@@ -313,32 +315,54 @@ __device__ __forceinline__ void force_predict_one(
     float3 v;    // viscosity term
     float3 c1;   // cohesion term
     float3 c2;   // normal-difference term
-    bool close, visc;
+    bool close, visc, ok;
   };
   auto load = [&](uint32_t j) {
     return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j), __ldg(nb_nrm + j)};
   };
-  auto terms = [&](uint32_t j, const Rec &q) {
+  // The pair's terms, with the correctly rounded fast reciprocal, square
+  // root and quotients (FAST; t.ok reports whether every operand was in
+  // their validated range) or with the IEEE operations.
+  auto terms_impl = [&](uint32_t j, const Rec &q, auto fast) {
+    constexpr bool FAST = decltype(fast)::value;
     Terms t;
+    bool ok = true;
+    auto div = [&](float a, float b) -> float {
+      if constexpr (FAST) {
+        ok = ok && fast_num_ok(a) && fast_ok(b);
+        return markstein(a, b, rcp_fast(b));
+      } else {
+        return a / b;
+      }
+    };
     const float3 pos_j = xyz(q.p);
     const float3 vel_j = xyz(q.v);
     const float3 n_j = xyz(q.n);
     const float3 r_vec = pos_i - pos_j;
     const float r_sq = dot3(r_vec, r_vec);
-    const float rr = sqrtf(r_sq);
+    float rr, y_rr;
+    if constexpr (FAST) {
+      ok = fast_ok(r_sq);
+      rr = sqrt_fast(r_sq);
+      ok = ok && fast_ok(rr);
+      y_rr = rcp_fast(rr);
+    } else {
+      rr = sqrtf(r_sq);
+      y_rr = __frcp_rn(rr);
+    }
     t.close = rr < min_dist;
     // normalize(pos_j - pos_i): its length is sqrt(dot(-r, -r)) == rr bit for
     // bit, so dividing by rr is the same operation sequence
     // (pos_j - pos_i) / rr with one shared reciprocal, bit-identical; and
     // pos_j - pos_i is -r_vec exactly (IEEE subtraction is sign-symmetric).
-    // The three components and r / min_dist share one range check.
     const float dvx = -r_vec.x, dvy = -r_vec.y, dvz = -r_vec.z;
-    const float y_rr = __frcp_rn(rr);
-    float3 dir_far = f3(markstein(dvx, rr, y_rr), markstein(dvy, rr, y_rr),
-                        markstein(dvz, rr, y_rr));
-    float q_sep = markstein(rr, min_dist, y_min_dist);
-    if (!(min_dist_ok && rcp_den_ok(rr) && rcp_num_ok(rr) && rcp_num_ok(dvx) &&
-          rcp_num_ok(dvy) && rcp_num_ok(dvz))) {
+    float3 dir_far;
+    float q_sep;
+    if constexpr (FAST) {
+      dir_far = f3(markstein(dvx, rr, y_rr), markstein(dvy, rr, y_rr), markstein(dvz, rr, y_rr));
+      q_sep = markstein(rr, min_dist, y_min_dist);
+      ok = ok && min_dist_ok && fast_num_ok(dvx) && fast_num_ok(dvy) && fast_num_ok(dvz);
+    } else {
       dir_far = f3(dvx / rr, dvy / rr, dvz / rr);
       q_sep = rr / min_dist;
     }
@@ -354,24 +378,32 @@ __device__ __forceinline__ void force_predict_one(
     const float near_pressure_j = near_k * near_density_j;
     const float dg = h - rr;
     const float grad = scale_g * dg * dg;
-    t.p = (-mass * (near_pressure_i + near_pressure_j) /
-           (2.0f * density_i * near_density_j)) * dir * grad;
+    t.p = div(-mass * (near_pressure_i + near_pressure_j), 2.0f * density_i * near_density_j) *
+          dir * grad;
     const float sep = 200.0f * (1.0f - q_sep);
     t.sep = (-sep) * dir;
     const float3 v_ij = vel_i - vel_j;
     const float v_dot_x = dot3(v_ij, r_vec);
-    const float mu = h * v_dot_x / (r_sq + 0.01f * h2);
+    const float mu = div(h * v_dot_x, r_sq + 0.01f * h2);
     const float avg_density = (density_i + density_j) * 0.5f;
-    const float pi_visc = -visc * mu / avg_density;
+    const float pi_visc = div(-visc * mu, avg_density);
     t.v = (-mass * pi_visc * grad) * dir;
     t.visc = v_dot_x < 0.0f;
-    const float K_ij = 2.0f * rho0 / (density_i + density_j);
+    const float K_ij = div(2.0f * rho0, density_i + density_j);
     const float r3 = rr * rr * rr;
     const float coh_far = scale_c * dg * dg * dg * r3;
     const float coh_near = scale_c * (2.0f * dg * dg * dg * r3 - P.kernel_radius_pow6 / 64.0f);
     const float coh = rr >= h * 0.5f ? coh_far : coh_near;
     t.c1 = (mass * K_ij * coh) * dir;
     t.c2 = (mass * K_ij) * (n_i - n_j);
+    t.ok = ok;
+    return t;
+  };
+  // the fast form, recomputed with IEEE operations when an operand is out of
+  // range (never on ordinary inputs: one rarely taken branch per pair)
+  auto terms = [&](uint32_t j, const Rec &q) {
+    Terms t = terms_impl(j, q, std::true_type{});
+    if (!t.ok) t = terms_impl(j, q, std::false_type{});
     return t;
   };
   auto add = [&](const Terms &t) {

@@ -15,7 +15,7 @@ import numpy as np
 
 from .build import LIB_PATH
 
-FS_ABI_VERSION = 0x00010053
+FS_ABI_VERSION = 0x00010054
 FS_OK = 0
 FS_STAGE_COUNT = 10
 FS_STAT_COUNT = 5
@@ -203,6 +203,7 @@ SIGNATURES = {
     "fs_prefix_scan_noalloc": (C.c_int, [_vp, _vp, _u32, _vp, _vp]),
     "fs_export_particles_aos": (C.c_int, [_vp, _u32, C.c_int, _vp, _u32]),
     "fs_load_batching": (C.c_int, [_vp, _P(C.c_int), _P(C.c_int)]),
+    "fs_selftest_arithmetic": (C.c_int, [C.c_int, _P(C.c_ulonglong)]),
     "fs_batch_create": (C.c_int, [_vp, _P(_u32), _u32, _vp, _vp, _vp, _u32, C.c_int, _u32,
                                   _P(_vp)]),
     "fs_batch_num_scenes": (C.c_int, [_vp, _P(_u32)]),

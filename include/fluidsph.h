@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010053u
+#define FS_ABI_VERSION 0x00010054u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -635,6 +635,20 @@ int fs_adj_backward(FsAdj *adj, float *dl_dpos0, float *dl_dvel0, int on_device,
 int fs_prefix_scan_noalloc(const uint32_t *cell_counts, uint32_t *cell_starts,
                            uint32_t total_cells, uint32_t *device_status,
                            void *stream);
+
+/* ---- arithmetic self-test ---------------------------------------------------
+ * No counterpart in the reference. The force and solve passes compute square
+ * roots, reciprocals and quotients from the hardware approximations
+ * (rsqrt.approx, rcp.approx) refined to the correctly rounded result, where
+ * every operand of a pair lies in [2^-60, 2^60), and with the IEEE operations
+ * otherwise; the results are the IEEE bits. This call re-checks that on
+ * `device`: results[0] = bit patterns (all 2^32) whose reciprocal differs
+ * from __frcp_rn, [1] = the same for the square root against sqrtf, [2] =
+ * quotients that differ from IEEE division on 2^32 pseudo-random operand pairs
+ * (half of them inside the fast range), [3] = how many of those pairs took the
+ * fast path. The first three are 0 on a device the library's parity claims
+ * hold for. Synchronous, tens of milliseconds. */
+int fs_selftest_arithmetic(int device, unsigned long long results[4]);
 
 #ifdef __cplusplus
 } /* extern "C" */
