@@ -167,7 +167,17 @@ __device__ __forceinline__ void density_one(
           const float r_sq = rx * rx + ry * ry + rz * rz;
           const bool hit = r_sq < h2;
           const bool ns = hit && r_sq > 1e-12f;
-          const float rr = sqrtf(r_sq);
+          float rr;
+          if constexpr (B > 1) {
+            // correctly rounded fast square root (the batched form only: it
+            // is what the clumped workloads that pick it gain from); r_sq = +0
+            // (coincident particles) gives +0 as sqrtf does; anything else
+            // outside the validated range takes sqrtf
+            rr = r_sq == 0.0f ? 0.0f : sqrt_fast(r_sq);
+            if (!(fast_ok(r_sq) || r_sq == 0.0f)) rr = sqrtf(r_sq);
+          } else {
+            rr = sqrtf(r_sq);
+          }
           const float diff = h2 - r_sq;
           const float td = mass * (scale_d * diff * diff * diff);
           const float dn = h - rr;
@@ -505,14 +515,19 @@ __device__ __forceinline__ void solve_one(
     // iteration (read only when there is pressure)
     const float self_term = HAS_PRESSURE ? pterm_in[s] : 0.0f;
     auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
-      const float rr = sqrtf(r_sq);
       const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
-      const float y_rr = __frcp_rn(rr);
       const float3 nr = -r_vec;
+      // correctly rounded fast square root, reciprocal and quotients, one
+      // range check for the pair (IEEE operations outside it)
+      float rr = sqrt_fast(r_sq);
+      const float y_rr = rcp_fast(rr);
       float3 dir = f3(markstein(nr.x, rr, y_rr), markstein(nr.y, rr, y_rr),
                       markstein(nr.z, rr, y_rr));
-      if (!(rcp_den_ok(rr) && rcp_num_ok(nr.x) && rcp_num_ok(nr.y) && rcp_num_ok(nr.z)))
+      if (!(fast_ok(r_sq) && fast_ok(rr) && fast_num_ok(nr.x) && fast_num_ok(nr.y) &&
+            fast_num_ok(nr.z))) {
+        rr = sqrtf(r_sq);
         dir = f3(nr.x / rr, nr.y / rr, nr.z / rr);
+      }
       const float dg = h - rr;
       const float grad = scale_g * dg * dg;
       a_p = a_p + (-mass * (self_term + pt) * grad) * dir;
