@@ -111,6 +111,15 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.pred_rho[1] = c.take<float>(M);
   d.pterm[0] = c.take<float>(M);
   d.pterm[1] = c.take<float>(M);
+  d.rep_of = c.take<uint32_t>(M);
+  d.dd_list = c.take<uint32_t>(M);
+  d.dd_warp = c.take<uint32_t>((M + 31) / 32 + 1);
+  d.dd_count = c.take<uint32_t>(1);
+  d.dd_bucket = c.take<uint8_t>((M + 31) / 32);
+  d.dd_order = c.take<uint32_t>((M + 31) / 32);
+  d.dd_hist = c.take<uint32_t>(2 * 33);
+  d.dens_cand = c.take<uint32_t>(M);
+  d.dens_hits = c.take<uint32_t>(M);
   d.pred_v = c.take<float4>(M);
   d.cell_of = c.take<uint32_t>(M);
   d.rank_of = c.take<uint32_t>(M);

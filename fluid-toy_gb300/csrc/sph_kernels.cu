@@ -107,6 +107,7 @@ __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, 
 // once per particle instead of once per pair.
 struct NbrRecords {
   float4 *pos, *vel, *nrm;
+  uint32_t *hits;  // per slot: pairs with r^2 < h^2 (statistics of dedupe copies)
 };
 
 __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int dir_half) {
@@ -199,6 +200,7 @@ __device__ __forceinline__ void density_one(
       }
     }
     mask_hits[s] = nonself;
+    nb.hits[s] = hits;
     const float gamma = boundary_gamma(U->geom, h, pos_i);
     density = density / gamma;
     const float h8 = P.kernel_radius_pow6 * h * h;
@@ -653,7 +655,7 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(256)
     k_scatter_order(SceneView v, const uint8_t *__restrict__ warp_bucket,
                     const uint32_t *__restrict__ hist, uint32_t *__restrict__ cursor,
-                    uint32_t *__restrict__ order) {
+                    uint32_t *__restrict__ order, const uint32_t *__restrict__ count) {
   __shared__ uint32_t base[ORDER_BUCKETS];
   if (threadIdx.x == 0) {
     uint32_t acc = 0u;
@@ -664,7 +666,7 @@ __global__ void __launch_bounds__(256)
   }
   __syncthreads();
   const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= (v.b->n_sorted + 31u) / 32u) return;
+  if (w >= ((count ? *count : v.b->n_sorted) + 31u) / 32u) return;
   const uint32_t b = warp_bucket[w];
   order[base[b] + atomicAdd(&cursor[b], 1u)] = w;
 }
@@ -725,6 +727,139 @@ __global__ void __launch_bounds__(256)
   if (int(lane) == leader) pos = atomicAdd(&cursor[k], uint32_t(__popc(peers)));
   pos = __shfl_sync(peers, pos, leader);
   perm[base[k] + pos + uint32_t(__popc(peers & ((1u << lane) - 1u)))] = s;
+}
+
+// ---- density dedupe ------------------------------------------------------------
+// Particles at bit-identical positions (and of the same scene) have the same
+// candidate runs and the same r^2 to every candidate, so their density, near
+// density, normal, hit mask and neighbour records are identical: the density
+// pass computes one representative per group and copies the rest. Groups are
+// found inside each 32-slot warp (__match_any_sync on the position bits) and
+// the representatives of all warps are compacted in slot order into tasks of
+// 32, heaviest first. Over-compressed starts clamp thousands of particles to
+// the same wall corner coordinates (the 1M-particle dam break: ~57,000
+// particles in such groups, 28% of the pass's candidate tests).
+__global__ void __launch_bounds__(256)
+    k_dedupe_mark(SceneView v, const float4 *__restrict__ s_pos, uint32_t *__restrict__ rep_of,
+                  uint32_t *__restrict__ warp_reps) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t n = v.b->n_sorted;
+  const bool active = s < n;
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  bool is_rep = false;
+  if (active) {
+    const float4 p = s_pos[s];
+    const unsigned m = __match_any_sync(act, __float_as_uint(p.x)) &
+                       __match_any_sync(act, __float_as_uint(p.y)) &
+                       __match_any_sync(act, __float_as_uint(p.z)) &
+                       __match_any_sync(act, uint32_t(v.scene_of_slot[s]));
+    const int leader = __ffs(m) - 1;
+    rep_of[s] = (s & ~31u) + uint32_t(leader);
+    is_rep = int(lane) == leader;
+  }
+  const unsigned reps = __ballot_sync(0xffffffffu, is_rep);
+  if (lane == 0u && (s >> 5) < (n + 31u) / 32u) warp_reps[s >> 5] = uint32_t(__popc(reps));
+}
+
+// Exclusive scan of the per-warp representative counts (one block); the
+// total goes to *count.
+__global__ void __launch_bounds__(1024)
+    k_dd_scan(uint32_t *__restrict__ warp_reps, uint32_t nwarps, uint32_t *__restrict__ count) {
+  __shared__ uint32_t part[1024];
+  const uint32_t t = threadIdx.x;
+  const uint32_t per = (nwarps + 1023u) / 1024u;
+  const uint32_t lo = min(t * per, nwarps), hi = min(lo + per, nwarps);
+  uint32_t sum = 0u;
+  for (uint32_t i = lo; i < hi; i++) sum += warp_reps[i];
+  part[t] = sum;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024u; off <<= 1) {
+    const uint32_t add = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += add;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - sum;
+  for (uint32_t i = lo; i < hi; i++) {
+    const uint32_t c = warp_reps[i];
+    warp_reps[i] = run;
+    run += c;
+  }
+  if (t == 1023u) *count = part[1023];
+}
+
+__global__ void __launch_bounds__(256)
+    k_dedupe_list(SceneView v, const uint32_t *__restrict__ rep_of,
+                  const uint32_t *__restrict__ warp_base, uint32_t *__restrict__ list) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31u;
+  const bool is_rep = s < v.b->n_sorted && rep_of[s] == s;
+  const unsigned reps = __ballot_sync(0xffffffffu, is_rep);
+  if (is_rep)
+    list[warp_base[s >> 5] + uint32_t(__popc(reps & ((1u << lane) - 1u)))] = s;
+}
+
+// Task buckets of the compacted list (k_warp_work over list entries); also
+// records each representative's candidate count.
+__global__ void __launch_bounds__(256)
+    k_list_work(SceneView v, const float4 *__restrict__ s_pos, const uint32_t *__restrict__ begin,
+                const uint32_t *__restrict__ list, const uint32_t *__restrict__ count,
+                uint32_t *__restrict__ cand, uint8_t *__restrict__ task_bucket,
+                uint32_t *__restrict__ hist) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t entries = *count;
+  uint32_t total = 0u;
+  const bool active = i < entries;
+  if (active) {
+    const uint32_t s = list[i];
+    const DevUniforms *U = v.u + v.scene_of_slot[s];
+    Runs R;
+    neighbor_runs(xyz(s_pos[s]), U->grid, begin + U->c_offset, R);
+    total = R.total;
+    cand[s] = total;
+  }
+  const uint32_t m = __reduce_max_sync(0xffffffffu, total);
+  if ((threadIdx.x & 31u) == 0u && active) {
+    const uint32_t b = 32u - uint32_t(__clz(m));
+    task_bucket[i >> 5] = uint8_t(b);
+    atomicAdd(&hist[b], 1u);
+  }
+}
+
+// The copies: each slot that is not a representative takes its
+// representative's results (its own pre-XSPH velocity in its record) and adds
+// the representative's pair counts to the statistics.
+__global__ void __launch_bounds__(256)
+    k_dedupe_copy(SceneView v, const uint32_t *__restrict__ rep_of, const float4 *__restrict__ s_vel,
+                  float2 *__restrict__ s_dens, float4 *__restrict__ s_nrm, NbrRecords nb,
+                  uint32_t *__restrict__ mask_off, uint32_t *__restrict__ mask_hits,
+                  const uint32_t *__restrict__ cand, unsigned long long *__restrict__ stats) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t c = 0u, h = 0u, ns = 0u;
+  if (s < v.b->n_sorted) {
+    const uint32_t r = rep_of[s];
+    if (r != s) {
+      s_dens[s] = s_dens[r];
+      s_nrm[s] = s_nrm[r];
+      nb.pos[s] = nb.pos[r];
+      nb.nrm[s] = nb.nrm[r];
+      const float4 vs = s_vel[s];
+      nb.vel[s] = make_float4(vs.x, vs.y, vs.z, nb.vel[r].w);
+      mask_off[s] = mask_off[r];
+      ns = mask_hits[r];
+      mask_hits[s] = ns;
+      h = nb.hits[r];
+      nb.hits[s] = h;
+      c = cand[r];
+    }
+  }
+  const unsigned long long cs = warp_sum_u64(c), hs = warp_sum_u64(h), nss = warp_sum_u64(ns);
+  if ((threadIdx.x & 31u) == 0u && cs) {
+    atomicAdd(stats + STAT_CAND_DENSITY, cs);
+    atomicAdd(stats + STAT_HIT_DENSITY, hs);
+    atomicAdd(stats + STAT_HIT_NONSELF, nss);
+  }
 }
 
 template <int B>
@@ -1090,7 +1225,7 @@ cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st) {
   const uint32_t nwarps = (n + 31u) / 32u;
   k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(d.view(), d.warp_bucket, d.order_hist,
                                                            d.order_hist + ORDER_BUCKETS,
-                                                           d.warp_order);
+                                                           d.warp_order, nullptr);
   return cudaGetLastError();
 }
 
@@ -1106,10 +1241,31 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d.mask_alloc, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
+  // dedupe, except while recording for the reverse pass (the recorded PCISPH
+  // levels write per-particle masks at the density mask's offsets, which
+  // copies would share)
+  const bool dedupe = d.rec_hits == nullptr;
+  const uint32_t nwarps = (n + 31u) / 32u;
   TaskQueue q;
-  e = prepare_queue(d, d.warp_order, false, n, TASK_COUNTERS - 1, st, &q);
+  if (dedupe) {
+    k_dedupe_mark<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.rep_of, d.dd_warp);
+    k_dd_scan<<<1, 1024, 0, st>>>(d.dd_warp, nwarps, d.dd_count);
+    k_dedupe_list<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.rep_of, d.dd_warp, d.dd_list);
+    e = cudaMemsetAsync(d.dd_hist, 0, sizeof(uint32_t) * 2 * ORDER_BUCKETS, st);
+    if (e != cudaSuccess) return e;
+    k_list_work<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.cell_begin, d.dd_list,
+                                                    d.dd_count, d.dens_cand, d.dd_bucket,
+                                                    d.dd_hist);
+    k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(
+        d.view(), d.dd_bucket, d.dd_hist, d.dd_hist + ORDER_BUCKETS, d.dd_order, d.dd_count);
+    e = prepare_queue(d, d.dd_order, false, n, TASK_COUNTERS - 1, st, &q);
+    q.list = d.dd_list;
+    q.count = d.dd_count;
+  } else {
+    e = prepare_queue(d, d.warp_order, false, n, TASK_COUNTERS - 1, st, &q);
+  }
   if (e != cudaSuccess) return e;
-  const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm};
+  const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm, d.dens_hits};
   if (d.batched_loads) {
     static unsigned blocks = 0;
     if (!blocks) blocks = persistent_blocks(k_density<kBatchedLoads>, d.sm_count);
@@ -1123,6 +1279,10 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
         q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm, nb, d.stats,
         d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc, d.mask_cap);
   }
+  if (dedupe)
+    k_dedupe_copy<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.rep_of, d.s_vel, d.s_dens,
+                                                      d.s_nrm, nb, d.mask_off, d.mask_hits,
+                                                      d.dens_cand, d.stats);
   return cudaGetLastError();
 }
 

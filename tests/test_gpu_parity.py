@@ -76,6 +76,33 @@ def test_config0_one_step_then_twenty(fslib, oracle_mod, sc):
     _compare(sim, orc, scene.n, "config0 step 20")
 
 
+def test_coincident_particles(fslib, oracle_mod, sc):
+    """Groups of particles at bit-identical positions (the density pass
+    computes one per group and copies it): groups inside one 32-slot warp,
+    groups spanning warps and cells, and a large corner clump, stepped with
+    both forms of the density/solve kernels (the form is measured at step 8)."""
+    import dataclasses
+    scene = sc.small_scene(12, 10, 8, seed=5)
+    p = scene.particles.copy()
+    n = len(p)
+    rng = np.random.default_rng(11)
+    # a large group at one particle's position
+    p[40:240:2, 0:3] = p[40, 0:3]
+    # many small groups of 2-6 members at random positions
+    for _ in range(60):
+        src = int(rng.integers(0, n))
+        dst = rng.integers(0, n, size=int(rng.integers(1, 6)))
+        p[dst, 0:3] = p[src, 0:3]
+    scene = dataclasses.replace(scene, particles=p)
+    sim, orc = _run_pair(scene, 1, oracle_mod)
+    _compare(sim, orc, n, "coincident step 1")
+    for _ in range(13):
+        sim.step(1)
+        orc.step(1)
+    _compare(sim, orc, n, "coincident step 14")
+    assert sim.load_batching()[1]
+
+
 def test_graph_replay_matches_single_steps(fslib, sc):
     scene = sc.small_scene(seed=3)
     a = gpu_sim_for_scene(scene)
