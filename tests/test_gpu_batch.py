@@ -176,3 +176,35 @@ def test_full_ensemble_sampled_scenes(sc):
     for k in pick:
         sims[k].step(3)
         _compare_scene(b, k, sims[k], f"ensemble scene {k} ({scenes[k].n} particles)")
+
+
+def test_batch_coincident_particles(sc):
+    """Scenes with groups of bit-identical positions (the density pass
+    computes one per group and copies it), including the same coordinates in
+    two scenes whose slots share a 32-slot warp at the scene boundary: each
+    scene equals its plain simulation bit for bit."""
+    import dataclasses
+    rng = np.random.default_rng(7)
+    scenes = []
+    for k, (nx, ny, nz) in enumerate([(9, 7, 5), (8, 8, 6)]):
+        s = sc.small_scene(nx, ny, nz, seed=20 + k)
+        p = s.particles.copy()
+        n = len(p)
+        p[10:120:3, 0:3] = p[10, 0:3]
+        for _ in range(30):
+            src = int(rng.integers(0, n))
+            p[rng.integers(0, n, size=int(rng.integers(1, 5))), 0:3] = p[src, 0:3]
+        scenes.append(dataclasses.replace(s, particles=p))
+    # the second scene's first particles at the first scene's group position
+    scenes[1].particles[0:8, 0:3] = scenes[0].particles[10, 0:3]
+    b = _batch_for(scenes)
+    plains = [_plain_for(s) for s in scenes]
+    for steps in (1, 13):
+        b.step(steps)
+        for sim in plains:
+            sim.step(steps)
+        for k, sim in enumerate(plains):
+            _compare_scene(b, k, sim, f"scene {k} after {steps}")
+    b.close()
+    for sim in plains:
+        sim.close()
