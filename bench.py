@@ -40,6 +40,16 @@ METRIC = "particle-steps/s"
 # and keeps the faster (same results either way); warm-ups run past that, so
 # timed regions use the chosen kernels (the reported warm-up is the count run).
 WARMUP_PAST_TUNING = 16
+
+
+def kernels_per_step(iterations: int) -> int:
+    """Kernel launches of one step without rigid-body coupling: hash, scan,
+    scatter, sort/gather, warp work + order (2), density dedupe (mark, scan,
+    list, list work, order: 5), density, dedupe copy, hit keys, key bases,
+    key scatter, XSPH, force + predict, one solve per PCISPH iteration and
+    finalize + integrate. The grid clear is a memset, not counted."""
+    return 20 + iterations
+
 # algorithmic bytes per particle-step and per stage (SoA, compulsory traffic)
 STAGE_BYTES = {"hash": 16, "reorder": 60, "density": 32, "xsph": 40, "force_predict": 68 + 68,
                "pcisph_solve": 100, "finalize_integrate": 48 + 48}
@@ -379,7 +389,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                 "d2h_bytes_per_step": d2h,
                 "pattern": "per step: upload sph/geometry/gravity/rigid-body structs, "
                            "fs_step(1), read rigid-body accumulator (sync)"},
-        "gpu_launches": K * (13 + scene.iterations),
+        "gpu_launches": K * kernels_per_step(scene.iterations),
         "clocks": clk,
     }
     if forms is not None:
@@ -479,7 +489,7 @@ def run_batch(args, dist: Dist) -> dict | None:
                          "pattern": "one SphSimulation3DGrid per scene on one stream, "
                                     "each fs_step(k) graph-replayed, scene after scene"},
         "batched_over_looped": round(value / loop_value, 3) if loop_value else None,
-        "gpu_launches": K * (13 + scenes[0].iterations),
+        "gpu_launches": K * kernels_per_step(scenes[0].iterations),
         "clocks": clk,
     }
 
