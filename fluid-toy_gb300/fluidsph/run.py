@@ -1,11 +1,18 @@
 """Headless runner: step one of the seeded workloads through the C ABI.
 
-    python fluid-toy_gb300/fluidsph/run.py --config 1 --steps 12 [--graph]
+    python fluid-toy_gb300/fluidsph/run.py --config 1 --steps 12 [--graph] [--warmup 16]
+    python fluid-toy_gb300/fluidsph/run.py --batch --steps 10 --warmup 16
     python fluid-toy_gb300/fluidsph/run.py --identify --iterations 2
 
 Each step is one fs_step(sim, 1) call (one launch per kernel, the form that
 profilers can address launch by launch) unless --graph replays them as one
-captured graph. Prints the particle count, steps and wall time.
+captured graph. Prints the particle count, steps and wall time. --warmup
+steps run first (a simulation measures its two density/solve kernel forms on
+its steps 8-11 and keeps the faster from then on); the measured steps run
+inside the NVTX range `steps` (when torch is importable).
+
+--batch runs the 256-scene ensemble of scenes.config2 as one SphBatch3DGrid
+(one launch per stage for all scenes) instead of a single scene.
 
 --identify runs the batched parameter-identification workload instead (the
 64 scenes of scenes.config4 as one batch, 150 steps, checkpoint every 15;
@@ -92,11 +99,32 @@ def identify(iterations: int, steps: int = 150, every: int = 15, num_scenes: int
     b.close()
 
 
+def run_steps(sim, steps: int, warmup: int, graph: bool) -> float:
+    """Warm-up steps, then `steps` steps inside the NVTX range `steps`; returns
+    the wall seconds of the measured steps."""
+    if warmup:
+        sim.step(warmup)
+    sim.sync()
+    nv = _Ranges()
+    t0 = time.perf_counter()
+    nv.push("steps")
+    if graph:
+        sim.step(steps)
+    else:
+        for _ in range(steps):
+            sim.step(1)
+    sim.sync()
+    nv.pop()
+    return time.perf_counter() - t0
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", type=int, default=0, choices=sorted(scenes.CONFIGS))
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--graph", action="store_true")
+    ap.add_argument("--warmup", type=int, default=0)
+    ap.add_argument("--batch", action="store_true", help="the 256-scene batched ensemble")
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--identify", action="store_true")
     ap.add_argument("--iterations", type=int, default=2)
@@ -107,20 +135,28 @@ def main(argv=None) -> int:
     if a.identify:
         identify(a.iterations, a.rollout_steps, a.every, a.scenes, device=a.device)
         return 0
+    if a.batch:
+        from fluidsph.sim import SphBatch3DGrid
+
+        scs = scenes.config2()
+        b = SphBatch3DGrid([s.particles for s in scs], [s.sph for s in scs],
+                           [s.geom for s in scs], device=a.device)
+        for k, s in enumerate(scs):
+            b.update_scene(k, gravity=s.gravity)
+        b.set_pcisph_iterations(scs[0].iterations)
+        secs = run_steps(b, a.steps, a.warmup, a.graph)
+        print(f"batched ensemble: {len(scs)} scenes, {sum(s.n for s in scs)} particles, "
+              f"{a.steps} steps, {secs:.3f} s")
+        b.close()
+        return 0
     sc = scenes.CONFIGS[a.config]()
     sim = SphSimulation3DGrid(sc.particles, sc.sph, sc.geom, device=a.device)
     sim.update_gravity(sc.gravity)
     sim.set_pcisph_iterations(sc.iterations)
     if sc.rigid is not None:
         sim.update_rigid_body(sc.rigid)
-    t0 = time.perf_counter()
-    if a.graph:
-        sim.step(a.steps)
-    else:
-        for _ in range(a.steps):
-            sim.step(1)
-    sim.sync()
-    print(f"{sc.name}: {sc.n} particles, {a.steps} steps, {time.perf_counter() - t0:.3f} s")
+    secs = run_steps(sim, a.steps, a.warmup, a.graph)
+    print(f"{sc.name}: {sc.n} particles, {a.steps} steps, {secs:.3f} s")
     sim.close()
     return 0
 
