@@ -47,8 +47,9 @@ def kernels_per_step(iterations: int) -> int:
     scatter, sort/gather, warp work + order (2), density dedupe (mark, scan,
     list, list work, order: 5), density, dedupe copy, hit keys, key bases,
     key scatter, XSPH, force + predict, one solve per PCISPH iteration and
-    finalize + integrate. The grid clear is a memset, not counted."""
-    return 20 + iterations
+    finalize + integrate: 19 + iterations. The grid clear is a memset, not
+    counted."""
+    return 19 + iterations
 
 # algorithmic bytes per particle-step and per stage (SoA, compulsory traffic)
 STAGE_BYTES = {"hash": 16, "reorder": 60, "density": 32, "xsph": 40, "force_predict": 68 + 68,
