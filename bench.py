@@ -51,6 +51,7 @@ def kernels_per_step(iterations: int) -> int:
     counted."""
     return 19 + iterations
 
+
 # algorithmic bytes per particle-step and per stage (SoA, compulsory traffic)
 STAGE_BYTES = {"hash": 16, "reorder": 60, "density": 32, "xsph": 40, "force_predict": 68 + 68,
                "pcisph_solve": 100, "finalize_integrate": 48 + 48}
