@@ -84,12 +84,13 @@ struct DevState {
   // density dedupe (particles at bit-identical positions within a 32-slot warp)
   uint32_t *rep_of;     // representative slot of each sorted slot
   uint32_t *dd_list;    // representatives, compacted in slot order
-  uint32_t *dd_warp;    // per 32-slot warp: representatives, then exclusive bases
-  uint32_t *dd_count;   // representatives in dd_list
+  uint32_t *dd_warp;    // per 32-slot warp: representatives
+  uint32_t *dd_incl;    // inclusive scan of dd_warp (the last entry: size of dd_list)
+  unsigned long long *dd_tiles;  // scan descriptors for dd_incl + ticket word
   uint8_t *dd_bucket;   // per 32-entry task of dd_list: candidate bucket
   uint32_t *dd_order;   // tasks of dd_list, heaviest first
   uint32_t *dd_hist;    // bucket histogram + cursors
-  uint32_t *dens_cand;  // candidates of each representative (statistics of its copies)
+  uint32_t *dens_cand;  // candidates of each sorted slot (k_warp_work)
   uint32_t *dens_hits;  // its pairs with r^2 < h^2
   float4 *anp;      // non-pressure acceleration a_np
   float4 *pred_xp[2];  // predicted position, pressure (ping-pong)

@@ -114,7 +114,8 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.rep_of = c.take<uint32_t>(M);
   d.dd_list = c.take<uint32_t>(M);
   d.dd_warp = c.take<uint32_t>((M + 31) / 32 + 1);
-  d.dd_count = c.take<uint32_t>(1);
+  d.dd_incl = c.take<uint32_t>((M + 31) / 32 + 1);
+  d.dd_tiles = c.take<unsigned long long>(scan_tiles((M + 31) / 32) + 1);
   d.dd_bucket = c.take<uint8_t>((M + 31) / 32);
   d.dd_order = c.take<uint32_t>((M + 31) / 32);
   d.dd_hist = c.take<uint32_t>(2 * 33);

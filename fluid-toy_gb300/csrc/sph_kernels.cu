@@ -626,23 +626,49 @@ __device__ __forceinline__ uint32_t work_key(uint32_t c) {
   return c < 4096u ? c : 4096u + min((c - 4096u) >> 4, 4095u);
 }
 
-// Count a key with warp-aggregated atomics; returns nothing.
-__device__ __forceinline__ void count_key(bool active, uint32_t k, uint32_t *hist) {
+// The hit-count keys are histogrammed and scattered per block of KEY_CHUNK
+// slots in shared memory (a bucket receives one global atomic per block):
+// most particles share a few hundred hit counts, and per-warp global atomics
+// on those buckets serialised (4.35M slots of the 256-scene ensemble: 0.26 ms
+// per kernel).
+constexpr unsigned KEY_THREADS = 1024, KEY_ITEMS = 8, KEY_CHUNK = KEY_THREADS * KEY_ITEMS;
+
+// Adds 1 to h[k] for every active lane, warp-aggregated; returns the lane's
+// rank among all additions to h[k] (the old value plus its rank among the
+// warp's lanes with the same key).
+__device__ __forceinline__ uint32_t shared_rank(bool active, uint32_t k, uint32_t *h) {
   const unsigned act = __ballot_sync(0xffffffffu, active);
-  if (!active) return;
+  if (!active) return 0u;
   const unsigned peers = __match_any_sync(act, k);
-  if (int(threadIdx.x & 31u) == __ffs(peers) - 1) atomicAdd(&hist[k], uint32_t(__popc(peers)));
+  const int leader = __ffs(peers) - 1;
+  const unsigned lane = threadIdx.x & 31u;
+  uint32_t old = 0u;
+  if (int(lane) == leader) old = atomicAdd(&h[k], uint32_t(__popc(peers)));
+  old = __shfl_sync(peers, old, leader);
+  return old + uint32_t(__popc(peers & ((1u << lane) - 1u)));
+}
+
+// Adds a block's bucket counts (shared) to the global histogram, one atomic
+// per non-empty bucket; all threads of the block call it.
+template <int NB>
+__device__ __forceinline__ void flush_buckets(const uint32_t (&h)[NB], uint32_t *hist) {
+  __syncthreads();
+  if (threadIdx.x < unsigned(NB) && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
 }
 
 // Task order, heaviest first: k_warp_work puts every warp (32 sorted slots)
 // in a bucket floor(log2(max candidates of its particles)) + 1 and counts the
 // buckets; k_scatter_order writes the warps bucket by bucket, heaviest bucket
-// first (the order inside a bucket is immaterial).
+// first (the order inside a bucket is immaterial). k_warp_work also keeps
+// each slot's candidate count (the density dedupe's tasks and statistics).
 constexpr int ORDER_BUCKETS = 33;
 __global__ void __launch_bounds__(256)
     k_warp_work(SceneView v, const float4 *__restrict__ s_pos,
                 const uint32_t *__restrict__ begin, uint8_t *__restrict__ warp_bucket,
-                uint32_t *__restrict__ hist) {
+                uint32_t *__restrict__ hist, uint32_t *__restrict__ cand) {
+  __shared__ uint32_t h[ORDER_BUCKETS];
+  if (threadIdx.x < unsigned(ORDER_BUCKETS)) h[threadIdx.x] = 0u;
+  __syncthreads();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t total = 0u;
   const bool active = s < v.b->n_sorted;
@@ -651,20 +677,24 @@ __global__ void __launch_bounds__(256)
     Runs R;
     neighbor_runs(xyz(s_pos[s]), U->grid, begin + U->c_offset, R);
     total = R.total;
+    cand[s] = total;
   }
   const uint32_t m = __reduce_max_sync(0xffffffffu, total);
   if ((threadIdx.x & 31u) == 0u && active) {
     const uint32_t b = 32u - uint32_t(__clz(m));
     warp_bucket[s >> 5] = uint8_t(b);
-    atomicAdd(&hist[b], 1u);
+    atomicAdd(&h[b], 1u);
   }
+  flush_buckets(h, hist);
 }
 
+// Each block ranks its warps per bucket in shared memory and reserves one
+// range per bucket with a global atomic.
 __global__ void __launch_bounds__(256)
     k_scatter_order(SceneView v, const uint8_t *__restrict__ warp_bucket,
                     const uint32_t *__restrict__ hist, uint32_t *__restrict__ cursor,
                     uint32_t *__restrict__ order, const uint32_t *__restrict__ count) {
-  __shared__ uint32_t base[ORDER_BUCKETS];
+  __shared__ uint32_t base[ORDER_BUCKETS], local[ORDER_BUCKETS];
   if (threadIdx.x == 0) {
     uint32_t acc = 0u;
     for (int b = ORDER_BUCKETS - 1; b >= 0; b--) {
@@ -672,24 +702,43 @@ __global__ void __launch_bounds__(256)
       acc += hist[b];
     }
   }
+  if (threadIdx.x < unsigned(ORDER_BUCKETS)) local[threadIdx.x] = 0u;
   __syncthreads();
   const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= ((count ? *count : v.b->n_sorted) + 31u) / 32u) return;
-  const uint32_t b = warp_bucket[w];
-  order[base[b] + atomicAdd(&cursor[b], 1u)] = w;
+  const bool active = w < ((count ? *count : v.b->n_sorted) + 31u) / 32u;
+  const uint32_t b = active ? uint32_t(warp_bucket[w]) : 0u;
+  const uint32_t r = shared_rank(active, b, local);
+  __syncthreads();
+  if (threadIdx.x < unsigned(ORDER_BUCKETS) && local[threadIdx.x])
+    local[threadIdx.x] = atomicAdd(&cursor[threadIdx.x], local[threadIdx.x]);
+  __syncthreads();
+  if (active) order[base[b] + local[b] + r] = w;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(KEY_THREADS)
     k_hit_keys(SceneView v, const uint32_t *__restrict__ mask_hits, uint16_t *__restrict__ key,
                uint32_t *__restrict__ hist) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = s < v.b->n_sorted;
-  uint32_t k = 0u;
-  if (active) {
-    k = work_key(mask_hits[s]);
-    key[s] = uint16_t(k);
+  __shared__ uint32_t h[KEY_BUCKETS];
+  for (unsigned i = threadIdx.x; i < unsigned(KEY_BUCKETS); i += KEY_THREADS) h[i] = 0u;
+  __syncthreads();
+  const uint32_t n = v.b->n_sorted;
+  const uint32_t first = blockIdx.x * KEY_CHUNK + threadIdx.x;
+  uint32_t hits[KEY_ITEMS];
+#pragma unroll
+  for (unsigned k = 0; k < KEY_ITEMS; k++) {
+    const uint32_t s = first + k * KEY_THREADS;
+    hits[k] = s < n ? mask_hits[s] : 0u;
   }
-  count_key(active, k, hist);
+#pragma unroll
+  for (unsigned k = 0; k < KEY_ITEMS; k++) {
+    const uint32_t s = first + k * KEY_THREADS;
+    const uint32_t c = work_key(hits[k]);
+    if (s < n) key[s] = uint16_t(c);
+    shared_rank(s < n, c, h);
+  }
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < unsigned(KEY_BUCKETS); i += KEY_THREADS)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
 // Exclusive bases of the key buckets, heaviest bucket first (one block).
@@ -720,21 +769,36 @@ __global__ void __launch_bounds__(1024) k_key_bases(const uint32_t *__restrict__
   }
 }
 
-__global__ void __launch_bounds__(256)
+// Each block ranks its slots per key in shared memory, reserves one range
+// per key with a global atomic, then writes its slots (the order inside a
+// key is immaterial).
+__global__ void __launch_bounds__(KEY_THREADS)
     k_key_scatter(SceneView v, const uint16_t *__restrict__ key, const uint32_t *__restrict__ base,
                   uint32_t *__restrict__ cursor, uint32_t *__restrict__ perm) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = s < v.b->n_sorted;
-  const uint32_t k = active ? key[s] : 0u;
-  const unsigned act = __ballot_sync(0xffffffffu, active);
-  if (!active) return;
-  const unsigned peers = __match_any_sync(act, k);
-  const int leader = __ffs(peers) - 1;
-  const unsigned lane = threadIdx.x & 31u;
-  uint32_t pos = 0u;
-  if (int(lane) == leader) pos = atomicAdd(&cursor[k], uint32_t(__popc(peers)));
-  pos = __shfl_sync(peers, pos, leader);
-  perm[base[k] + pos + uint32_t(__popc(peers & ((1u << lane) - 1u)))] = s;
+  __shared__ uint32_t h[KEY_BUCKETS];
+  for (unsigned i = threadIdx.x; i < unsigned(KEY_BUCKETS); i += KEY_THREADS) h[i] = 0u;
+  __syncthreads();
+  const uint32_t n = v.b->n_sorted;
+  const uint32_t first = blockIdx.x * KEY_CHUNK + threadIdx.x;
+  uint32_t kk[KEY_ITEMS], rank[KEY_ITEMS];
+#pragma unroll
+  for (unsigned k = 0; k < KEY_ITEMS; k++) {
+    const uint32_t s = first + k * KEY_THREADS;
+    kk[k] = s < n ? uint32_t(key[s]) : 0u;
+  }
+#pragma unroll
+  for (unsigned k = 0; k < KEY_ITEMS; k++) rank[k] = shared_rank(first + k * KEY_THREADS < n, kk[k], h);
+  __syncthreads();
+  for (unsigned i = threadIdx.x; i < unsigned(KEY_BUCKETS); i += KEY_THREADS) {
+    const uint32_t c = h[i];
+    if (c) h[i] = base[i] + atomicAdd(&cursor[i], c);
+  }
+  __syncthreads();
+#pragma unroll
+  for (unsigned k = 0; k < KEY_ITEMS; k++) {
+    const uint32_t s = first + k * KEY_THREADS;
+    if (s < n) perm[h[kk[k]] + rank[k]] = s;
+  }
 }
 
 // ---- density dedupe ------------------------------------------------------------
@@ -770,69 +834,38 @@ __global__ void __launch_bounds__(256)
   if (lane == 0u && (s >> 5) < (n + 31u) / 32u) warp_reps[s >> 5] = uint32_t(__popc(reps));
 }
 
-// Exclusive scan of the per-warp representative counts (one block); the
-// total goes to *count.
-__global__ void __launch_bounds__(1024)
-    k_dd_scan(uint32_t *__restrict__ warp_reps, uint32_t nwarps, uint32_t *__restrict__ count) {
-  __shared__ uint32_t part[1024];
-  const uint32_t t = threadIdx.x;
-  const uint32_t per = (nwarps + 1023u) / 1024u;
-  const uint32_t lo = min(t * per, nwarps), hi = min(lo + per, nwarps);
-  uint32_t sum = 0u;
-  for (uint32_t i = lo; i < hi; i++) sum += warp_reps[i];
-  part[t] = sum;
-  __syncthreads();
-  for (uint32_t off = 1; off < 1024u; off <<= 1) {
-    const uint32_t add = t >= off ? part[t - off] : 0u;
-    __syncthreads();
-    part[t] += add;
-    __syncthreads();
-  }
-  uint32_t run = part[t] - sum;
-  for (uint32_t i = lo; i < hi; i++) {
-    const uint32_t c = warp_reps[i];
-    warp_reps[i] = run;
-    run += c;
-  }
-  if (t == 1023u) *count = part[1023];
-}
-
 __global__ void __launch_bounds__(256)
     k_dedupe_list(SceneView v, const uint32_t *__restrict__ rep_of,
-                  const uint32_t *__restrict__ warp_base, uint32_t *__restrict__ list) {
+                  const uint32_t *__restrict__ warp_incl, uint32_t *__restrict__ list) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned lane = threadIdx.x & 31u;
   const bool is_rep = s < v.b->n_sorted && rep_of[s] == s;
   const unsigned reps = __ballot_sync(0xffffffffu, is_rep);
   if (is_rep)
-    list[warp_base[s >> 5] + uint32_t(__popc(reps & ((1u << lane) - 1u)))] = s;
+    list[warp_incl[s >> 5] - uint32_t(__popc(reps)) + uint32_t(__popc(reps & ((1u << lane) - 1u)))] = s;
 }
 
-// Task buckets of the compacted list (k_warp_work over list entries); also
-// records each representative's candidate count.
+// Task buckets of the compacted list (as k_warp_work, over list entries,
+// from the candidate counts k_warp_work kept).
 __global__ void __launch_bounds__(256)
-    k_list_work(SceneView v, const float4 *__restrict__ s_pos, const uint32_t *__restrict__ begin,
-                const uint32_t *__restrict__ list, const uint32_t *__restrict__ count,
-                uint32_t *__restrict__ cand, uint8_t *__restrict__ task_bucket,
+    k_list_work(const uint32_t *__restrict__ list, const uint32_t *__restrict__ count,
+                const uint32_t *__restrict__ cand, uint8_t *__restrict__ task_bucket,
                 uint32_t *__restrict__ hist) {
+  __shared__ uint32_t h[ORDER_BUCKETS];
+  if (threadIdx.x < unsigned(ORDER_BUCKETS)) h[threadIdx.x] = 0u;
+  __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t entries = *count;
   uint32_t total = 0u;
   const bool active = i < entries;
-  if (active) {
-    const uint32_t s = list[i];
-    const DevUniforms *U = v.u + v.scene_of_slot[s];
-    Runs R;
-    neighbor_runs(xyz(s_pos[s]), U->grid, begin + U->c_offset, R);
-    total = R.total;
-    cand[s] = total;
-  }
+  if (active) total = cand[list[i]];
   const uint32_t m = __reduce_max_sync(0xffffffffu, total);
   if ((threadIdx.x & 31u) == 0u && active) {
     const uint32_t b = 32u - uint32_t(__clz(m));
     task_bucket[i >> 5] = uint8_t(b);
-    atomicAdd(&hist[b], 1u);
+    atomicAdd(&h[b], 1u);
   }
+  flush_buckets(h, hist);
 }
 
 // The copies: each slot that is not a representative takes its
@@ -1219,8 +1252,8 @@ cudaError_t prepare_queue(const DevState &d, const uint32_t *order, bool slots, 
 
 cudaError_t order_by_keys(const DevState &d, uint32_t n, uint32_t *perm, cudaStream_t st) {
   k_key_bases<<<1, 1024, 0, st>>>(d.key_hist, d.key_hist + KEY_BUCKETS);
-  k_key_scatter<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.work_key, d.key_hist + KEY_BUCKETS,
-                                                    d.key_hist + 2 * KEY_BUCKETS, perm);
+  k_key_scatter<<<blocks_for(n, KEY_CHUNK), KEY_THREADS, 0, st>>>(
+      d.view(), d.work_key, d.key_hist + KEY_BUCKETS, d.key_hist + 2 * KEY_BUCKETS, perm);
   return cudaGetLastError();
 }
 }  // namespace
@@ -1230,7 +1263,7 @@ cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(d.order_hist, 0, sizeof(uint32_t) * 2 * ORDER_BUCKETS, st);
   if (e != cudaSuccess) return e;
   k_warp_work<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.cell_begin, d.warp_bucket,
-                                                  d.order_hist);
+                                                  d.order_hist, d.dens_cand);
   const uint32_t nwarps = (n + 31u) / 32u;
   k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(d.view(), d.warp_bucket, d.order_hist,
                                                            d.order_hist + ORDER_BUCKETS,
@@ -1242,7 +1275,8 @@ cudaError_t launch_order_hits(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d.key_hist, 0, sizeof(uint32_t) * 3 * KEY_BUCKETS, st);
   if (e != cudaSuccess) return e;
-  k_hit_keys<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.mask_hits, d.work_key, d.key_hist);
+  k_hit_keys<<<blocks_for(n, KEY_CHUNK), KEY_THREADS, 0, st>>>(d.view(), d.mask_hits, d.work_key,
+                                                              d.key_hist);
   return order_by_keys(d, n, d.perm_hit, st);
 }
 
@@ -1257,19 +1291,24 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   const uint32_t nwarps = (n + 31u) / 32u;
   TaskQueue q;
   if (dedupe) {
+    // representatives per warp, their inclusive scan (decoupled look-back),
+    // the compacted list; its size is the scan's last entry
+    const uint32_t *dd_count = d.dd_incl + (nwarps - 1u);
     k_dedupe_mark<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.rep_of, d.dd_warp);
-    k_dd_scan<<<1, 1024, 0, st>>>(d.dd_warp, nwarps, d.dd_count);
-    k_dedupe_list<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.rep_of, d.dd_warp, d.dd_list);
+    e = cudaMemsetAsync(d.dd_tiles, 0, sizeof(unsigned long long) * (scan_tiles(nwarps) + 1), st);
+    if (e != cudaSuccess) return e;
+    e = launch_scan_with_scratch(d.dd_warp, d.dd_incl, nwarps, d.dd_tiles, d.err, st);
+    if (e != cudaSuccess) return e;
+    k_dedupe_list<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.rep_of, d.dd_incl, d.dd_list);
     e = cudaMemsetAsync(d.dd_hist, 0, sizeof(uint32_t) * 2 * ORDER_BUCKETS, st);
     if (e != cudaSuccess) return e;
-    k_list_work<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.cell_begin, d.dd_list,
-                                                    d.dd_count, d.dens_cand, d.dd_bucket,
+    k_list_work<<<blocks_for(n, 256), 256, 0, st>>>(d.dd_list, dd_count, d.dens_cand, d.dd_bucket,
                                                     d.dd_hist);
     k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(
-        d.view(), d.dd_bucket, d.dd_hist, d.dd_hist + ORDER_BUCKETS, d.dd_order, d.dd_count);
+        d.view(), d.dd_bucket, d.dd_hist, d.dd_hist + ORDER_BUCKETS, d.dd_order, dd_count);
     e = prepare_queue(d, d.dd_order, false, n, TASK_COUNTERS - 1, st, &q);
     q.list = d.dd_list;
-    q.count = d.dd_count;
+    q.count = dd_count;
   } else {
     e = prepare_queue(d, d.warp_order, false, n, TASK_COUNTERS - 1, st, &q);
   }
