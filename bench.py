@@ -44,12 +44,12 @@ WARMUP_PAST_TUNING = 16
 
 def kernels_per_step(iterations: int) -> int:
     """Kernel launches of one step without rigid-body coupling: hash, scan,
-    scatter, sort/gather, warp work + order (2), density dedupe (mark, scan,
-    list, list work, order: 5), density, dedupe copy, hit keys, key bases,
-    key scatter, XSPH, force + predict, one solve per PCISPH iteration and
-    finalize + integrate: 19 + iterations. The grid clear is a memset, not
-    counted."""
-    return 19 + iterations
+    scatter, sort/gather with the big-cell sort and rank (3), warp work +
+    order (2), density dedupe (mark, scan, list, list work, order: 5),
+    density, dedupe copy, hit keys, key bases, key scatter, XSPH, force +
+    predict, one solve per PCISPH iteration and finalize + integrate:
+    21 + iterations. The grid clear is a memset, not counted."""
+    return 21 + iterations
 
 
 # algorithmic bytes per particle-step and per stage (SoA, compulsory traffic)

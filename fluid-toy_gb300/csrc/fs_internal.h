@@ -100,6 +100,7 @@ struct DevState {
   uint32_t *cell_of;     // particle -> cell (hash output)
   uint32_t *rank_of;     // particle -> arrival rank within its cell
   uint32_t *t_tmp;       // unsorted slot -> particle
+  uint32_t *big_cells;   // [4 + 2 big_item_cap(M)]: items, 2 tickets, pad, (cell, chunk) items
   uint32_t *s2o;         // sorted slot -> particle (sorted_to_orig)
   uint32_t *cidx;        // particle -> sorted slot (particle_cell_indices)
   uint32_t *counts;      // cell_counts[total_cells]
@@ -171,6 +172,17 @@ cudaError_t launch_density_splat(const SplatArgs &a, const float4 *s_pos, const 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Cells with more than SORT_SMALL particles are ordered in chunks of
+// SORT_CHUNK slots (each sorted by one block in shared memory, then each
+// particle ranked by binary searches in the cell's other chunks); smaller
+// ones by per-slot counting (O(count^2) per cell, every slot in parallel).
+constexpr uint32_t SORT_SMALL = 512, SORT_CHUNK = 4096;
+// work items (cell, chunk) the reorder can list: at most one partial chunk
+// per big cell beyond the full chunks
+inline uint32_t big_item_cap(uint32_t max_particles) {
+  return max_particles / SORT_CHUNK + max_particles / (SORT_SMALL + 1) + 1;
+}
 
 inline uint32_t scan_tiles(uint32_t total_cells) {
   return (total_cells + SCAN_TILE - 1) / SCAN_TILE;

@@ -221,6 +221,25 @@ __global__ void __launch_bounds__(256) k_scatter(SceneView v, const uint32_t *__
 // particle v; its final slot is begin[cell] + #{particles of the cell with a
 // smaller index}. The record is gathered into grid order (grid_reorder.wgsl:
 // 54-62) and both index maps and the slot's scene are written.
+__device__ __forceinline__ void gather_slot(const SceneView &sv, uint32_t v, uint32_t d,
+                                            const float4 *__restrict__ p_pos,
+                                            const float4 *__restrict__ p_vel,
+                                            const float4 *__restrict__ p_force,
+                                            float4 *__restrict__ s_pos, float4 *__restrict__ s_vel,
+                                            float4 *__restrict__ s_frc, uint32_t *__restrict__ s2o,
+                                            uint32_t *__restrict__ cidx,
+                                            uint16_t *__restrict__ scene_of_slot) {
+  s2o[d] = v;
+  cidx[v] = d;
+  scene_of_slot[d] = sv.scene_of[v];
+  s_pos[d] = p_pos[v];
+  s_vel[d] = p_vel[v];
+  s_frc[d] = p_force[v];
+}
+
+// Per slot, counting the cell's smaller indices (O(count^2) per cell); the
+// cells with more than SORT_SMALL particles are listed instead, as one work
+// item per chunk of SORT_CHUNK slots, for k_big_sort and k_big_rank.
 __global__ void __launch_bounds__(256)
     k_sort_gather(SceneView sv, const uint32_t *__restrict__ t_tmp,
                   const uint32_t *__restrict__ cell_of, const uint32_t *__restrict__ begin,
@@ -228,21 +247,116 @@ __global__ void __launch_bounds__(256)
                   const float4 *__restrict__ p_force, float4 *__restrict__ s_pos,
                   float4 *__restrict__ s_vel, float4 *__restrict__ s_frc,
                   uint32_t *__restrict__ s2o, uint32_t *__restrict__ cidx,
-                  uint16_t *__restrict__ scene_of_slot) {
+                  uint16_t *__restrict__ scene_of_slot, uint32_t *__restrict__ big) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= sv.b->n_sorted) return;
   const uint32_t v = t_tmp[s];
   const uint32_t c = cell_of[v];
   const uint32_t b = begin[c], e = begin[c + 1];
+  if (e - b > SORT_SMALL) {
+    if (s == b) {
+      const uint32_t chunks = (e - b + SORT_CHUNK - 1u) / SORT_CHUNK;
+      const uint32_t first = atomicAdd(&big[0], chunks);
+      for (uint32_t q = 0; q < chunks; q++) {
+        big[4 + 2 * (first + q)] = c;
+        big[4 + 2 * (first + q) + 1] = q;
+      }
+    }
+    return;
+  }
   uint32_t rank = 0;
   for (uint32_t k = b; k < e; k++) rank += (t_tmp[k] < v) ? 1u : 0u;
-  const uint32_t d = b + rank;
-  s2o[d] = v;
-  cidx[v] = d;
-  scene_of_slot[d] = sv.scene_of[v];
-  s_pos[d] = p_pos[v];
-  s_vel[d] = p_vel[v];
-  s_frc[d] = p_force[v];
+  gather_slot(sv, v, b + rank, p_pos, p_vel, p_force, s_pos, s_vel, s_frc, s2o, cidx,
+              scene_of_slot);
+}
+
+// Takes the next listed item for the whole block from ticket counter `t`;
+// false when none is left. Sets the item's cell range and chunk.
+__device__ __forceinline__ bool next_big_item(uint32_t *big, int t, const uint32_t *begin,
+                                              uint32_t &b, uint32_t &m, uint32_t &q) {
+  __shared__ uint32_t s_item;
+  __syncthreads();  // the block is done with the previous item
+  if (threadIdx.x == 0) s_item = atomicAdd(&big[t], 1u);
+  __syncthreads();
+  const uint32_t item = s_item;
+  if (item >= big[0]) return false;
+  const uint32_t c = big[4 + 2 * item];
+  q = big[4 + 2 * item + 1];
+  b = begin[c];
+  m = begin[c + 1] - b;
+  return true;
+}
+
+// Sorts each listed chunk of t_tmp ascending in place (bitonic network in
+// shared memory, padded to a power of two with 0xffffffff; the particle
+// indices are distinct).
+constexpr unsigned BIG_THREADS = 512;
+__global__ void __launch_bounds__(BIG_THREADS) k_big_sort(uint32_t *__restrict__ t_tmp,
+                                                          const uint32_t *__restrict__ begin,
+                                                          uint32_t *__restrict__ big) {
+  __shared__ uint32_t ids[SORT_CHUNK];
+  const unsigned t = threadIdx.x;
+  uint32_t b, m, q;
+  while (next_big_item(big, 1, begin, b, m, q)) {
+    const uint32_t lo = b + q * SORT_CHUNK, len = min(SORT_CHUNK, m - q * SORT_CHUNK);
+    uint32_t P = 1u;
+    while (P < len) P <<= 1;
+    for (uint32_t i = t; i < P; i += BIG_THREADS) ids[i] = i < len ? t_tmp[lo + i] : 0xffffffffu;
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t r = t; r < P / 2; r += BIG_THREADS) {
+          const uint32_t i0 = ((r & ~(j - 1u)) << 1) | (r & (j - 1u));  // bit j clear
+          const uint32_t i1 = i0 | j;
+          const uint32_t x = ids[i0], y = ids[i1];
+          if ((x > y) == ((i0 & k) == 0u)) {
+            ids[i0] = y;
+            ids[i1] = x;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (uint32_t i = t; i < len; i += BIG_THREADS) t_tmp[lo + i] = ids[i];
+  }
+}
+
+// Number of entries of the ascending run a[0, len) below v.
+__device__ __forceinline__ uint32_t count_below(const uint32_t *__restrict__ a, uint32_t len,
+                                                uint32_t v) {
+  uint32_t lo = 0u, hi = len;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < v) lo = mid + 1u;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// The particles of each listed chunk: rank = position in its sorted chunk +
+// the entries below it in the cell's other chunks; gathered into grid order.
+__global__ void __launch_bounds__(BIG_THREADS)
+    k_big_rank(SceneView sv, const uint32_t *__restrict__ t_tmp,
+               const uint32_t *__restrict__ begin, const float4 *__restrict__ p_pos,
+               const float4 *__restrict__ p_vel, const float4 *__restrict__ p_force,
+               float4 *__restrict__ s_pos, float4 *__restrict__ s_vel,
+               float4 *__restrict__ s_frc, uint32_t *__restrict__ s2o,
+               uint32_t *__restrict__ cidx, uint16_t *__restrict__ scene_of_slot,
+               uint32_t *__restrict__ big) {
+  uint32_t b, m, q;
+  while (next_big_item(big, 2, begin, b, m, q)) {
+    const uint32_t lo = b + q * SORT_CHUNK, len = min(SORT_CHUNK, m - q * SORT_CHUNK);
+    const uint32_t chunks = (m + SORT_CHUNK - 1u) / SORT_CHUNK;
+    for (uint32_t i = threadIdx.x; i < len; i += BIG_THREADS) {
+      const uint32_t v = t_tmp[lo + i];
+      uint32_t rank = i;
+      for (uint32_t r = 0; r < chunks; r++)
+        if (r != q)
+          rank += count_below(t_tmp + b + r * SORT_CHUNK, min(SORT_CHUNK, m - r * SORT_CHUNK), v);
+      gather_slot(sv, v, b + rank, p_pos, p_vel, p_force, s_pos, s_vel, s_frc, s2o, cidx,
+                  scene_of_slot);
+    }
+  }
 }
 
 inline unsigned blocks_for(uint32_t n, unsigned threads) {
@@ -345,9 +459,16 @@ cudaError_t launch_export_aos(const DevState &d, bool sorted, uint32_t first, ui
 
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_t st) {
   if (n_sorted == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d.big_cells, 0, 4 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
   k_sort_gather<<<blocks_for(n_sorted, 256), 256, 0, st>>>(
       d.view(), d.t_tmp, d.cell_of, d.cell_begin, d.p_pos, d.p_vel, d.p_force, d.s_pos, d.s_vel,
-      d.s_frc, d.s2o, d.cidx, d.scene_of_slot);
+      d.s_frc, d.s2o, d.cidx, d.scene_of_slot, d.big_cells);
+  const unsigned blocks = 4u * unsigned(d.sm_count);
+  k_big_sort<<<blocks, BIG_THREADS, 0, st>>>(d.t_tmp, d.cell_begin, d.big_cells);
+  k_big_rank<<<blocks, BIG_THREADS, 0, st>>>(d.view(), d.t_tmp, d.cell_begin, d.p_pos, d.p_vel,
+                                             d.p_force, d.s_pos, d.s_vel, d.s_frc, d.s2o, d.cidx,
+                                             d.scene_of_slot, d.big_cells);
   return cudaGetLastError();
 }
 

@@ -125,6 +125,7 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.cell_of = c.take<uint32_t>(M);
   d.rank_of = c.take<uint32_t>(M);
   d.t_tmp = c.take<uint32_t>(M);
+  d.big_cells = c.take<uint32_t>(4 + 2 * size_t(big_item_cap(M)));
   d.s2o = c.take<uint32_t>(M);
   d.cidx = c.take<uint32_t>(M);
   d.counts = c.take<uint32_t>(G);

@@ -103,6 +103,46 @@ def test_coincident_particles(fslib, oracle_mod, sc):
     assert sim.load_batching()[1]
 
 
+def test_big_cells(fslib, oracle_mod, sc):
+    """Cells holding more than 512 particles (the reorder sorts them in
+    chunks of 4096 and ranks across chunks) beside ordinary cells: just above
+    the threshold, exactly one chunk, one chunk plus one particle, and three
+    chunks, with the particles' indices shuffled so each cell's arrival order
+    is random."""
+    import copy
+    import dataclasses
+
+    from fluidsph.abi import COL_POS
+    scene = sc.small_scene(12, 10, 8, seed=9)
+    base = scene.particles
+    h = float(scene.sph.kernel_radius)
+    origin = -2.0 - h  # the reference grid's origin (bounds extent 2, one cell margin)
+    rng = np.random.default_rng(17)
+    lo, hi = base[:, COL_POS].min(axis=0), base[:, COL_POS].max(axis=0)
+    rows = [base]
+    # 4096 and 4097 particles alone in cells past the lattice's corners
+    past = 1.5 * h / (hi - lo)
+    for size, frac in ((513, 0.2), (4096, 1.0 + past), (4097, -past), (9000, 0.7)):
+        k = np.floor((lo + frac * (hi - lo) - origin) / h)
+        centre = origin + (k + 0.5) * h
+        blk = np.repeat(base[:1], size, axis=0)
+        blk[:, COL_POS] = (centre + rng.uniform(-0.3 * h, 0.3 * h, size=(size, 3))).astype(np.float32)
+        rows.append(blk)
+    p = np.concatenate(rows)
+    p = p[rng.permutation(len(p))]
+    sph = copy.copy(scene.sph)
+    sph.num_particles = len(p)  # the dispatch count, as the reference's params carry it
+    scene = dataclasses.replace(scene, particles=p, sph=sph)
+    sim, orc = _run_pair(scene, 1, oracle_mod)
+    counts, _ = sim.cells()
+    assert (counts > 512).sum() == 4 and (counts == 4096).sum() == 1 and (counts == 4097).sum() == 1
+    _compare(sim, orc, len(p), "big cells step 1")
+    for _ in range(2):
+        sim.step(1)
+        orc.step(1)
+    _compare(sim, orc, len(p), "big cells step 3")
+
+
 def test_graph_replay_matches_single_steps(fslib, sc):
     scene = sc.small_scene(seed=3)
     a = gpu_sim_for_scene(scene)
