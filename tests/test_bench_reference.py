@@ -1,0 +1,28 @@
+"""bench.py's reference arm on CPU: the oracle timed on the host cores after
+the requested warm-up steps, printed as one JSON line with the arm's keys.
+Runs the 49,600-particle dam break (configuration 0) to stay quick."""
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_reference_arm_json_line():
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--config", "0", "--steps", "2", "--warmup", "3", "--cpu-steps", "1"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == "particle-steps/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3
+    assert d["config"]["particles"] == 49600
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert "steps 4..4" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "particle-steps/s",
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
