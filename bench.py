@@ -718,36 +718,61 @@ def run_identify(args, dist: Dist) -> dict | None:
     }
 
 
+def repo_libraries() -> list[str]:
+    """Shared objects of this repository mapped into this process (Linux)."""
+    try:
+        maps = Path("/proc/self/maps").read_text()
+    except OSError:
+        return []
+    root = str(ROOT)
+    found = {ln.split()[-1] for ln in maps.splitlines()
+             if ln.split() and ln.split()[-1].startswith(root) and ".so" in ln.split()[-1]}
+    return sorted(str(Path(f).relative_to(root)) for f in found)
+
+
 def run_reference(args, dist: Dist) -> dict | None:
+    """The reference arm: the reference step's CPU restatement (the oracle) on
+    all host cores. It warms up exactly as this library's arm does
+    (max(--warmup, WARMUP_PAST_TUNING) steps from the same seeded scene; the
+    oracle's trajectory is the GPU's bit for bit), so both arms time the same
+    rollout states from step W+1 on, and it builds its parameter structs with
+    the oracle's own restatement of the reference's host builders, so the
+    product library is never loaded."""
     if dist.rank != 0:
         return None
-    scene = make_scene(args.config)
-    W, K = args.warmup, args.steps
-    # the reference arm runs the bounded sample: up to 20 warm-up steps (the
-    # same rollout states this library's own CPU-baseline sample starts from,
-    # the step after its 20 warm-ups: the oracle's trajectory is the GPU's bit
-    # for bit) and K timed steps capped so the run stays within minutes
-    from oracle import oracle
+    from fluidsph import scenes
+    from oracle import host_params, oracle
+    if args.config not in (0, 1):
+        raise SystemExit("--impl reference runs the plain configurations 0 and 1")
+    scene = scenes.CONFIGS[args.config](builders=host_params)
+    W, K = max(args.warmup, WARMUP_PAST_TUNING), args.steps
     nthreads = oracle.set_threads(0)
     o = oracle.oracle_for_scene(scene)
+    if scene.rigid is not None:
+        o.clear_rigid_body_accum()
     k_cpu = min(K, args.cpu_steps)
-    w_cpu = min(W, 20)
-    o.step(w_cpu)
+    o.step(W)
     t0 = time.perf_counter()
     o.step(k_cpu)
     secs = time.perf_counter() - t0
     value = scene.n * k_cpu / secs
     sample = (f"{scene.name}: oracle (FP32 C++ restatement of the step WGSL, OpenMP), "
-              f"steps {w_cpu + 1}..{w_cpu + k_cpu}")
+              f"steps {W + 1}..{W + k_cpu}")
     return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": METRIC,
-            "n_gpus": dist.world, "steps": k_cpu, "warmup": w_cpu,
+            "n_gpus": dist.world, "steps": k_cpu, "warmup": W,
             "ms_per_step": round(secs / k_cpu * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": scene.name, "particles": scene.n},
+            "config": {"workload": scene.name, "particles": scene.n,
+                       "steps_timed": f"{W + 1}..{W + k_cpu}",
+                       "gpu_arm_steps_timed": f"{W + 1}..{W + K}",
+                       "same_states": "both arms start timing at step W+1 of the same seeded "
+                                      "rollout; this arm times the first "
+                                      f"{k_cpu} of the GPU arm's {K} steps"},
             "cpu_baseline": {"value": round(value, 1), "unit": METRIC, "cores": nthreads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": round(value, 1), "unit": METRIC, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "libraries_loaded": repo_libraries()}
 
 
 def main():
@@ -757,7 +782,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1)
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched and differentiable forms in the default run")

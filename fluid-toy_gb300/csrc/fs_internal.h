@@ -196,6 +196,12 @@ cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st
 cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uint32_t total_cells,
                                      unsigned long long *tile_status, uint32_t *err,
                                      cudaStream_t st);
+// The scan on caller-provided scratch of scan_tiles(total_cells) + 2 zeroed
+// words; inject = every look-back wait runs out (the failure-detection
+// self-test, fs_selftest_scan_wait).
+cudaError_t launch_scan_selftest(const uint32_t *counts, uint32_t *ends, uint32_t total_cells,
+                                 unsigned long long *tile_status, uint32_t *err, bool inject,
+                                 cudaStream_t st);
 cudaError_t launch_scatter(const DevState &d, uint32_t n_canon, cudaStream_t st);
 cudaError_t launch_sort_gather(const DevState &d, uint32_t n_sorted, cudaStream_t st);
 // 64-byte AoS records of canonical particles or sorted slots [first, first + count)

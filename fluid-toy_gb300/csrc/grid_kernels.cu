@@ -75,6 +75,11 @@ __global__ void __launch_bounds__(256) k_hash(const float4 *__restrict__ pos, Sc
 constexpr unsigned long long FLAG_AGG = 1ull << 32;
 constexpr unsigned long long FLAG_PRE = 2ull << 32;
 constexpr int LOOKBACK_POLL_LIMIT = 1 << 22;
+// Failure-detection self-test (fs_selftest_scan_wait): the look-back polls a
+// word that nothing ever publishes, with this short bound, so every wait of a
+// tile after the first runs out on every call; the kernel then finishes as
+// after a real expiry (a wrong prefix, the expiry recorded in the error word).
+constexpr int INJECTED_POLL_LIMIT = 64;
 
 __device__ __forceinline__ void publish(unsigned long long *slot, unsigned long long v) {
   cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> r(*slot);
@@ -85,10 +90,11 @@ __device__ __forceinline__ unsigned long long peek(unsigned long long *slot) {
   return r.load(cuda::memory_order_acquire);
 }
 
+template <bool kInjectExpiry>
 __global__ void __launch_bounds__(SCAN_THREADS)
     k_scan(const uint32_t *__restrict__ counts, uint32_t *__restrict__ ends,
            uint32_t total, unsigned long long *tile_status, uint32_t *tile_ticket,
-           uint32_t *err) {
+           uint32_t *err, unsigned long long *never_published) {
   // items staged through shared memory; padded to avoid bank conflicts when
   // each thread walks its 16 consecutive items.
   __shared__ uint32_t sm[SCAN_TILE + SCAN_TILE / 32];
@@ -157,15 +163,17 @@ __global__ void __launch_bounds__(SCAN_THREADS)
         unsigned long long d = FLAG_PRE;  // lanes before tile 0 read "prefix 0"
         if (idx >= 0) {
           int polls = 0;
-          d = peek(&tile_status[idx]);
+          unsigned long long *slot = kInjectExpiry ? never_published : &tile_status[idx];
+          const int limit = kInjectExpiry ? INJECTED_POLL_LIMIT : LOOKBACK_POLL_LIMIT;
+          d = peek(slot);
           while ((d >> 32) == 0ull) {
-            if (++polls > LOOKBACK_POLL_LIMIT) {
+            if (++polls > limit) {
               timed_out = true;
               d = FLAG_PRE;  // give up: treat as zero prefix
               break;
             }
             __nanosleep(64);
-            d = peek(&tile_status[idx]);
+            d = peek(slot);
           }
         }
         const unsigned pre_mask = __ballot_sync(0xffffffffu, (d >> 32) == 2ull);
@@ -379,8 +387,8 @@ cudaError_t launch_scan(const DevState &d, uint32_t total_cells, cudaStream_t st
   cudaError_t e = cudaMemsetAsync(d.tile_status, 0,
                                   sizeof(unsigned long long) * (size_t(tiles) + 1), st);
   if (e != cudaSuccess) return e;
-  k_scan<<<tiles, SCAN_THREADS, 0, st>>>(d.counts, d.cell_begin + 1, total_cells,
-                                         d.tile_status, d.tile_ticket, d.err);
+  k_scan<false><<<tiles, SCAN_THREADS, 0, st>>>(d.counts, d.cell_begin + 1, total_cells,
+                                                d.tile_status, d.tile_ticket, d.err, nullptr);
   return cudaGetLastError();
 }
 
@@ -389,8 +397,26 @@ cudaError_t launch_scan_with_scratch(const uint32_t *counts, uint32_t *ends, uin
                                      cudaStream_t st) {
   if (total_cells == 0) return cudaSuccess;
   const uint32_t tiles = scan_tiles(total_cells);
-  k_scan<<<tiles, SCAN_THREADS, 0, st>>>(counts, ends, total_cells, tile_status,
-                                         reinterpret_cast<uint32_t *>(tile_status + tiles), err);
+  k_scan<false><<<tiles, SCAN_THREADS, 0, st>>>(
+      counts, ends, total_cells, tile_status, reinterpret_cast<uint32_t *>(tile_status + tiles),
+      err, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan_selftest(const uint32_t *counts, uint32_t *ends, uint32_t total_cells,
+                                 unsigned long long *tile_status, uint32_t *err, bool inject,
+                                 cudaStream_t st) {
+  if (total_cells == 0) return cudaSuccess;
+  const uint32_t tiles = scan_tiles(total_cells);
+  // tile_status: tiles descriptors, the ticket word, then the word that the
+  // injected form polls and nothing writes (all cleared by the caller)
+  uint32_t *ticket = reinterpret_cast<uint32_t *>(tile_status + tiles);
+  if (inject)
+    k_scan<true><<<tiles, SCAN_THREADS, 0, st>>>(counts, ends, total_cells, tile_status, ticket,
+                                                 err, tile_status + tiles + 1);
+  else
+    k_scan<false><<<tiles, SCAN_THREADS, 0, st>>>(counts, ends, total_cells, tile_status, ticket,
+                                                  err, nullptr);
   return cudaGetLastError();
 }
 

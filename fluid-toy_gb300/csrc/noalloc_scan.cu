@@ -19,7 +19,11 @@
 //     GPU (different streams without ordering) race on the descriptors;
 //   - the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture.
+//     before any stream capture. Every later call made while its stream is
+//     not capturing looks the address up again, so a context that was torn
+//     down and rebuilt (cudaDeviceReset, or another runtime resetting the
+//     primary context) is followed; a call inside a capture uses the address
+//     of the last call outside one.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -39,10 +43,12 @@ std::mutex g_setup_mutex;
 unsigned long long *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_scan_scratch on the current device (host code may not
-// take the address of a __device__ symbol directly).
-cudaError_t scratch_address(int device, unsigned long long **out) {
+// take the address of a __device__ symbol directly). Looked up again on every
+// call with `refresh` set: after a context reset the module is loaded anew and
+// the array can sit at another address.
+cudaError_t scratch_address(int device, bool refresh, unsigned long long **out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[device]) {
+  if (refresh || !g_scratch_addr[device]) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_scan_scratch);
     if (e != cudaSuccess) return e;
@@ -74,13 +80,20 @@ extern "C" int fs_prefix_scan_noalloc(const uint32_t *cell_counts, uint32_t *cel
     fs::set_last_error("fs_prefix_scan_noalloc: no usable current CUDA device");
     return FS_E_NO_DEVICE;
   }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // outside a capture the lookup is an ordinary runtime call; inside one the
+  // cached address is used (a lookup there could load the module)
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &capture) != cudaSuccess) {
+    (void)cudaGetLastError();
+    capture = cudaStreamCaptureStatusActive;
+  }
   unsigned long long *scratch = nullptr;
-  e = scratch_address(device, &scratch);
+  e = scratch_address(device, capture == cudaStreamCaptureStatusNone, &scratch);
   if (e != cudaSuccess) {
     fs::set_last_error("fs_prefix_scan_noalloc: cudaGetSymbolAddress failed");
     return FS_E_CUDA;
   }
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   const uint32_t tiles = fs::scan_tiles(total_cells);
   // descriptors and ticket start at zero for every call
   e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (size_t(tiles) + 1), st);
@@ -91,6 +104,14 @@ extern "C" int fs_prefix_scan_noalloc(const uint32_t *cell_counts, uint32_t *cel
   uint32_t *status = device_status
                          ? device_status
                          : reinterpret_cast<uint32_t *>(scratch + kMaxTiles + 1);
+  if (!device_status) {
+    // the internal status word starts clear too, like the descriptors
+    e = cudaMemsetAsync(status, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) {
+      fs::set_last_error("fs_prefix_scan_noalloc: clearing the status word failed");
+      return FS_E_CUDA;
+    }
+  }
   // the reference's cell_starts are the inclusive prefix sums
   e = fs::launch_scan_with_scratch(cell_counts, cell_starts, total_cells, scratch, status, st);
   if (e != cudaSuccess) {

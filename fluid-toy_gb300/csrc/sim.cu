@@ -1058,6 +1058,33 @@ int fs_sync(FsSim *s) {
   return check_device_error(s);
 }
 
+int fs_selftest_scan_wait(FsSim *s, int inject, uint32_t *starts_out) {
+  CHECK_SIM(s);
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (capturing(s)) return fail(FS_E_STATE, "fs_selftest_scan_wait: stream is capturing");
+  const uint32_t G = s->cells_total;
+  const uint32_t tiles = scan_tiles(G);
+  // scratch of its own: the simulation's cell tables stay as the last step
+  // left them; only the device error word is shared with the step
+  uint32_t *ends = nullptr;
+  unsigned long long *desc = nullptr;
+  FS_CUDA(cudaMalloc(&ends, sizeof(uint32_t) * size_t(G)), "self-test scratch");
+  cudaError_t e = cudaMalloc(&desc, sizeof(unsigned long long) * (size_t(tiles) + 2));
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(desc, 0, sizeof(unsigned long long) * (size_t(tiles) + 2), s->stream);
+  if (e == cudaSuccess)
+    e = launch_scan_selftest(s->d.counts, ends, G, desc, s->d.err, inject != 0, s->stream);
+  if (e == cudaSuccess && starts_out)
+    e = cudaMemcpyAsync(starts_out, ends, sizeof(uint32_t) * size_t(G), cudaMemcpyDeviceToHost,
+                        s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(desc);
+  cudaFree(ends);
+  FS_CUDA(e, "fs_selftest_scan_wait");
+  return FS_OK;
+}
+
 int fs_enable_stage_timing(FsSim *s, int enable) {
   CHECK_SIM(s);
   s->timing = enable != 0;

@@ -99,31 +99,38 @@ def lattice_block(nx: int, ny: int, nz: int, box, spacing: float = 0.02, jitter:
 
 def make_scene(name: str, particles: np.ndarray, box, c: Common | None = None, steps: int = 1,
                rigid: GpuRigidBody | None = None, tilt_x: float = 0.0, tilt_z: float = 0.0,
-               info: dict | None = None) -> Scene:
+               info: dict | None = None, builders=None) -> Scene:
+    """A scene over `particles`. `builders` supplies sph_params_3d,
+    container_geometry and gravity with the signatures of fluidsph.params
+    (the default, which evaluates them in this library); any module that
+    restates the reference's builders bit for bit gives the same scene."""
+    B = builders or P
     c = c or Common()
     Lx, Ly, Lz = box
-    sph = P.sph_params_3d(c.h, c.mass, c.rest_density, c.stiffness, c.near_stiffness,
+    sph = B.sph_params_3d(c.h, c.mass, c.rest_density, c.stiffness, c.near_stiffness,
                           c.viscosity, c.surface_tension, c.xsph_epsilon, c.dt, len(particles))
-    geom = P.container_geometry(Lx, Lz, 0.0, Ly, tilt_x, tilt_z, c.wall_stiffness, c.damping)
-    return Scene(name, particles, sph, geom, P.gravity(c.gravity), rigid, c.iterations, steps,
+    geom = B.container_geometry(Lx, Lz, 0.0, Ly, tilt_x, tilt_z, c.wall_stiffness, c.damping)
+    return Scene(name, particles, sph, geom, B.gravity(c.gravity), rigid, c.iterations, steps,
                  tuple(box), info or {})
 
 
-def config0(seed: int = 0) -> Scene:
+def config0(seed: int = 0, builders=None) -> Scene:
     """Plain dam break: 40x40x31 = 49,600 particles in a 1.6x1.2x0.8 box, 1000 steps."""
     box = (1.6, 1.2, 0.8)
-    return make_scene("dam_break_49600", lattice_block(40, 40, 31, box, seed=seed), box, steps=1000)
+    return make_scene("dam_break_49600", lattice_block(40, 40, 31, box, seed=seed), box, steps=1000,
+                      builders=builders)
 
 
-def config1(seed: int = 0) -> Scene:
+def config1(seed: int = 0, builders=None) -> Scene:
     """Plain at scale: 128x64x128 = 1,048,576 particles in a 4x2x3 box with a held
     sphere (radius 0.3, box centre (3.0,0.4,1.5) -> container (1.0,0.4,0.0)), 500 steps."""
+    B = builders or P
     box = (4.0, 2.0, 3.0)
     c = Common()
-    rb = P.rigid_body(position=(3.0 - box[0] / 2, 0.4, 1.5 - box[2] / 2), half_extent=0.3,
+    rb = B.rigid_body(position=(3.0 - box[0] / 2, 0.4, 1.5 - box[2] / 2), half_extent=0.3,
                       active=True, stiffness=c.wall_stiffness, shape=1)
     return make_scene("dam_break_1048576_sphere", lattice_block(128, 64, 128, box, seed=seed),
-                      box, c, steps=500, rigid=rb)
+                      box, c, steps=500, rigid=rb, builders=builders)
 
 
 def small_scene(nx: int = 10, ny: int = 8, nz: int = 6, box=(0.6, 0.5, 0.4), seed: int = 1,

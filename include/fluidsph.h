@@ -630,11 +630,29 @@ int fs_adj_backward(FsAdj *adj, float *dl_dpos0, float *dl_dvel0, int on_device,
  * cudaStream_t, NULL = legacy default stream). All calls share the array:
  * each clears it on its stream first, but calls that overlap on the GPU race.
  * The first call on a device looks up the array's address (with that device
- * current); make it before any stream capture. */
+ * current); make it before any stream capture. Later calls outside a capture
+ * look the address up again, so a rebuilt context is followed. */
 #define FS_NOALLOC_SCAN_MAX_CELLS (1u << 26)
 int fs_prefix_scan_noalloc(const uint32_t *cell_counts, uint32_t *cell_starts,
                            uint32_t total_cells, uint32_t *device_status,
                            void *stream);
+
+/* ---- failure-detection self-test ------------------------------------------
+ * No counterpart in the reference (its prefix scan has no waits across
+ * workgroups). Exercises the bounded look-back wait of the prefix scan the
+ * step runs (decoupled look-back, prefix_scan.wgsl's role) and its reporting
+ * path. Runs that scan over the simulation's current cell counts into scratch
+ * of its own (the simulation's tables are left as they are). With inject != 0
+ * every look-back polls a descriptor that nothing publishes and gives up
+ * after a short bound, as a wait that ran out would: the kernel still
+ * finishes (with a wrong prefix) and records the expiry in the simulation's
+ * device error word, so the next synchronising call (fs_sync,
+ * fs_read_rigid_body_accum, the downloads) returns FS_E_DEVICE_TIMEOUT and
+ * clears the word; the call after that returns FS_OK. With inject = 0 the
+ * result equals the step's cell_starts. starts_out (host, total cells), if
+ * not NULL, receives the scan's output. Synchronises the simulation's stream
+ * without reading the error word. */
+int fs_selftest_scan_wait(FsSim *sim, int inject, uint32_t *starts_out);
 
 /* ---- arithmetic self-test ---------------------------------------------------
  * No counterpart in the reference. The force and solve passes compute square

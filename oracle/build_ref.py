@@ -3,8 +3,9 @@ mechanically to C++ (oracle/wgsl2cpp.py) from the WGSL files in the reference
 tree, driven by ref_driver.cpp with the dispatch sequence of
 SphSimulation3DGrid::step() (src/simulation/sph_3d_grid.rs:1261-1444).
 
-TEST INFRASTRUCTURE ONLY. The reference tree is read where it lies; outputs go
-only to oracle/_ref/ (git-ignored). When the reference sources are absent (the
+TEST INFRASTRUCTURE ONLY. The reference tree ($FLUID_TOY_REFERENCE, or the
+checkout named `reference` beside this repository) is read where it lies;
+outputs go only to oracle/_ref/ (git-ignored). When the reference sources are absent (the
 GPU machine) but a translation made earlier is present in oracle/_ref/, only
 the C++ compile step runs.
 """
@@ -18,7 +19,16 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF_SHADERS = Path(os.environ.get("FLUID_TOY_REFERENCE", "/root/reference")) / "src" / "shaders"
+
+
+def reference_root() -> Path:
+    """The fluid-toy checkout the translation reads: $FLUID_TOY_REFERENCE if
+    set, else a checkout named `reference` beside this repository."""
+    env = os.environ.get("FLUID_TOY_REFERENCE")
+    return Path(env) if env else HERE.parent.parent / "reference"
+
+
+REF_SHADERS = reference_root() / "src" / "shaders"
 
 # (namespace, shader file, prepend container_common.wgsl) — the prepend list
 # follows sph_3d_grid.rs:169-193

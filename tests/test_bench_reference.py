@@ -1,6 +1,7 @@
 """bench.py's reference arm on CPU: the oracle timed on the host cores after
-the requested warm-up steps, printed as one JSON line with the arm's keys.
-Runs the 49,600-particle dam break (configuration 0) to stay quick."""
+the same warm-up as the GPU arm (at least 16 steps), printed as one JSON line
+with the arm's keys, without the product library loaded. Runs the
+49,600-particle dam break (configuration 0) to stay quick."""
 import json
 import subprocess
 import sys
@@ -19,10 +20,16 @@ def test_reference_arm_json_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference"
     assert d["metric"] == "particle-steps/s" and d["higher_is_better"] is True
-    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3
+    # the GPU arm warms up max(--warmup, 16) steps; so does this arm
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 16
     assert d["config"]["particles"] == 49600
+    assert d["config"]["steps_timed"] == "17..17"
+    assert d["config"]["gpu_arm_steps_timed"] == "17..18"
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
-    assert "steps 4..4" in cb["sample"]
+    assert "steps 17..17" in cb["sample"]
+    # the oracle only: the product library is never mapped into the arm
+    assert "oracle/liboracle.so" in d["libraries_loaded"]
+    assert not any("libfluidsph" in f for f in d["libraries_loaded"]), d["libraries_loaded"]
     assert d["e2e"] == {"value": d["value"], "unit": "particle-steps/s",
                         "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

@@ -105,3 +105,44 @@ def test_grid_sizing(fslib):
     out = __import__("fluidsph.abi", fromlist=["GpuGridParams"]).GpuGridParams()
     assert fslib.fs_grid_params_for(0.0, 1, C.byref(out)) == -1      # invalid h
     assert fslib.fs_grid_params_for(0.001, 1, C.byref(out)) == -3    # grid too large
+
+
+def _struct_bytes(s) -> bytes:
+    import ctypes as C
+    return C.string_at(C.addressof(s), C.sizeof(s))
+
+
+def test_oracle_builders_equal_library_builders(fslib):
+    """The oracle's float32 restatement of the host builders (used by the
+    bench's reference arm) and the library's give byte-identical structs."""
+    from fluidsph import params as P
+    from oracle import host_params as H
+    rng = np.random.default_rng(11)
+    for _ in range(20):
+        h = float(rng.uniform(0.02, 0.12))
+        m = float(rng.uniform(0.5, 2.0))
+        rho = None if rng.random() < 0.3 else float(rng.uniform(500, 9000))
+        dt = float(rng.uniform(0.001, 0.01))
+        args = (h, m, rho, 35.0, 0.45, 15.0, 6.5, 0.305, dt, int(rng.integers(1, 10**6)))
+        assert _struct_bytes(P.sph_params_3d(*args)) == _struct_bytes(H.sph_params_3d(*args))
+        g = (float(rng.uniform(0.5, 3)), float(rng.uniform(0.5, 3)), float(rng.uniform(-1, 1)),
+             float(rng.uniform(0.5, 3)), float(rng.uniform(-0.3, 0.3)),
+             float(rng.uniform(-0.3, 0.3)), 250.0, 0.55, bool(rng.random() < 0.5), 0.03)
+        assert _struct_bytes(P.container_geometry(*g)) == _struct_bytes(H.container_geometry(*g))
+        q = rng.standard_normal(4)
+        q /= np.linalg.norm(q)
+        kw = dict(position=tuple(rng.uniform(-1, 1, 3)), half_extent=0.2, active=True,
+                  stiffness=250.0, shape=int(rng.integers(0, 5)), orientation=tuple(q))
+        assert _struct_bytes(P.rigid_body(**kw)) == _struct_bytes(H.rigid_body(**kw))
+
+
+def test_scenes_from_oracle_builders_are_identical(fslib):
+    from fluidsph import scenes
+    from oracle import host_params as H
+    for cfg in (scenes.config0, scenes.config1):
+        a, b = cfg(), cfg(builders=H)
+        assert np.array_equal(a.particles, b.particles)
+        for x, y in ((a.sph, b.sph), (a.geom, b.geom), (a.gravity, b.gravity)):
+            assert _struct_bytes(x) == _struct_bytes(y)
+        if a.rigid is not None:
+            assert _struct_bytes(a.rigid) == _struct_bytes(b.rigid)
