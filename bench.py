@@ -553,9 +553,10 @@ def run_adjoint(args, dist: Dist) -> dict | None:
     t0 = time.perf_counter()
     r.forward(T)
     loss = r.splat_mse_loss(mc, sc.geom, target)
-    dpos, dvel, dpar = r.backward()
+    dpos, dvel, _ = r.backward()
     torch.cuda.synchronize(dev)
     total_ms = (time.perf_counter() - t0) * 1e3 / T
+    dpar = r.param_gradients()
     finite = bool(np.isfinite(dvel).all() and np.isfinite(dpar).all())
     r.close()
     sim.close()
@@ -573,17 +574,18 @@ def run_adjoint(args, dist: Dist) -> dict | None:
         "forward_ms_per_step": round(fwd_ms, 4),
         "fwd_adjoint_over_forward": round(total_ms / fwd_ms, 3),
         "loss": loss, "gradient_finite": finite,
-        "grad_params": {"viscosity": float(dpar[0, 0]), "stiffness": float(dpar[0, 1]),
-                        "surface_tension": float(dpar[0, 2])},
+        "grad_params": {n: float(dpar[0, i])
+                        for i, n in enumerate(DifferentiableRollout.PARAM_NAMES)},
     }
 
 
 def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, tape_budget=0):
-    """Batched gradient descent on per-scene viscosity and surface tension
-    (and stiffness, whose gradient is 0) against hidden-parameter targets.
-    Steps are sign steps scaled by a decaying rate relative to each
-    parameter's range, robust to the gradients' magnitude. Returns the
-    parameter errors, the losses and (timed) fwd+adjoint ms/step."""
+    """Batched gradient descent on per-scene viscosity, pcisph_delta (the
+    pressure strength the step reads) and surface tension against
+    hidden-parameter targets. Steps are sign steps scaled by a decaying rate
+    relative to each parameter's range, robust to the gradients' magnitude.
+    Returns the parameter errors, the losses and (timed) fwd+adjoint
+    ms/step."""
     import torch
     from fluidsph import scenes as S
     from fluidsph.adjoint import DifferentiableRollout
@@ -613,7 +615,8 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, 
     params = [with_(s.sph) for s in scenes]
     b = batch(params)
     r = DifferentiableRollout(b, every, tape_budget_bytes=tape_budget)
-    names = ("viscosity", "stiffness", "surface_tension")
+    names = ("viscosity", "pcisph_delta", "surface_tension")
+    cols = [DifferentiableRollout.PARAM_NAMES.index(n) for n in names]
     init = np.array([[getattr(p, n) for n in names] for p in params], np.float64)
     cur = init.copy()
     truth = np.array([[h[n] for n in names] for h in hidden], np.float64)
@@ -621,7 +624,7 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, 
     losses, ms = [], []
     for it in range(iters):
         for k, p in enumerate(params):
-            p.viscosity, p.stiffness, p.surface_tension = (float(v) for v in cur[k])
+            p.viscosity, p.pcisph_delta, p.surface_tension = (float(v) for v in cur[k])
             b.update_scene(k, sph_params=p)
         for k, s in enumerate(scenes):
             b.upload_scene_particles(k, s.particles)
@@ -631,7 +634,8 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, 
         r.forward(steps)
         loss = sum(r.splat_mse_loss(grids[k], scenes[k].geom, targets[k], scene=k)
                    for k in range(len(scenes)))
-        _, _, g = r.backward(scenes=len(scenes))
+        r.backward(scenes=len(scenes))
+        g = r.param_gradients(scenes=len(scenes))[:, cols]
         torch.cuda.synchronize(dev)
         ms.append((time.perf_counter() - t0) * 1e3 / steps)
         losses.append(loss)

@@ -37,7 +37,9 @@ struct AdjView {
   float *gp;      // d/d pressure carried between PCISPH levels
   float4 *gu[2];  // per level: d/d pressure acceleration (pre-clamp), d/d next density
   double *gparam; // [scenes][3]: viscosity, stiffness, surface_tension (FP64)
+  double *gparam2;  // [scenes][2]: near_stiffness, pcisph_delta (FP64)
   double2 *gpart; // [N] canonical: each particle's share of d/d (viscosity, surface tension)
+  double2 *gpart2;  // [N] canonical: each particle's share of d/d (near_stiffness, pcisph_delta)
   uint32_t *counters;  // task counters of the gather launches [kMaxAdjIters + 3]
   uint32_t *err;
 };
@@ -49,8 +51,9 @@ cudaError_t launch_adj_step(const SceneView &v, const TapeView &t, const AdjView
 // partial: one double per 256 voxels
 cudaError_t launch_splat_mse(const SplatArgs &sa, const float *field, const float *target,
                              float *gg, double *partial, double *loss, cudaStream_t st);
-cudaError_t launch_reduce_params(const double2 *gpart, const uint32_t *scene_first,
-                                 const uint32_t *scene_count, uint32_t scenes, double *gparam,
+cudaError_t launch_reduce_params(const double2 *gpart, const double2 *gpart2,
+                                 const uint32_t *scene_first, const uint32_t *scene_count,
+                                 uint32_t scenes, double *gparam, double *gparam2,
                                  cudaStream_t st);
 cudaError_t launch_rows_to_f4(uint32_t n, const float *rows, float4 *out, cudaStream_t st);
 cudaError_t launch_f4_to_rows(uint32_t n, const float4 *in, float *rows, cudaStream_t st);

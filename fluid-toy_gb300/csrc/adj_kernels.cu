@@ -27,7 +27,8 @@
 // ERR_ADJ_OUTSIDE_GRID otherwise.
 //
 // Per-particle adjoints are FP32; the scalar-parameter gradients (viscosity,
-// surface tension) are reduced in FP64.
+// surface tension, near stiffness, the PCISPH pressure factor delta) are
+// summed per particle and reduced per scene in FP64.
 #include "adj_internal.h"
 #include "sph_device.cuh"
 
@@ -319,6 +320,10 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
     const float rhat = rb + (rho_q > P.rest_density ? P.pcisph_delta * p_bar : 0.0f);
     gu_out[q] = f4(apb, rhat);
     a.gp[q] = p_bar;
+    // p^k = p^(k-1) + delta max(0, rho*^k - rho0): the particle's share of
+    // d/d delta at this level (pcisph_solve.wgsl's density_error)
+    const float density_error = fmaxf(0.0f, rho_q - P.rest_density);
+    a.gpart2[t.s2o[q]].y += double(p_bar) * double(density_error);
   }
   // k == 0: predict, x*^0 = x + dt v*^0, v*^0 = vhat + dt a (done above)
 }
@@ -391,7 +396,7 @@ __device__ __forceinline__ PairGeom pair_geom(float3 r, float r2, const ForceCon
 
 struct ForceAcc {
   float3 gx, gvh, gv, gn;
-  float grho, grhon, sv, ss;
+  float grho, grhon, sv, ss, sn;
 };
 
 // w . T_{i<-j} reversed (T from sph_force_3d_grid.wgsl:127-220, forward in
@@ -422,6 +427,8 @@ __device__ __forceinline__ void force_half(const ForceSide &I, const ForceSide &
   if (!JSIDE) {
     acc.grho += I.m ? (-alpha / I.rb) * Gwe : 0.0f;
     acc.grhon += I.mn ? (-c.mass * c.near_k * inv2) * Gwe : 0.0f;
+    // d alpha / d near_stiffness = -m (rho_near_i + rho_near_j) / (2 rho_i rho_near_j)
+    acc.sn += (-c.mass * (I.rnb + J.rnb) * inv2) * Gwe;
   } else {
     acc.grhon += J.mn ? (c.mass * Pn_i * inv2 / J.rnb) * Gwe : 0.0f;
   }
@@ -500,7 +507,7 @@ __device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const Sc
   (void)scene;
   ForceAcc acc;
   acc.gx = acc.gvh = acc.gv = acc.gn = f3(0.f, 0.f, 0.f);
-  acc.grho = acc.grhon = acc.sv = acc.ss = 0.f;
+  acc.grho = acc.grhon = acc.sv = acc.ss = acc.sn = 0.f;
   if (active) {
     const DevUniforms *U = v.u + scene;
     const ForceConst c = force_const(U->sph);
@@ -534,6 +541,7 @@ __device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const Sc
   }
   acc.sv = group_sum<L>(acc.sv);
   acc.ss = group_sum<L>(acc.ss);
+  acc.sn = group_sum<L>(acc.sn);
   acc.gx = group_sum3<L>(acc.gx);
   acc.gvh = group_sum3<L>(acc.gvh);
   acc.gv = group_sum3<L>(acc.gv);
@@ -546,10 +554,13 @@ __device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const Sc
   a.gv[q] = f4(acc.gv, 0.f);
   a.grho[q] = make_float2(acc.grho, acc.grhon);
   a.gn[q] = f4(acc.gn, 0.f);
-  // the particle's share of d/d viscosity and d/d surface tension, summed
-  // over steps in canonical order (FP64), reduced per scene at the end
-  double2 &gp = a.gpart[t.s2o[q]];
+  // the particle's share of d/d viscosity, d/d surface tension and d/d near
+  // stiffness, summed over steps in canonical order (FP64), reduced per
+  // scene at the end
+  const uint32_t o = t.s2o[q];
+  double2 &gp = a.gpart[o];
   gp = make_double2(gp.x + double(acc.sv), gp.y + double(acc.ss));
+  a.gpart2[o].x += double(acc.sn);
 }
 
 template <int L>
@@ -810,24 +821,33 @@ __global__ void __launch_bounds__(128)
 // Per-scene sums of the particles' parameter-gradient shares in a fixed
 // order: one block per scene, strided partial sums then a shared-memory tree.
 __global__ void __launch_bounds__(256)
-    k_reduce_params(const double2 *__restrict__ gpart, const uint32_t *__restrict__ scene_first,
-                    const uint32_t *__restrict__ scene_count, double *__restrict__ gparam) {
-  __shared__ double sv[256], ss[256];
+    k_reduce_params(const double2 *__restrict__ gpart, const double2 *__restrict__ gpart2,
+                    const uint32_t *__restrict__ scene_first,
+                    const uint32_t *__restrict__ scene_count, double *__restrict__ gparam,
+                    double *__restrict__ gparam2) {
+  __shared__ double sv[256], ss[256], sn[256], sd[256];
   const uint32_t sc = blockIdx.x;
   const uint32_t first = scene_first[sc], count = scene_count[sc];
-  double v = 0.0, w = 0.0;
+  double v = 0.0, w = 0.0, x = 0.0, y = 0.0;
   for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
     const double2 g = gpart[first + i];
+    const double2 g2 = gpart2[first + i];
     v += g.x;
     w += g.y;
+    x += g2.x;
+    y += g2.y;
   }
   sv[threadIdx.x] = v;
   ss[threadIdx.x] = w;
+  sn[threadIdx.x] = x;
+  sd[threadIdx.x] = y;
   __syncthreads();
   for (unsigned o = blockDim.x / 2; o > 0; o >>= 1) {
     if (threadIdx.x < o) {
       sv[threadIdx.x] += sv[threadIdx.x + o];
       ss[threadIdx.x] += ss[threadIdx.x + o];
+      sn[threadIdx.x] += sn[threadIdx.x + o];
+      sd[threadIdx.x] += sd[threadIdx.x + o];
     }
     __syncthreads();
   }
@@ -835,6 +855,8 @@ __global__ void __launch_bounds__(256)
     gparam[3 * sc + 0] = sv[0];
     gparam[3 * sc + 1] = 0.0;  // stiffness: read by no stage of the step
     gparam[3 * sc + 2] = ss[0];
+    gparam2[2 * sc + 0] = sn[0];
+    gparam2[2 * sc + 1] = sd[0];
   }
 }
 
@@ -858,11 +880,13 @@ inline unsigned blocks_for(uint32_t n, unsigned threads) { return (n + threads -
 
 }  // namespace
 
-cudaError_t launch_reduce_params(const double2 *gpart, const uint32_t *scene_first,
-                                 const uint32_t *scene_count, uint32_t scenes, double *gparam,
+cudaError_t launch_reduce_params(const double2 *gpart, const double2 *gpart2,
+                                 const uint32_t *scene_first, const uint32_t *scene_count,
+                                 uint32_t scenes, double *gparam, double *gparam2,
                                  cudaStream_t st) {
   if (scenes == 0) return cudaSuccess;
-  k_reduce_params<<<scenes, 256, 0, st>>>(gpart, scene_first, scene_count, gparam);
+  k_reduce_params<<<scenes, 256, 0, st>>>(gpart, gpart2, scene_first, scene_count, gparam,
+                                          gparam2);
   return cudaGetLastError();
 }
 

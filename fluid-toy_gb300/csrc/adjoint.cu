@@ -84,6 +84,7 @@ struct FsAdj {
   float4 *cot[2][2] = {};  // [buffer][0 = d/d pos, 1 = d/d vel], canonical
   int cur = 0;
   bool seeded = false;
+  std::vector<double> param_grads;  // last backward: FS_ADJ_NUM_PARAMS per scene
   // loss scratch
   float *field = nullptr, *target = nullptr, *gg = nullptr;
   double *loss = nullptr, *partial = nullptr;
@@ -156,7 +157,9 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
   v.gu[0] = c.take<float4>(N);
   v.gu[1] = c.take<float4>(N);
   v.gparam = c.take<double>(3 * size_t(a->scenes));
+  v.gparam2 = c.take<double>(2 * size_t(a->scenes));
   v.gpart = c.take<double2>(N);
+  v.gpart2 = c.take<double2>(N);
   a->scene_first = c.take<uint32_t>(a->scenes);
   a->scene_count = c.take<uint32_t>(a->scenes);
   v.counters = c.take<uint32_t>(kMaxAdjIters + 3);
@@ -326,6 +329,8 @@ int tune_lanes(FsAdj *a, const SceneView &v, const TapeView &tv) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   FS_CUDA(cudaMemsetAsync(a->av.gpart, 0, sizeof(double2) * a->N, s->stream),
+          "clear parameter gradients");
+  FS_CUDA(cudaMemsetAsync(a->av.gpart2, 0, sizeof(double2) * a->N, s->stream),
           "clear parameter gradients");
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tuned_lanes[key] = best;
@@ -570,6 +575,18 @@ int fs_adj_splat_mse_loss(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
   return FS_OK;
 }
 
+int fs_adj_param_gradients(FsAdj *a, double *out, uint32_t scenes) {
+  CHECK_ADJ(a);
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_adj_param_gradients: null output");
+  if (a->param_grads.empty())
+    return fail(FS_E_STATE, "fs_adj_param_gradients: no fs_adj_backward has run");
+  if (scenes != a->scenes)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_param_gradients: scene count %u, expected %u",
+                scenes, a->scenes);
+  std::memcpy(out, a->param_grads.data(), sizeof(double) * a->param_grads.size());
+  return FS_OK;
+}
+
 int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
                     double *dl_dparams) {
   CHECK_ADJ(a);
@@ -583,6 +600,8 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
     return fail(FS_E_STATE, "fs_adj_backward: parameters changed since fs_adj_forward");
   const uint32_t N = a->N, K = a->K;
   FS_CUDA(cudaMemsetAsync(a->av.gpart, 0, sizeof(double2) * N, s->stream),
+          "clear parameter gradients");
+  FS_CUDA(cudaMemsetAsync(a->av.gpart2, 0, sizeof(double2) * N, s->stream),
           "clear parameter gradients");
   {
     std::vector<uint32_t> first(a->scenes), count(a->scenes);
@@ -655,13 +674,32 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
       }
     }
   }
-  FS_CUDA(launch_reduce_params(a->av.gpart, a->scene_first, a->scene_count, a->scenes,
-                               a->av.gparam, s->stream),
+  FS_CUDA(launch_reduce_params(a->av.gpart, a->av.gpart2, a->scene_first, a->scene_count,
+                               a->scenes, a->av.gparam, a->av.gparam2, s->stream),
           "parameter gradients");
   if (dl_dparams)
     FS_CUDA(cudaMemcpyAsync(dl_dparams, a->av.gparam, sizeof(double) * 3 * a->scenes,
                             cudaMemcpyDeviceToHost, s->stream),
             "download parameter gradients");
+  a->param_grads.resize(size_t(FS_ADJ_NUM_PARAMS) * a->scenes);
+  {
+    std::vector<double> g3(3 * size_t(a->scenes)), g2(2 * size_t(a->scenes));
+    FS_CUDA(cudaMemcpyAsync(g3.data(), a->av.gparam, sizeof(double) * g3.size(),
+                            cudaMemcpyDeviceToHost, s->stream),
+            "download parameter gradients");
+    FS_CUDA(cudaMemcpyAsync(g2.data(), a->av.gparam2, sizeof(double) * g2.size(),
+                            cudaMemcpyDeviceToHost, s->stream),
+            "download parameter gradients");
+    FS_CUDA(cudaStreamSynchronize(s->stream), "download parameter gradients");
+    for (uint32_t k = 0; k < a->scenes; k++) {
+      double *o = a->param_grads.data() + size_t(FS_ADJ_NUM_PARAMS) * k;
+      o[0] = g3[3 * size_t(k)];
+      o[1] = g3[3 * size_t(k) + 1];
+      o[2] = g3[3 * size_t(k) + 2];
+      o[3] = g2[2 * size_t(k)];
+      o[4] = g2[2 * size_t(k) + 1];
+    }
+  }
   // leave the simulation at the rollout's final state
   if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, a->final_state, a->final_state + N, N)))
     return rc;

@@ -234,11 +234,13 @@ SIGNATURES = {
     "fs_adj_splat_mse_loss": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),
                                         _vp, C.c_int, _P(C.c_double)]),
     "fs_adj_backward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
+    "fs_adj_param_gradients": (C.c_int, [_vp, _vp, _u32]),
     "fs_adj_final_splat": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),
                                      _vp, C.c_int]),
 }
 FS_BATCH_MAX_SCENES = 65535
 FS_NOALLOC_SCAN_MAX_CELLS = 1 << 26
+FS_ADJ_NUM_PARAMS = 5
 
 _lib = None
 

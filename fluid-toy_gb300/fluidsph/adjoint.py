@@ -106,6 +106,15 @@ class DifferentiableRollout:
                                         dpar.ctypes.data))
         return dpos, dvel, dpar
 
+    PARAM_NAMES = ("viscosity", "stiffness", "surface_tension", "near_stiffness", "pcisph_delta")
+
+    def param_gradients(self, scenes: int = 1) -> np.ndarray:
+        """(scenes, 5) float64 gradients of the last backward() with respect
+        to PARAM_NAMES (fs_adj_param_gradients)."""
+        out = np.zeros((scenes, len(self.PARAM_NAMES)), np.float64)
+        check(self._lib.fs_adj_param_gradients(self._h, out.ctypes.data, int(scenes)))
+        return out
+
 
 def rollout_function():
     """torch.autograd.Function: (vel0 (N,3), viscosity, surface_tension) ->

@@ -208,12 +208,19 @@ def config4(seed: int = 0, num_scenes: int = 64, lo: int = 8192, hi: int = 32768
     """Batched parameter identification: `num_scenes` scenes set up as the
     batched ensemble (batch_scene) with counts log-uniform in [lo, hi], and per
     scene a hidden target: viscosity U[5, 25] and stiffness U[20, 50] (the
-    surface tension keeps the scene's own value). Returns (scenes, hidden)."""
+    surface tension keeps the scene's own value). The step reads no
+    `stiffness` (src/state/simulation.rs:326 sets it; pressure strength is
+    pcisph_delta, pcisph_solve.wgsl:178-179), so the hidden stiffness is
+    carried into the live pressure parameter: the hidden pcisph_delta is the
+    scene's delta times stiffness / 35 (35 = the configured stiffness).
+    Returns (scenes, hidden)."""
     scs = [batch_scene(k, seed + 4_000, lo, hi, steps) for k in range(num_scenes)]
     hidden = []
     for k in range(num_scenes):
         u = uniform01(seed * 1_000_003 + 104_729 * (k + 1), 2)
-        hidden.append({"viscosity": float(5.0 + 20.0 * u[0]), "stiffness": float(20.0 + 30.0 * u[1]),
+        stiff = float(20.0 + 30.0 * u[1])
+        hidden.append({"viscosity": float(5.0 + 20.0 * u[0]), "stiffness": stiff,
+                       "pcisph_delta": float(np.float32(scs[k].sph.pcisph_delta * stiff / 35.0)),
                        "surface_tension": float(scs[k].sph.surface_tension)})
     return scs, hidden
 
@@ -230,6 +237,7 @@ def reference_physics_batch(num_scenes: int = 64, steps: int = 20, seed: int = 0
         sc = reference_physics_rollout(nx, ny, nz, steps, seed + k)
         scs.append(sc)
         hidden.append({"viscosity": float(0.35 + 1.05 * u[3]), "stiffness": float(sc.sph.stiffness),
+                       "pcisph_delta": float(sc.sph.pcisph_delta),
                        "surface_tension": float(sc.sph.surface_tension)})
     return scs, hidden
 

@@ -612,6 +612,17 @@ int fs_adj_final_splat(FsAdj *adj, uint32_t scene, const GpuMcGridParams *grid,
  * unspecified until the next step). Synchronises. */
 int fs_adj_backward(FsAdj *adj, float *dl_dpos0, float *dl_dvel0, int on_device,
                     double *dl_dparams);
+/* No counterpart in the reference. The scalar-parameter gradients of the
+ * last fs_adj_backward, FS_ADJ_NUM_PARAMS doubles per scene (`scenes` must be
+ * the simulation's scene count), in the order viscosity, stiffness,
+ * surface_tension, near_stiffness, pcisph_delta. stiffness is read by no
+ * stage of the step (pressure strength comes from pcisph_delta,
+ * pcisph_solve.wgsl:178-179), so its gradient is 0; near_stiffness scales the
+ * near pressure of sph_force_3d_grid.wgsl:127, 180-183 and pcisph_delta the
+ * pressure update of pcisph_solve.wgsl:178-179. Each per-particle share is
+ * FP32 and the sums are FP64. */
+#define FS_ADJ_NUM_PARAMS 5
+int fs_adj_param_gradients(FsAdj *adj, double *out, uint32_t scenes);
 
 /* ---- prefix scan without allocation -------------------------------------- */
 

@@ -84,6 +84,10 @@ def _bind(lib):
             getattr(lib, name).argtypes = [vp, vp]
         lib.or_set_gravity.argtypes = [vp, C.POINTER(C.c_float)]
         lib.or_set_iterations.argtypes = [vp, u32]
+        if hasattr(lib, "or_set_cells_f32"):  # the restatement only
+            lib.or_set_cells_f32.argtypes = [vp, C.c_int]
+            lib.or_track_terms.argtypes = [vp, C.c_int]
+            lib.or_get_term_magnitudes.argtypes = [vp, vp, u32]
         lib.or_clear_accum.argtypes = [vp]
         lib.or_get_particles.argtypes = [vp, vp, u32]
         lib.or_get_sorted.argtypes = [vp, vp, u32]
@@ -98,7 +102,8 @@ def _bind(lib):
             lib.or_spray_frame.argtypes = [vp, vp, vp, vp, vp, vp]
         if hasattr(lib, "or_tangent_rollout_loss"):
             lib.or_tangent_rollout_loss.argtypes = [vp, u32, vp, vp, vp, u32, u32, vp, vp,
-                                                    C.c_double, C.c_double, vp, vp, C.c_int,
+                                                    C.c_double, C.c_double, C.c_double,
+                                                    C.c_double, vp, vp, C.c_int,
                                                     C.POINTER(C.c_double),
                                                     C.POINTER(C.c_double)]
         lib.or_max_threads.restype = C.c_int
@@ -117,10 +122,13 @@ def sincos_f32(x: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
 
 def tangent_rollout_loss(particles, sph_params, container_geom, gravity, iterations: int,
                          steps: int, mc_params, target, dpos=None, dvel=None,
-                         dvisc: float = 0.0, dst: float = 0.0, precision: int = 32):
+                         dvisc: float = 0.0, dst: float = 0.0, dnear: float = 0.0,
+                         ddelta: float = 0.0, precision: int = 32):
     """(L, dL) of L = mean((splat(x_T) - target)^2) after `steps` steps, with
-    dL its forward-mode derivative along (dpos, dvel, dvisc, dst): the oracle
-    on dual numbers (precision 32: the FP32 restatement's own trajectory)."""
+    dL its forward-mode derivative along (dpos, dvel, dvisc, dst, dnear,
+    ddelta) (viscosity, surface tension, near stiffness, PCISPH delta): the
+    oracle on dual numbers (precision 32: the FP32 restatement's own
+    trajectory)."""
     lib = load()
     parts = np.ascontiguousarray(particles, np.float32)
     g = (C.c_float * 3)(*gravity.direction)
@@ -132,7 +140,8 @@ def tangent_rollout_loss(particles, sph_params, container_geom, gravity, iterati
                                 C.addressof(container_geom), g, int(iterations), int(steps),
                                 None if dp is None else dp.ctypes.data,
                                 None if dv is None else dv.ctypes.data, float(dvisc),
-                                float(dst), C.addressof(mc_params), t.ctypes.data,
+                                float(dst), float(dnear), float(ddelta), C.addressof(mc_params),
+                                t.ctypes.data,
                                 int(precision), C.byref(loss), C.byref(dloss))
     return loss.value, dloss.value
 
@@ -201,6 +210,27 @@ class OracleSim:
 
     def set_pcisph_iterations(self, k: int):
         self._lib.or_set_iterations(self._h, int(k))
+
+    def track_terms(self, on: bool = True):
+        """Keep, per particle, the sums of the magnitudes of the terms that
+        the force pass, the last PCISPH iteration and the Akinci normal add
+        (see term_magnitudes)."""
+        self._lib.or_track_terms(self._h, 1 if on else 0)
+
+    def term_magnitudes(self) -> np.ndarray:
+        """(N, 3) float64, canonical order: sum over the force pass's pair
+        terms of their magnitudes (plus |gravity|), the same for the last
+        PCISPH iteration's pressure acceleration, and for the Akinci normal
+        (scaled like the normal). Comparing them with the magnitude of the
+        result gives the conditioning of each computed sum."""
+        out = np.zeros((self._n, 3), np.float64)
+        self._lib.or_get_term_magnitudes(self._h, out.ctypes.data, self._n)
+        return out
+
+    def set_cells_f32(self, on: bool = True):
+        """Hash cells in FP32 arithmetic (for the FP64 twin): the integer
+        stages then follow the FP32 pipeline's decisions."""
+        self._lib.or_set_cells_f32(self._h, 1 if on else 0)
 
     def clear_rigid_body_accum(self):
         self._lib.or_clear_accum(self._h)

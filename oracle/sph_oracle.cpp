@@ -167,6 +167,10 @@ template <class R, class = std::enable_if_t<std::is_arithmetic_v<R>>>
 inline R fabs_(R x) { return std::fabs(x); }
 template <class R> inline R len3(V3<R> a) { return sqrt_(dot3(a, a)); }
 template <class R> inline V3<R> normalize3(V3<R> a) { return a / len3(a); }
+template <class R> inline double norm_d(V3<R> a) {
+  const double x = double(a.x), y = double(a.y), z = double(a.z);
+  return std::sqrt(x * x + y * y + z * z);
+}
 template <class R> inline V3<R> cross3(V3<R> a, V3<R> b) {
   return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
@@ -309,8 +313,25 @@ struct Oracle {
   std::vector<float> sdf;                 // SDF texture texels (x fastest)
   uint32_t sdf_res = 1;
 
+  // Cell coordinates in FP32 arithmetic whatever R is (set on the FP64 twin
+  // for per-particle error reports: the integer stages then take the FP32
+  // pipeline's decisions, so only the continuous arithmetic differs).
+  bool cells_in_f32 = false;
+  // Per-particle sums of the magnitudes of the terms each sum adds (canonical
+  // order), kept when track_terms is set: the conditioning of the computed
+  // sums, for error reports (|sum| << sum of |terms| means cancellation).
+  bool track_terms = false;
+  std::vector<double> tmag_force, tmag_solve, tmag_normal;
   // grid_build.wgsl:33-44 / sph_density_3d_grid.wgsl:68-81
   inline void position_to_cell(V3<R> pos, int32_t c[3]) const {
+    if (cells_in_f32) {
+      const float lx = float(pos.x) - grid.ox, ly = float(pos.y) - grid.oy,
+                  lz = float(pos.z) - grid.oz;
+      c[0] = f2i_sat(double(std::floor(lx * grid.inv_cell_size)));
+      c[1] = f2i_sat(double(std::floor(ly * grid.inv_cell_size)));
+      c[2] = f2i_sat(double(std::floor(lz * grid.inv_cell_size)));
+      return;
+    }
     V3<R> l{pos.x - R(grid.ox), pos.y - R(grid.oy), pos.z - R(grid.oz)};
     c[0] = f2i_sat(double(floor_(l.x * R(grid.inv_cell_size))));
     c[1] = f2i_sat(double(floor_(l.y * R(grid.inv_cell_size))));
@@ -417,6 +438,7 @@ struct Oracle {
       V3<R> pos_i = S[s].pos;
       R density = R(0), near_density = R(0);
       V3<R> normal{R(0), R(0), R(0)};
+      double tnorm = 0.0;
       for_neighbors(pos_i, [&](uint32_t j) {
         V3<R> r_vec = pos_i - S[j].pos;
         R r_sq = dot3(r_vec, r_vec);
@@ -431,9 +453,11 @@ struct Oracle {
           if (r_sq > R(1e-12f)) {
             R diff2 = p.h2 - r_sq;
             normal = normal + m_over_rho0 * r_vec * diff2 * diff2;
+            if (track_terms) tnorm += norm_d(m_over_rho0 * r_vec * diff2 * diff2);
           }
         }
       });
+      if (track_terms) tmag_normal[s2o[s]] = tnorm * double(normal_scale);
       R gamma = boundary_gamma(pos_i);
       density = density / gamma;
       normal = normal * normal_scale;
@@ -487,6 +511,7 @@ struct Oracle {
       V3<R> n_i = S[s].normal;
       R near_pressure_i = p.near_k * near_density_i;
       V3<R> a_p{R(0), R(0), R(0)}, a_v{R(0), R(0), R(0)}, a_c{R(0), R(0), R(0)};
+      double tf = 0.0, tc = 0.0;
       for_neighbors(pos_i, [&](uint32_t j) {
         V3<R> pos_j = S[j].pos;
         V3<R> r_vec = pos_i - pos_j;
@@ -509,9 +534,13 @@ struct Oracle {
           R grad = scale_g * dg * dg;
           a_p = a_p + (-p.mass * (near_pressure_i + near_pressure_j) /
                        (R(2) * density_i * near_density_j)) * dir * grad;
+          if (track_terms)
+            tf += norm_d((-p.mass * (near_pressure_i + near_pressure_j) /
+                          (R(2) * density_i * near_density_j)) * dir * grad);
           if (r < min_dist) {
             R sep = R(200.0f) * (R(1) - r / min_dist);
             a_p = a_p + (-sep) * dir;
+            if (track_terms) tf += std::fabs(double(sep));
           }
           V3<R> vel_j = S[j].vel;
           V3<R> v_ij = vel_i - vel_j;
@@ -522,6 +551,7 @@ struct Oracle {
             R avg_density = (density_i + density_j) * R(0.5f);
             R pi_visc = -p.visc * mu / avg_density;
             a_v = a_v + (-p.mass * pi_visc * grad) * dir;
+            if (track_terms) tf += norm_d((-p.mass * pi_visc * grad) * dir);
           }
           R K_ij = R(2) * p.rho0 / (density_i + density_j);
           // akinci_cohesion_kernel, sph_force_3d_grid.wgsl:77-88
@@ -535,8 +565,14 @@ struct Oracle {
           a_c = a_c + (p.mass * K_ij * coh) * dir;
           V3<R> n_j = S[j].normal;
           a_c = a_c - (p.mass * K_ij) * (n_i - n_j);
+          if (track_terms)
+            tc += norm_d((p.mass * K_ij * coh) * dir) + norm_d((p.mass * K_ij) * (n_i - n_j));
         }
       });
+      if (track_terms)
+        tmag_force[orig] = tf + tc * std::fabs(double(p.st)) +
+                           std::sqrt(double(g0) * double(g0) + double(g1) * double(g1) +
+                                     double(g2) * double(g2));
       a_c = a_c * p.st;
       V3<R> a_g{g0, g1, g2};
       P[orig].force = a_p + a_v + a_c + a_g;
@@ -573,6 +609,7 @@ struct Oracle {
       V3<R> pos_i = P[orig].pos;
       R pred_density = R(0);
       V3<R> a_p{R(0), R(0), R(0)};
+      double ts = 0.0;
       for_neighbors(pos_i, [&](uint32_t j) {
         const Pred<R> &nb = in[j];
         V3<R> r_vec = pred_pos - nb.x;
@@ -589,9 +626,12 @@ struct Oracle {
             R dg = h - r;
             R grad = scale_g * dg * dg;
             a_p = a_p + (-p.mass * (old_p / (sd * sd) + np / (nd * nd)) * grad) * dir;
+            if (track_terms)
+              ts += norm_d((-p.mass * (old_p / (sd * sd) + np / (nd * nd)) * grad) * dir);
           }
         }
       });
+      if (track_terms) tmag_solve[orig] = ts;
       R density_error = fmax_(R(0), pred_density - p.rho0);
       R new_p = old_p + p.delta * density_error;
       R max_accel = R(0.25f) * h / (p.dt * p.dt);
@@ -1212,8 +1252,8 @@ template <class V>
 void tangent_loss_impl(const ParticleF *parts, uint32_t n, const SphParamsF *params,
                        const GeomF *geom, const float *gravity, uint32_t iterations,
                        uint32_t steps, const double *dpos, const double *dvel, double dvisc,
-                       double dst, const McGridF *mc, const float *target, double *loss,
-                       double *dloss) {
+                       double dst, double dnear, double ddelta, const McGridF *mc,
+                       const float *target, double *loss, double *dloss) {
   using R = Dual<V>;
   std::unique_ptr<Oracle<R>> o(create_impl<R>(parts, n, params, geom, 0, nullptr, 0));
   for (int a = 0; a < 3; a++) o->gravity[a] = R(gravity[a]);
@@ -1232,6 +1272,8 @@ void tangent_loss_impl(const ParticleF *parts, uint32_t n, const SphParamsF *par
   }
   o->p.visc.d = dvisc;
   o->p.st.d = dst;
+  o->p.near_k.d = dnear;
+  o->p.delta.d = ddelta;
   for (uint32_t k = 0; k < steps; k++) o->step(nullptr, nullptr);
   o->stage_hash();
   o->stage_scan();
@@ -1346,6 +1388,32 @@ void or_set_rigid(void *hv, const void *q) {
   auto *h = (Handle *)hv;
   DISPATCH(h, o->rigid = *(const RigidF *)q);
 }
+void or_track_terms(void *hv, int on) {
+  auto *h = (Handle *)hv;
+  DISPATCH(h, {
+    o->track_terms = on != 0;
+    const size_t n = o->P.size();
+    o->tmag_force.assign(n, 0.0);
+    o->tmag_solve.assign(n, 0.0);
+    o->tmag_normal.assign(n, 0.0);
+  });
+}
+// Term-magnitude sums of the last step, canonical order: force pass, last
+// PCISPH iteration's pressure acceleration, Akinci normal (3 doubles each).
+void or_get_term_magnitudes(void *hv, double *out, uint32_t n) {
+  auto *h = (Handle *)hv;
+  DISPATCH(h, {
+    for (uint32_t i = 0; i < n && i < o->tmag_force.size(); i++) {
+      out[3 * size_t(i)] = o->tmag_force[i];
+      out[3 * size_t(i) + 1] = o->tmag_solve[i];
+      out[3 * size_t(i) + 2] = o->tmag_normal[i];
+    }
+  });
+}
+void or_set_cells_f32(void *hv, int on) {
+  auto *h = (Handle *)hv;
+  DISPATCH(h, o->cells_in_f32 = on != 0);
+}
 void or_set_iterations(void *hv, uint32_t it) {
   auto *h = (Handle *)hv;
   DISPATCH(h, o->iterations = std::max(it, 1u));
@@ -1429,16 +1497,16 @@ void or_get_grid(void *hv, void *out) {
 void or_tangent_rollout_loss(const void *particles, uint32_t n, const void *params,
                              const void *geom, const float *gravity, uint32_t iterations,
                              uint32_t steps, const double *dpos, const double *dvel, double dvisc,
-                             double dst, const void *mc, const float *target, int precision,
-                             double *loss, double *dloss) {
+                             double dst, double dnear, double ddelta, const void *mc,
+                             const float *target, int precision, double *loss, double *dloss) {
   if (precision == 64)
     tangent_loss_impl<double>((const ParticleF *)particles, n, (const SphParamsF *)params,
                               (const GeomF *)geom, gravity, iterations, steps, dpos, dvel, dvisc,
-                              dst, (const McGridF *)mc, target, loss, dloss);
+                              dst, dnear, ddelta, (const McGridF *)mc, target, loss, dloss);
   else
     tangent_loss_impl<float>((const ParticleF *)particles, n, (const SphParamsF *)params,
                              (const GeomF *)geom, gravity, iterations, steps, dpos, dvel, dvisc,
-                             dst, (const McGridF *)mc, target, loss, dloss);
+                             dst, dnear, ddelta, (const McGridF *)mc, target, loss, dloss);
 }
 
 // One whitewater frame (FP32 restatement): emit, ceiling update, simulate.

@@ -4,8 +4,10 @@ differences of the same discretisation.
 Loss: the mean squared difference between the density splat of the final
 positions (over the scene's box) and a hidden run's (different viscosity).
 Checked quantities: dL/dviscosity, dL/dsurface_tension, dL/dstiffness (0: no
-stage reads it) and the initial-velocity and initial-position gradients
-along random directions.
+stage reads it), dL/dnear_stiffness and dL/dpcisph_delta (the live pressure
+parameters: near pressure in the force pass, the PCISPH pressure update) and
+the initial-velocity and initial-position gradients along random
+directions.
 
 * The rollout with the reference application's default physics (2,048
   particles, 20 steps, checkpoint every 6): the loss is smooth, so the GPU
@@ -52,9 +54,12 @@ def _target(oracle_mod, sc, mc, steps, **hidden):
     return o.density_splat(mc, sc.geom).astype(np.float32)
 
 
-def _oracle_loss(oracle_mod, sc, mc, target, steps, visc=None, st=None, vel=None):
+def _oracle_loss(oracle_mod, sc, mc, target, steps, visc=None, st=None, vel=None, near=None,
+                 delta=None):
     p = _with(sc.sph, viscosity=sc.sph.viscosity if visc is None else visc,
-              surface_tension=sc.sph.surface_tension if st is None else st)
+              surface_tension=sc.sph.surface_tension if st is None else st,
+              near_stiffness=sc.sph.near_stiffness if near is None else near,
+              pcisph_delta=sc.sph.pcisph_delta if delta is None else delta)
     parts = sc.particles.copy()
     if vel is not None:
         parts[:, 4:7] = vel
@@ -75,9 +80,12 @@ def _gpu_grad(sc, mc, target, steps, every=6, tape_budget=0, info=None):
     r.forward(steps)
     loss = r.splat_mse_loss(mc, sc.geom, target)
     dpos, dvel, dpar = r.backward()
+    full = r.param_gradients()
+    # the five-parameter read-out repeats the backward's three
+    assert np.array_equal(full[:, :3], dpar)
     if info is not None:
         info.append(r.tape_info())
-    return loss, dpos.astype(np.float64), dvel.astype(np.float64), dpar
+    return loss, dpos.astype(np.float64), dvel.astype(np.float64), full
 
 
 def _tangent(oracle_mod, sc, mc, target, steps, precision, **seed):
@@ -134,6 +142,26 @@ def test_smooth_parameter_gradients(smooth, oracle_mod):
             assert _rel(g, fd) < FD_RTOL
 
 
+def test_smooth_pressure_parameter_gradients(smooth, oracle_mod):
+    """dL/dnear_stiffness and dL/dpcisph_delta (the pressure strength the
+    step actually reads) equal the FP32 tangent of the same trajectory; over
+    5 steps they also match the FP64 tangent and FD64 (eps 1e-4)."""
+    sc, mc, target, (_, _, _, dpar) = smooth
+    for idx, name, kw, seed in ((3, "near_stiffness", "near", "dnear"),
+                                (4, "pcisph_delta", "delta", "ddelta")):
+        t32 = _tangent(oracle_mod, sc, mc, target, sc.steps, 32, **{seed: 1.0})
+        t64 = _tangent(oracle_mod, sc, mc, target, sc.steps, 64, **{seed: 1.0})
+        fd = _fd(oracle_mod, sc, mc, target, kw, getattr(sc.sph, name))
+        g = dpar[0, idx]
+        print(f"{sc.steps} steps dL/d{name}: reverse {g:.8e} tangent32 {t32:.8e} "
+              f"tangent64 {t64:.8e} FD64 {fd:.8e}")
+        assert g != 0.0
+        assert _rel(g, t32) < EXACT_RTOL
+        if sc.steps <= 5:
+            assert _rel(g, t64) < GRAD_RTOL
+            assert _rel(g, fd) < FD_RTOL
+
+
 def test_smooth_state_gradients(smooth, oracle_mod):
     sc, mc, target, (_, dpos, dvel, _) = smooth
     rng = np.random.default_rng(11)
@@ -171,6 +199,8 @@ def test_workload_copy_exact_derivative(oracle_mod, steps):
     assert dpar[0, 1] == 0.0
     assert _rel(dpar[0, 0], _tangent(oracle_mod, sc, mc, target, steps, 32, dvisc=1.0)) < EXACT_RTOL
     assert _rel(dpar[0, 2], _tangent(oracle_mod, sc, mc, target, steps, 32, dst=1.0)) < EXACT_RTOL
+    assert _rel(dpar[0, 3], _tangent(oracle_mod, sc, mc, target, steps, 32, dnear=1.0)) < EXACT_RTOL
+    assert _rel(dpar[0, 4], _tangent(oracle_mod, sc, mc, target, steps, 32, ddelta=1.0)) < EXACT_RTOL
     d = np.random.default_rng(3).standard_normal(dvel.shape)
     d /= np.linalg.norm(d)
     t = _tangent(oracle_mod, sc, mc, target, steps, 32, dvel=d)

@@ -1,5 +1,5 @@
 """The reverse pass on a batch: each scene's gradients (initial velocities,
-viscosity, surface tension) against the same scene's plain reverse pass, and
+viscosity, surface tension, near stiffness, PCISPH delta) against the same scene's plain reverse pass, and
 each scene's loss against its plain loss. The reverse gathers may pick a
 different lanes-per-particle variant for the batch's particle count (a
 different fixed summation order), so gradients agree to a stated relative
@@ -38,20 +38,22 @@ def test_batch_gradients_match_plain(oracle_mod):
     rb = DifferentiableRollout(b, 4)
     rb.forward(scs[0].steps)
     losses = [rb.splat_mse_loss(grids[k], scs[k].geom, targets[k], scene=k) for k in range(3)]
-    dpos_b, dvel_b, dpar_b = rb.backward(scenes=3)
+    dpos_b, dvel_b, _ = rb.backward(scenes=3)
+    dpar_b = rb.param_gradients(scenes=3)
     off = 0
     for k, s in enumerate(scs):
         sim = gpu_sim_for_scene(s)
         r = DifferentiableRollout(sim, 4)
         r.forward(s.steps)
         loss = r.splat_mse_loss(grids[k], s.geom, targets[k])
-        _, dvel, dpar = r.backward()
+        _, dvel, _ = r.backward()
+        dpar = r.param_gradients()
         assert loss == losses[k]
         n = s.n
         g_b = dvel_b[off:off + n].astype(np.float64)
         scale = np.abs(dvel).max()
         assert np.abs(g_b - dvel).max() <= RTOL * scale, k
-        for idx in (0, 2):
+        for idx in (0, 2, 3, 4):  # viscosity, surface tension, near stiffness, delta
             assert abs(dpar_b[k, idx] - dpar[0, idx]) <= RTOL * abs(dpar[0, idx]), (k, idx)
         assert dpar_b[k, 1] == 0.0
         off += n
