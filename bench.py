@@ -168,8 +168,20 @@ def make_scene(config: int):
     return scenes.CONFIGS[config]()
 
 
-def fp32_peak_tflops(device: int) -> tuple[float, str]:
+def fp32_peak_tflops(device: int) -> tuple[float, str, dict]:
+    """The FP32 roofline denominator: measured on this GPU by the library's
+    FP32 throughput kernel (fs_selftest_fp32_rate: independent fma.rn chains
+    at 32 warps per SM, best of five CUDA-event-timed launches); the nominal
+    152 SMs x 128 lanes x 2 FLOP x max SM clock only if that call fails."""
+    import ctypes as C
+
     import torch
+    from fluidsph import abi
+    rates = (C.c_double * 2)()
+    if abi.load().fs_selftest_fp32_rate(device, rates) == 0 and rates[0] > 0:
+        info = {"fma_tflops": round(rates[0], 2), "mul_add_tflops": round(rates[1], 2)}
+        return rates[0], ("measured: fs_selftest_fp32_rate (fma.rn chains, 32 warps/SM, "
+                          "CUDA events, best of 5)"), info
     p = torch.cuda.get_device_properties(device)
     sms = p.multi_processor_count
     mhz = 2070.0
@@ -181,7 +193,7 @@ def fp32_peak_tflops(device: int) -> tuple[float, str]:
     except Exception:
         pass
     peak = sms * 128 * 2 * mhz * 1e6 / 1e12
-    return peak, f"nominal: {sms} SMs x 128 FP32 lanes x 2 FLOP x {mhz:.0f} MHz"
+    return peak, f"nominal: {sms} SMs x 128 FP32 lanes x 2 FLOP x {mhz:.0f} MHz", {}
 
 
 def measured_peaks() -> dict:
@@ -220,6 +232,47 @@ def cpu_sample(scene, parts_np, steps: int, threads: int = 0) -> dict:
     dt = time.perf_counter() - t0
     return {"value": scene.n * steps / dt, "unit": METRIC, "cores": nthreads, "kind": "port",
             "seconds": dt, "steps": steps}
+
+
+def statistics_vs_fp64(scene, steps: int, dev: int, first: int = 105, every: int = 5,
+                       band: float = 0.01) -> dict:
+    """The multi-step check of the plain step: this library's rollout and the
+    oracle's FP64 twin (all host cores) over `steps` steps, flow statistics
+    (total mass, mean density deviation, mean kinetic energy, |v|^2
+    percentiles) sampled every `every` steps from step `first` and averaged;
+    the relative differences must stay within `band` (the rollouts are
+    chaotic, so trajectories are not compared)."""
+    from fluidsph.sim import SphSimulation3DGrid
+    from oracle import oracle
+    from oracle.flow_stats import NAMES, fp64_sample, gpu_sample
+    oracle.set_threads(0)
+    rho0, mass = float(scene.sph.rest_density), float(scene.sph.mass)
+    sim = SphSimulation3DGrid(scene.particles, scene.sph, scene.geom, device=dev)
+    sim.update_gravity(scene.gravity)
+    sim.set_pcisph_iterations(scene.iterations)
+    if scene.rigid is not None:
+        sim.update_rigid_body(scene.rigid)
+    o64 = oracle.oracle_for_scene(scene, precision=64)
+    gs, os_ = [], []
+    done, t_cpu = 0, 0.0
+    while done < steps:
+        k = min(every - done % every, steps - done)
+        sim.step(k)
+        t0 = time.perf_counter()
+        o64.step(k)
+        t_cpu += time.perf_counter() - t0
+        done += k
+        if done >= first and done % every == 0:
+            gs.append(gpu_sample(sim, rho0, mass, scene.geom))
+            os_.append(fp64_sample(o64, rho0, mass, scene.geom))
+    sim.close()
+    g, o = np.mean(gs, axis=0), np.mean(os_, axis=0)
+    rel = np.abs(g - o) / np.abs(o)
+    return {"steps": steps, "window": f"steps {first}..{steps}, every {every}", "band": band,
+            "gpu": dict(zip(NAMES, map(float, g))), "fp64": dict(zip(NAMES, map(float, o))),
+            "relative_difference": dict(zip(NAMES, map(float, rel))),
+            "within_band": bool(g[0] == o[0] and (rel[1:] <= band).all()),
+            "fp64_cpu_seconds": round(t_cpu, 1)}
 
 
 def run_ours(args, dist: Dist) -> dict | None:
@@ -336,7 +389,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         "force_predict": 6 * cand + 64 * nonself,
         "pcisph_solve": 6 * cand_s + 32 * hits_s,
     }
-    fp32_peak, fp32_src = fp32_peak_tflops(dev)
+    fp32_peak, fp32_src, fp32_rates = fp32_peak_tflops(dev)
     peaks = measured_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
@@ -365,6 +418,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                     "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4),
                     "traffic": traffic, "kernel": kernel_name, "launches_per_step": iters,
                     "flop_per_step": flops[dom], "peak_source": fp32_src,
+                    "peak_rates_measured": fp32_rates,
                     "flop_model": "6 per candidate pair test + per in-range pair 16 density, "
                                   "16 xsph, 64 force, 32 solve; counts measured each step"}
     else:
@@ -396,6 +450,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     }
     if forms is not None:
         out["forms"] = forms
+    if args.config == 0 and args.stats_steps > 0:
+        out["statistics_vs_fp64"] = statistics_vs_fp64(scene, args.stats_steps, dev)
     if state_after_warmup is not None:
         cs = cpu_sample(scene, state_after_warmup, args.cpu_steps)
         cs["sample"] = (f"{scene.name}: oracle (FP32 C++ restatement, OpenMP) from the GPU "
@@ -790,6 +846,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched and differentiable forms in the default run")
+    ap.add_argument("--stats-steps", type=int, default=1000,
+                    help="--config 0: steps of the rollout compared with the FP64 twin's "
+                         "flow statistics (0: skip)")
     ap.add_argument("--gd-iters", type=int, default=3,
                     help="gradient-descent iterations of the --config 4 workload")
     ap.add_argument("--loop-steps", type=int, default=20,

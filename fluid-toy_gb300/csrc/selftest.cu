@@ -68,8 +68,83 @@ __global__ void __launch_bounds__(256) k_check_div(unsigned long long *bad) {
   atomicAdd(bad + 3, n_in);
 }
 
+// ---- FP32 pipe throughput ---------------------------------------------------
+// Eight independent dependency chains per thread, kFp32Unroll steps each per
+// loop iteration. FUSED: one fma.rn per step (2 FLOP); otherwise one FMUL
+// and one FADD per step (2 FLOP in two instructions: the non-contracted
+// arithmetic the bit-exact kernels compile to under -fmad=false). The
+// result is written so that nothing is eliminated.
+constexpr int kFp32Unroll = 16;
+
+template <bool FUSED>
+__global__ void __launch_bounds__(256) k_fp32_rate(float *__restrict__ out, float b, float c,
+                                                  int iters) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) a[k] = float(t & 1023u) * 1e-3f + float(k);
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int u = 0; u < kFp32Unroll; u++) {
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        if (FUSED) {
+          a[k] = __fmaf_rn(a[k], b, c);
+        } else {
+          a[k] = __fmul_rn(a[k], b);
+          a[k] = __fadd_rn(a[k], c);
+        }
+      }
+    }
+  }
+  float sum = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 8; k++) sum += a[k];
+  out[t] = sum;
+}
+
 }  // namespace
 }  // namespace fs
+
+extern "C" int fs_selftest_fp32_rate(int device, double tflops[2]) {
+  if (!tflops) return FS_E_INVALID_ARGUMENT;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return FS_E_NO_DEVICE;
+  if (device < 0 || device >= count) return FS_E_INVALID_ARGUMENT;
+  if (cudaSetDevice(device) != cudaSuccess) return FS_E_CUDA;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return FS_E_CUDA;
+  const int blocks = sms * 4, threads = 256;  // 32 warps per SM
+  const int iters = 16384;
+  float *out = nullptr;
+  if (cudaMalloc(&out, sizeof(float) * size_t(blocks) * threads) != cudaSuccess) return FS_E_CUDA;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const double flop = 2.0 * 8.0 * fs::kFp32Unroll * double(iters) * blocks * threads;
+  for (int fused = 1; fused >= 0 && e == cudaSuccess; fused--) {
+    float best = 0.0f;
+    for (int rep = 0; rep < 6 && e == cudaSuccess; rep++) {  // first launch warms up
+      e = cudaEventRecord(e0);
+      if (fused)
+        fs::k_fp32_rate<true><<<blocks, threads>>>(out, 0.999999f, 1e-7f, iters);
+      else
+        fs::k_fp32_rate<false><<<blocks, threads>>>(out, 0.999999f, 1e-7f, iters);
+      if (e == cudaSuccess) e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaEventRecord(e1);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0 && (best == 0.0f || ms < best)) best = ms;
+    }
+    tflops[fused ? 0 : 1] = best > 0.0f ? flop / (double(best) * 1e-3) / 1e12 : 0.0;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  return e == cudaSuccess ? FS_OK : FS_E_CUDA;
+}
 
 extern "C" int fs_selftest_arithmetic(int device, unsigned long long results[4]) {
   if (!results) return FS_E_INVALID_ARGUMENT;

@@ -205,6 +205,7 @@ SIGNATURES = {
     "fs_load_batching": (C.c_int, [_vp, _P(C.c_int), _P(C.c_int)]),
     "fs_selftest_arithmetic": (C.c_int, [C.c_int, _P(C.c_ulonglong)]),
     "fs_selftest_scan_wait": (C.c_int, [_vp, C.c_int, _vp]),
+    "fs_selftest_fp32_rate": (C.c_int, [C.c_int, _P(C.c_double)]),
     "fs_batch_create": (C.c_int, [_vp, _P(_u32), _u32, _vp, _vp, _vp, _u32, C.c_int, _u32,
                                   _P(_vp)]),
     "fs_batch_num_scenes": (C.c_int, [_vp, _P(_u32)]),

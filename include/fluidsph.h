@@ -679,6 +679,15 @@ int fs_selftest_scan_wait(FsSim *sim, int inject, uint32_t *starts_out);
  * hold for. Synchronous, tens of milliseconds. */
 int fs_selftest_arithmetic(int device, unsigned long long results[4]);
 
+/* No counterpart in the reference. Measured FP32 pipe throughput of
+ * `device`, the denominator of the neighbour passes' FP32 roofline:
+ * tflops[0] = fused multiply-add (2 FLOP per instruction), tflops[1] =
+ * separate multiply and add (the non-contracted arithmetic that bit-exact
+ * kernels compile to). Each is the best of five timed launches of eight
+ * independent dependency chains per thread at 32 warps per SM. Synchronous,
+ * about 0.2 s. */
+int fs_selftest_fp32_rate(int device, double tflops[2]);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
