@@ -362,6 +362,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         import argparse as _ap
         b = run_batch(_ap.Namespace(steps=50, warmup=3, loop_steps=10), dist)
         a = run_adjoint(_ap.Namespace(steps=200, warmup=3), dist)
+        ident = run_identify(_ap.Namespace(gd_iters=3, identify_only=True), dist)
         if dist.rank == 0:
             forms = {
                 "batched": {k: b[k] for k in ("value", "unit", "ms_per_step", "looped_plain",
@@ -370,6 +371,8 @@ def run_ours(args, dist: Dist) -> dict | None:
                 "adjoint": {k: a[k] for k in ("value", "unit", "forward_ms_per_step",
                                               "fwd_adjoint_over_forward", "gradient_finite",
                                               "config")},
+                "batched_adjoint": {k: ident[k] for k in ("value", "unit", "forward_ms_per_step",
+                                                          "fwd_adjoint_over_forward", "config")},
             }
 
     if dist.rank != 0:
@@ -747,16 +750,28 @@ def run_identify(args, dist: Dist) -> dict | None:
     fwd_ms = e0.elapsed_time(e1) / 150
     b.close()
     spec = _identify(scs, hidden, 150, 15, args.gd_iters, 64, dev)
-    # the same with a tape budget of half the free device memory: the forward
-    # records as many checkpoint segments as fit and the backward re-runs only
-    # the others (timing only: two iterations)
-    free, _ = torch.cuda.mem_get_info(dev)
-    budget = int(free * 0.5)
-    budgeted = _identify(scs, hidden, 150, 15, 2, 64, dev, tape_budget=budget)
-    well = _identify(*S.reference_physics_batch(64, 20), 20, 5, 50, 32, dev)
+    budgeted = well = None
+    if not getattr(args, "identify_only", False):
+        # the same with a tape budget of half the free device memory: the
+        # forward records as many checkpoint segments as fit and the backward
+        # re-runs only the others (timing only: two iterations)
+        free, _ = torch.cuda.mem_get_info(dev)
+        budget = int(free * 0.5)
+        budgeted = _identify(scs, hidden, 150, 15, 2, 64, dev, tape_budget=budget)
+        well = _identify(*S.reference_physics_batch(64, 20), 20, 5, 50, 32, dev)
     if dist.rank != 0:
         return None
     v = spec["fwd_adjoint_ms_per_step"]
+    if budgeted is None:
+        return {"metric": "batched fwd+adjoint ms/step", "value": round(v, 4), "unit": "ms/step",
+                "forward_ms_per_step": round(fwd_ms, 4),
+                "fwd_adjoint_over_forward": round(v / fwd_ms, 3),
+                "config": {"workload": "batched_identification_64_scenes", "scenes": len(scs),
+                           "particles": total, "steps": 150, "checkpoint_every": 15,
+                           "tape_budget": 0, "gd_iterations": args.gd_iters,
+                           "timing": "median over the iterations of fs_adj_forward(150) + "
+                                     "losses + fs_adj_backward, wall clock"},
+                "identification": spec}
     return {
         "metric": "batched fwd+adjoint ms/step", "value": round(v, 4), "unit": "ms/step",
         "n_gpus": dist.world, "steps": 150, "warmup": 0, "ms_per_step": round(v, 4),
