@@ -205,6 +205,31 @@ int fs_mc_grid_params(const float grid_min[3], const float grid_max[3], uint32_t
   return FS_OK;
 }
 
+int fs_spawn_positions(const float position[3], uint32_t count, float spread,
+                       uint32_t num_particles, uint32_t max_particles, SphParticle3D *out,
+                       uint32_t *spawned) {
+  if (!position || !spawned) return FS_E_INVALID_ARGUMENT;
+  *spawned = 0;
+  if (num_particles > max_particles) return FS_E_INVALID_ARGUMENT;
+  const uint32_t available = max_particles - num_particles;
+  const uint32_t spawn = std::min(count, available);
+  if (spawn == 0) return FS_OK;
+  if (!out) return FS_E_INVALID_ARGUMENT;
+  // golden-angle spiral in layers of 20, sph_3d_grid.rs:1546-1557; the
+  // records are SphParticle3D::new (particle.rs:19-31): zero but the position
+  for (uint32_t i = 0; i < spawn; i++) {
+    const float angle = float(i) * 2.39996f;
+    const float r = spread * std::sqrt(float(i) / float(spawn));
+    const uint32_t layer = i / 20u;
+    std::memset(&out[i], 0, sizeof(SphParticle3D));
+    out[i].position[0] = position[0] + r * std::cos(angle);
+    out[i].position[1] = position[1] + float(layer) * spread * 0.3f;
+    out[i].position[2] = position[2] + r * std::sin(angle);
+  }
+  *spawned = spawn;
+  return FS_OK;
+}
+
 int fs_rigid_body_to_gpu(const FsRigidBodyState *state, GpuRigidBody *out) {
   if (!state || !out) return FS_E_INVALID_ARGUMENT;
   fs::rb::to_gpu(*state, *out);

@@ -843,17 +843,11 @@ int fs_spawn_particles(FsSim *s, const float position[3], uint32_t count, float 
   if (spawn == 0) return FS_OK;
   int rc;
   if ((rc = set_device(s))) return rc;
-  // golden-angle spiral in layers of 20, sph_3d_grid.rs:1546-1557
+  // the records of sph_3d_grid.rs:1543-1557 (fs_spawn_positions)
   std::vector<SphParticle3D> np(spawn);
-  for (uint32_t i = 0; i < spawn; i++) {
-    const float angle = float(i) * 2.39996f;
-    const float r = spread * std::sqrt(float(i) / float(spawn));
-    const uint32_t layer = i / 20u;
-    std::memset(&np[i], 0, sizeof(SphParticle3D));
-    np[i].position[0] = position[0] + r * std::cos(angle);
-    np[i].position[1] = position[1] + float(layer) * spread * 0.3f;
-    np[i].position[2] = position[2] + r * std::sin(angle);
-  }
+  uint32_t made = 0;
+  if ((rc = fs_spawn_positions(position, count, spread, n, s->max_n, np.data(), &made)))
+    return fail(rc, "fs_spawn_particles: spawn positions");
   if ((rc = write_particles(s, np.data(), n, spawn))) return rc;
   s->scene_n[0] = n + spawn;
   if ((rc = upload_uniforms(s))) return rc;

@@ -187,6 +187,7 @@ SIGNATURES = {
     "fs_num_particles": (C.c_int, [_vp, _P(_u32)]),
     "fs_grid_params": (C.c_int, [_vp, _P(GpuGridParams)]),
     "fs_spawn_particles": (C.c_int, [_vp, _P(_f), _u32, _f, _P(_u32)]),
+    "fs_spawn_positions": (C.c_int, [_P(C.c_float), _u32, C.c_float, _u32, _u32, _vp, _P(_u32)]),
     "fs_download_particles": (C.c_int, [_vp, _vp, _u32]),
     "fs_download_sorted": (C.c_int, [_vp, _vp, _u32]),
     "fs_download_cells": (C.c_int, [_vp, _vp, _vp, _u32]),

@@ -359,6 +359,16 @@ int fs_grid_params(const FsSim *sim, GpuGridParams *out);
  * capacity; *spawned receives the count actually added. */
 int fs_spawn_particles(FsSim *sim, const float position[3], uint32_t count,
                        float spread, uint32_t *spawned);
+/* The particle records spawn_particles (sph_3d_grid.rs:1543-1557) builds
+ * before writing them, on the host, for a simulation that holds
+ * num_particles of max_particles: *spawned = min(count, max - num) records
+ * on a golden-angle spiral around `position` (radius spread * sqrt(i / n),
+ * layers of 20 stacked 0.3 spread apart), zero but the position
+ * (SphParticle3D::new, particle.rs:19-31). out holds *spawned records.
+ * fs_spawn_particles writes exactly these. No GPU. */
+int fs_spawn_positions(const float position[3], uint32_t count, float spread,
+                       uint32_t num_particles, uint32_t max_particles, SphParticle3D *out,
+                       uint32_t *spawned);
 
 /* ---- device-resident rigid-body coupling ----------------------------------- */
 

@@ -78,7 +78,74 @@ def translate_all() -> bool:
     return True
 
 
+# The reference's host-side functions on the step's path, translated from its
+# Rust sources by oracle/rs2cpp.py: (file, structs, enums, functions).
+HOST_FILES = ["src/state/simulation.rs", "src/state/rigid_body.rs", "src/simulation/particle.rs",
+              "src/simulation/sph_3d_grid.rs"]
+HOST_ENUMS = ["ContainerStyle", "RigidBodyShape"]
+HOST_STRUCTS = ["ContainerConfig", "SphConfig", "GpuSphParams3D", "GpuContainerGeometry",
+                "RigidBodyConfig", "GpuRigidBody", "GpuRigidBodyAccum", "SphParticle3D",
+                "GpuGridParams"]
+HOST_FNS = [
+    "compute_rest_density", "compute_pcisph_delta",             # simulation.rs:402-480
+    "SphConfig::rest_density", "SphConfig::to_gpu_params_3d",   # :308-337
+    "ContainerConfig::rotation_matrices", "ContainerConfig::to_gpu_geometry",  # :137-184
+    "ContainerConfig::half_width", "ContainerConfig::half_depth",
+    "RigidBodyShape::volume", "RigidBodyShape::moment_of_inertia",  # rigid_body.rs:28-80
+    "RigidBodyConfig::to_gpu_rigid_body",                       # :131-146
+    "quat_normalize", "quat_mul", "quat_to_rotation_rows",      # :166-205
+    "integrate_rigid_body", "rotated_aabb_half_extents",        # :277-396
+    "clamp_rigid_body_to_container",                            # :400-479
+    "SphParticle3D::new",                                       # particle.rs:19-31
+    "SphSimulation3DGrid::spawn_particles",                     # sph_3d_grid.rs:1534-1569
+]
+
+
+def translate_host() -> bool:
+    root = reference_root()
+    if not all((root / f).exists() for f in HOST_FILES):
+        return False
+    sys.path.insert(0, str(HERE))
+    from rs2cpp import Translator, parse_file
+    mods = [parse_file(root / f) for f in HOST_FILES]
+    body = Translator(mods).translate(HOST_STRUCTS, HOST_ENUMS, HOST_FNS, "refhost",
+                                      after_structs='#include "../ref_host_shims.hpp"')
+    text = ("// generated by oracle/rs2cpp.py from the reference's Rust sources; do not edit\n"
+            "#pragma once\n#include \"../rs_runtime.hpp\"\n\n" + body)
+    OUT.mkdir(exist_ok=True)
+    dst = OUT / "ref_host.hpp"
+    if not dst.exists() or dst.read_text() != text:
+        dst.write_text(text)
+    return True
+
+
+def build_host(quiet: bool = False, force: bool = False) -> Path | None:
+    """oracle/_ref/libref_host.so: the translated host functions behind the C
+    ABI of ref_host_driver.cpp."""
+    translated = translate_host()
+    hdr = OUT / "ref_host.hpp"
+    if not hdr.exists():
+        return None
+    lib = OUT / "libref_host.so"
+    deps = [hdr, HERE / "ref_host_driver.cpp", HERE / "rs_runtime.hpp",
+            HERE / "ref_host_shims.hpp"]
+    if lib.exists() and not force and all(lib.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return lib
+    cxx = shutil.which("g++") or "c++"
+    tmp = lib.with_suffix(".so.tmp")
+    r = subprocess.run([cxx, "-std=c++20", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+                        "-shared", "-I", str(OUT), "-o", str(tmp),
+                        str(HERE / "ref_host_driver.cpp")], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host translation failed to compile:\n{r.stderr[-4000:]}")
+    os.replace(tmp, lib)
+    if not quiet:
+        print(f"built {lib} ({'translated now' if translated else 'from an earlier translation'})")
+    return lib
+
+
 def build(quiet: bool = False, force: bool = False) -> Path | None:
+    build_host(quiet, force)
     translated = translate_all()
     hdr = OUT / "ref_shaders.hpp"
     if not hdr.exists():

@@ -63,6 +63,45 @@ def load_ref():
     return _ref_lib
 
 
+_ref_host = None
+REF_HOST_LIB = HERE / "_ref" / "libref_host.so"
+
+
+def load_ref_host():
+    """The reference's host functions (parameter builders, rigid-body
+    integration, spawning) translated from its Rust sources (oracle/_ref), or
+    None when they are not built (the reference sources are needed once)."""
+    global _ref_host
+    if _ref_host is None:
+        try:
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("build_ref", HERE / "build_ref.py")
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build_host(quiet=True)
+        except Exception:
+            pass
+        if not REF_HOST_LIB.exists():
+            return None
+        lib = C.CDLL(str(REF_HOST_LIB))
+        f, u32, vp, i = C.c_float, C.c_uint32, C.c_void_p, C.c_int
+        fp = C.POINTER(C.c_float)
+        lib.rh_compute_rest_density.restype = f
+        lib.rh_compute_rest_density.argtypes = [f, f]
+        lib.rh_compute_pcisph_delta.restype = f
+        lib.rh_compute_pcisph_delta.argtypes = [f, f, f, f]
+        lib.rh_to_gpu_params_3d.argtypes = [f, f, f, f, f, f, f, u32, f, vp]
+        lib.rh_to_gpu_geometry.argtypes = [fp, f, f, i, f, vp]
+        lib.rh_quat_to_rotation_rows.argtypes = [fp, fp]
+        lib.rh_to_gpu_rigid_body.argtypes = [vp, f, vp]
+        lib.rh_integrate_rigid_body.argtypes = [vp, fp, f, u32, fp, vp]
+        lib.rh_clamp_rigid_body.argtypes = [vp, fp, i]
+        lib.rh_spawn_particles.restype = u32
+        lib.rh_spawn_particles.argtypes = [u32, u32, fp, u32, f, vp, C.POINTER(u32)]
+        _ref_host = lib
+    return _ref_host
+
+
 def load():
     global _lib
     if _lib is None:

@@ -217,6 +217,17 @@ def test_empty_and_spawn(fslib, oracle_mod, sc):
     assert sim.num_particles() == 300
     p = sim.particles()
     assert np.isfinite(p).all()
+    # the records are fs_spawn_positions' (pinned to the reference's
+    # spawn_particles by tests/test_ref_pin_host.py), byte for byte
+    import ctypes as C
+    want = np.zeros((300, 16), np.float32)
+    got = C.c_uint32()
+    pos = (C.c_float * 3)(0.0, 0.3, 0.0)
+    assert fslib.fs_spawn_positions(pos, 250, C.c_float(0.05), 0, 300, want.ctypes.data,
+                                    C.byref(got)) == 0 and got.value == 250
+    assert fslib.fs_spawn_positions(pos, 100, C.c_float(0.05), 250, 300,
+                                    want[250:].ctypes.data, C.byref(got)) == 0 and got.value == 50
+    assert p.tobytes() == want.tobytes()
     # the spawned block then steps like any other input
     params = scene.sph
     params.num_particles = 300
