@@ -300,7 +300,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     sim.set_stream(stream.cuda_stream)
     sim.step(W)
     sim.prepare_steps(K)  # capture the step graphs outside the timed region
-    batched_loads, _ = sim.load_batching()
+    depths = sim.kernel_forms()
     sim.sync()
     state_after_warmup = sim.particles() if dist.rank == 0 and not args.no_cpu else None
     sim.neighbor_stats(reset=True)
@@ -438,7 +438,8 @@ def run_ours(args, dist: Dist) -> dict | None:
         "data": "synthetic (seeded SplitMix64 lattice jitter)",
         "config": {"workload": scene.name, "particles": n, "steps_timed": f"{W + 1}..{W + K}",
                    "kernel_radius": 0.08, "pcisph_iterations": scene.iterations,
-                   "density_solve_loads": "batched" if batched_loads else "plain",
+                   "load_depths": {k: depths[k] for k in ("density_loads", "xsph_loads",
+                                                          "solve_loads", "decided", "bucket")},
                    "parallelism": f"replicas{dist.world}" if dist.world > 1 else "single",
                    "l2": "state > 250 MB exceeds the 129 MB L2 (no flush)"},
         "roofline": roofline,
@@ -453,6 +454,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     }
     if forms is not None:
         out["forms"] = forms
+    from fluidsph.sim import kernel_forms_table
+    out["load_depth_table"] = kernel_forms_table()
     if args.config == 0 and args.stats_steps > 0:
         out["statistics_vs_fp64"] = statistics_vs_fp64(scene, args.stats_steps, dev)
     if state_after_warmup is not None:
@@ -508,6 +511,7 @@ def run_batch(args, dist: Dist) -> dict | None:
     b.stage_times(reset=True)
     b.step(min(K, 20))
     stages, timed = b.stage_times(reset=True)
+    depths = b.kernel_forms()
     b.close()
 
     # looped plain: the same scenes one after another on one stream, each for
@@ -543,6 +547,8 @@ def run_batch(args, dist: Dist) -> dict | None:
         "config": {"workload": f"batched_ensemble_{len(scenes)}_scenes", "scenes": len(scenes),
                    "particles": total, "count_range": [int(counts.min()), int(counts.max())],
                    "steps_timed": f"{W + 1}..{W + K}", "graph_capture_s": round(capture_s, 3),
+                   "load_depths": {k: depths[k] for k in ("density_loads", "xsph_loads",
+                                                          "solve_loads", "decided", "bucket")},
                    "l2": "state > 1 GB exceeds the 129 MB L2 (no flush)"},
         "stages_ms_per_step": per_step_ms,
         "looped_plain": {"value": round(loop_value, 1), "unit": METRIC, "steps": k_loop,

@@ -9,6 +9,19 @@
 
 namespace fs {
 
+// Load depths (candidate records in flight per lane) each neighbour pass is
+// instantiated for; see kLoadDepths / kXsphDepths in sph_kernels.cu.
+constexpr int kNumLoadDepths = 4;
+constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16};
+constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16};
+
+// The neighbour passes' load-depth choice of a simulation (indices into the
+// lists above).
+struct KernelForms {
+  uint8_t density = 0, solve = 0, xsph = 1;
+  uint32_t key() const { return uint32_t(density) | uint32_t(solve) << 8 | uint32_t(xsph) << 16; }
+};
+
 // Parameter block resident in device memory. The update_* entry points copy
 // their struct here with cudaMemcpyAsync on the simulation's stream, which
 // orders them before later steps exactly like the reference's
@@ -142,9 +155,10 @@ struct DevState {
   float *const *rec_rho = nullptr;   // [iterations + 1]
   float4 *const *rec_ap = nullptr;   // [iterations] pressure acceleration before the clamp
   uint32_t *rec_hits = nullptr;  // union over the PCISPH levels of their hit masks (density mask layout)
-  // density and solve: the instantiation with batched candidate loads (true)
-  // or the plain loop (false); the same results, chosen per workload by speed
-  bool batched_loads = false;
+  // neighbour-pass instantiations: indices into the passes' load-depth lists
+  // (kLoadDepths for density and solve, kXsphDepths for XSPH, sph_kernels.cu);
+  // the same results whatever they are, chosen per workload by speed
+  uint8_t load_density = 0, load_solve = 0, load_xsph = 1;
 };
 
 // Set the thread-local text fs_last_error() returns (sim.cu).

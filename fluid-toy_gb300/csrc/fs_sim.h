@@ -28,7 +28,7 @@ constexpr int kGraphSlots = 4;
 struct StepGraph {
   cudaGraphExec_t exec = nullptr;
   uint32_t steps = 0, n_canon = 0, n_sorted = 0, iters = 0;
-  bool batched_loads = false;
+  uint32_t forms = 0;  // KernelForms::key() the graph was captured with
   cudaStream_t stream = nullptr;
   uint64_t last_use = 0;
 };
@@ -56,15 +56,21 @@ struct FsSim {
   std::vector<uint8_t> coupled;  // scenes whose rigid body is device-coupled
   float *splat_buf = nullptr;  // device staging of host-bound density fields
   size_t splat_cap = 0;
-  // Load-batching choice of the density and solve passes (DevState::
-  // batched_loads, the same results either way): once the simulation has run
-  // 8 steps, its next four steps run as plain / batched / batched / plain,
-  // each between two events, whatever the fs_step call sizes; the next call
-  // waits for them once and keeps the faster instantiation.
-  bool batched_loads = false;
-  int tune_state = 0;  // 0 measuring (phase), 1 measured (events pending), 2 decided
-  int tune_phase = 0;  // measured steps so far
-  cudaEvent_t tune_ev[8] = {};
+  // Load depths of the neighbour passes (DevState::load_*, the same results
+  // whatever they are), tuned per particle-count bucket: a simulation whose
+  // bucket (floor(log2 hashed particles), one or many scenes, PCISPH
+  // iterations) is in the process-wide table takes its entry; otherwise,
+  // once it has run kTuneAfterSteps steps, its next kTuneSteps steps run each
+  // candidate depth twice (palindromic order) with events around the density,
+  // XSPH and solve stages, whatever the fs_step call sizes, the next call
+  // waits for them once, and each pass keeps its fastest depth, which also
+  // enters the table.
+  fs::KernelForms forms;
+  int tune_state = 0;   // 0 measuring (phase), 1 measured (events pending), 2 decided
+  int tune_source = 0;  // how the forms were decided: 1 measured, 2 table, 3 set by the caller
+  int tune_phase = 0;   // measured steps so far
+  cudaEvent_t tune_ev[2 * fs::kNumLoadDepths][FS_STAGE_COUNT] = {};
+  float tune_ms[3][fs::kNumLoadDepths] = {};  // measured ms per pass (density, XSPH, solve) and depth
   uint64_t steps_done = 0;
   // stage timing
   bool timing = false;
@@ -88,7 +94,11 @@ int set_device(FsSim *s);
 int check_device_error(FsSim *s);
 // Enqueue one step on the simulation's stream (on `dv`'s buffers if given;
 // batched loads as decided for the simulation, or as `batched` when 0 / 1).
-int enqueue_step(FsSim *s, bool timed, const DevState *dv = nullptr, int batched = -1);
+// One step on the simulation's stream. timed: stage events into s->ev;
+// marks (if not null): stage events into marks[0..FS_STAGE_COUNT) instead;
+// forms (if not null): these load depths instead of the simulation's.
+int enqueue_step(FsSim *s, bool timed, const DevState *dv = nullptr,
+                 const KernelForms *forms = nullptr, cudaEvent_t *marks = nullptr);
 // Enqueue only the grid build (clear, hash, scan, reorder) of the current state.
 int enqueue_grid_build(FsSim *s);
 

@@ -19,8 +19,11 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "fs_sim.h"
@@ -273,15 +276,23 @@ int write_particles(FsSim *s, const SphParticle3D *parts, uint32_t offset, uint3
 // One step: the stage sequence of step(), sph_3d_grid.rs:1261-1444, over all
 // scenes at once, on the simulation's buffers or on `dv` (the same buffers
 // with some replaced, e.g. by a recording for the reverse pass).
-int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv, int batched) {
+int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv, const KernelForms *forms,
+                     cudaEvent_t *marks) {
   const uint32_t n = s->hb.n_sorted;
   const uint32_t n_canon = s->hb.n_canon;
   const uint32_t G = s->cells_total;
   cudaStream_t st = s->stream;
   DevState d = dv ? *dv : s->d;
-  d.batched_loads = batched < 0 ? s->batched_loads : batched != 0;
+  const KernelForms &f = forms ? *forms : s->forms;
+  d.load_density = f.density;
+  d.load_solve = f.solve;
+  d.load_xsph = f.xsph;
   auto mark = [&](int i) -> int {
-    if (timed) FS_CUDA(cudaEventRecord(s->ev[i], st), "record stage event");
+    if (marks) {
+      if (i < FS_STAGE_COUNT) FS_CUDA(cudaEventRecord(marks[i], st), "record stage event");
+    } else if (timed) {
+      FS_CUDA(cudaEventRecord(s->ev[i], st), "record stage event");
+    }
     return FS_OK;
   };
   int rc;
@@ -328,40 +339,89 @@ namespace {
 
 // The graph of `steps` back-to-back steps for the current counts, captured
 // on first use (least recently used slot replaced).
-// The load-batching choice (FsSim::batched_loads): measured once the
-// simulation has run this many steps (the clumps of an over-compressed start
-// have formed by then).
+// The neighbour passes' load depths (FsSim::forms): a simulation's bucket
+// is looked up in the process-wide table first; if it is not there, the
+// depths are measured once the simulation has run this many steps (the clumps
+// of an over-compressed start have formed by then).
 constexpr uint64_t kTuneAfterSteps = 8;
+constexpr int kTuneSteps = 2 * kNumLoadDepths;
 
 bool capturing(FsSim *s) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   return cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
 }
 
-constexpr int kTuneSteps = 4;
+// The process-wide table: bucket -> depths and the times they were chosen by.
+struct TuneEntry {
+  KernelForms forms;
+  float ms[3][kNumLoadDepths];
+};
+std::mutex g_forms_mu;
+std::map<std::tuple<int, uint32_t, uint32_t, uint32_t>, TuneEntry> g_forms_table;
 
-// Wait for the four measured steps and keep the faster instantiation.
+std::tuple<int, uint32_t, uint32_t, uint32_t> tune_key(const FsSim *s) {
+  const uint32_t n = std::max(s->hb.n_sorted, 1u);
+  uint32_t bucket = 0;
+  while ((n >> (bucket + 1)) != 0u) bucket++;
+  return {s->device, bucket, s->scenes() > 1 ? 1u : 0u, s->iterations};
+}
+
+// Adopt the table's depths for this simulation's bucket, if it holds them.
+void tune_lookup(FsSim *s) {
+  if (s->tune_state != 0 || s->tune_phase != 0) return;
+  std::lock_guard<std::mutex> lk(g_forms_mu);
+  const auto it = g_forms_table.find(tune_key(s));
+  if (it == g_forms_table.end()) return;
+  s->forms = it->second.forms;
+  s->tune_state = 2;
+  s->tune_source = 2;
+}
+
+// Candidate c of measured step p: 0, 1, .., n-1, n-1, .., 0.
+int tune_candidate(int p) { return p < kNumLoadDepths ? p : kTuneSteps - 1 - p; }
+
+// Wait for the measured steps and keep each pass's fastest depth.
 int tune_decide(FsSim *s) {
   if (s->tune_state != 1 || capturing(s)) return FS_OK;
-  FS_CUDA(cudaEventSynchronize(s->tune_ev[2 * kTuneSteps - 1]), "load-batching measurement");
-  float t[kTuneSteps];
-  for (int p = 0; p < kTuneSteps; p++)
-    FS_CUDA(cudaEventElapsedTime(&t[p], s->tune_ev[2 * p], s->tune_ev[2 * p + 1]),
-            "load-batching measurement");
-  s->batched_loads = t[1] + t[2] < t[0] + t[3];
+  FS_CUDA(cudaEventSynchronize(s->tune_ev[kTuneSteps - 1][8]), "kernel-form measurement");
+  float ms[3][kNumLoadDepths] = {};
+  for (int p = 0; p < kTuneSteps; p++) {
+    const int c = tune_candidate(p);
+    float t[3];
+    // density (with the work-order kernels around it: the same for every depth),
+    // XSPH, the PCISPH solve iterations
+    FS_CUDA(cudaEventElapsedTime(&t[0], s->tune_ev[p][4], s->tune_ev[p][5]), "kernel-form measurement");
+    FS_CUDA(cudaEventElapsedTime(&t[1], s->tune_ev[p][5], s->tune_ev[p][6]), "kernel-form measurement");
+    FS_CUDA(cudaEventElapsedTime(&t[2], s->tune_ev[p][7], s->tune_ev[p][8]), "kernel-form measurement");
+    for (int k = 0; k < 3; k++) ms[k][c] += t[k];
+  }
+  uint8_t best[3] = {0, 0, 0};
+  for (int k = 0; k < 3; k++)
+    for (int c = 1; c < kNumLoadDepths; c++)
+      if (ms[k][c] < ms[k][best[k]]) best[k] = uint8_t(c);
+  s->forms.density = best[0];
+  s->forms.xsph = best[1];
+  s->forms.solve = best[2];
+  std::memcpy(s->tune_ms, ms, sizeof(ms));
   s->tune_state = 2;
+  s->tune_source = 1;
+  std::lock_guard<std::mutex> lk(g_forms_mu);
+  TuneEntry e;
+  e.forms = s->forms;
+  std::memcpy(e.ms, ms, sizeof(ms));
+  g_forms_table[tune_key(s)] = e;
   return FS_OK;
 }
 
-// Run the measured steps that are due (plain / batched / batched / plain),
-// consuming them from nsteps.
+// Run the measured steps that are due, consuming them from nsteps.
 int tune_steps(FsSim *s, uint32_t &nsteps) {
   while (nsteps > 0 && s->tune_state == 0 && s->steps_done >= kTuneAfterSteps) {
     const int p = s->tune_phase;
-    FS_CUDA(cudaEventRecord(s->tune_ev[2 * p], s->stream), "load-batching measurement");
-    const int rc = enqueue_step(s, false, nullptr, (p == 1 || p == 2) ? 1 : 0);
+    const int c = tune_candidate(p);
+    KernelForms f;
+    f.density = f.solve = f.xsph = uint8_t(c);
+    const int rc = enqueue_step(s, false, nullptr, &f, s->tune_ev[p]);
     if (rc) return rc;
-    FS_CUDA(cudaEventRecord(s->tune_ev[2 * p + 1], s->stream), "load-batching measurement");
     s->steps_done++;
     nsteps--;
     if (++s->tune_phase == kTuneSteps) s->tune_state = 1;
@@ -374,7 +434,7 @@ int graph_for(FsSim *s, uint32_t steps, cudaGraphExec_t *out) {
   for (StepGraph &g : s->graphs) {
     if (g.exec && g.steps == steps && g.n_canon == s->hb.n_canon &&
         g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream &&
-        g.batched_loads == s->batched_loads) {
+        g.forms == s->forms.key()) {
       g.last_use = ++s->graph_clock;
       *out = g.exec;
       return FS_OK;
@@ -409,7 +469,7 @@ int graph_for(FsSim *s, uint32_t steps, cudaGraphExec_t *out) {
   slot->n_sorted = s->hb.n_sorted;
   slot->iters = s->iterations;
   slot->stream = s->stream;
-  slot->batched_loads = s->batched_loads;
+  slot->forms = s->forms.key();
   slot->last_use = ++s->graph_clock;
   *out = exec;
   return FS_OK;
@@ -516,8 +576,9 @@ int create_sim(const char *who, const SphParticle3D *particles, const uint32_t *
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     for (auto &e : s->ev)
       if (e) cudaEventDestroy(e);
-    for (auto &e : s->tune_ev)
-      if (e) cudaEventDestroy(e);
+    for (auto &row : s->tune_ev)
+      for (auto &e : row)
+        if (e) cudaEventDestroy(e);
     delete s;
     return code;
   };
@@ -530,10 +591,11 @@ int create_sim(const char *who, const SphParticle3D *particles, const uint32_t *
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return bail(cuda_fail(e, "create event"));
   }
-  for (auto &ev : s->tune_ev) {
-    e = cudaEventCreate(&ev);
-    if (e != cudaSuccess) return bail(cuda_fail(e, "create event"));
-  }
+  for (auto &row : s->tune_ev)
+    for (auto &ev : row) {
+      e = cudaEventCreate(&ev);
+      if (e != cudaSuccess) return bail(cuda_fail(e, "create event"));
+    }
   carve(s, nullptr, &s->arena_bytes);
   {
     int sms = 0;
@@ -673,8 +735,9 @@ int fs_destroy(FsSim *s) {
   if (s->frame_graph.exec) cudaGraphExecDestroy(s->frame_graph.exec);
   for (auto &e : s->ev)
     if (e) cudaEventDestroy(e);
-  for (auto &e : s->tune_ev)
-    if (e) cudaEventDestroy(e);
+  for (auto &row : s->tune_ev)
+    for (auto &e : row)
+      if (e) cudaEventDestroy(e);
   if (s->splat_buf) cudaFree(s->splat_buf);
   if (s->arena) cudaFree(s->arena);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -692,6 +755,7 @@ int fs_step(FsSim *s, uint32_t nsteps) {
   if ((rc = set_device(s))) return rc;
   if (nsteps == 0) return FS_OK;
   if (!capturing(s)) {
+    tune_lookup(s);
     if ((rc = tune_decide(s))) return rc;
     // stage-timed steps are never measurement steps
     if (!s->timing && s->tune_state == 0 && s->steps_done < kTuneAfterSteps &&
@@ -751,9 +815,85 @@ int fs_load_batching(FsSim *s, int *batched, int *decided) {
   CHECK_SIM(s);
   int rc;
   if ((rc = set_device(s))) return rc;
+  if (!capturing(s)) tune_lookup(s);
   if ((rc = tune_decide(s))) return rc;
-  if (batched) *batched = s->batched_loads ? 1 : 0;
+  if (batched) *batched = (s->forms.density > 0 || s->forms.solve > 0) ? 1 : 0;
   if (decided) *decided = s->tune_state == 2 ? 1 : 0;
+  return FS_OK;
+}
+
+int fs_kernel_forms(FsSim *s, FsKernelForms *out) {
+  CHECK_SIM(s);
+  if (!out) return fail(FS_E_INVALID_ARGUMENT, "fs_kernel_forms: null output");
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (!capturing(s)) tune_lookup(s);
+  if ((rc = tune_decide(s))) return rc;
+  std::memset(out, 0, sizeof(*out));
+  out->density_loads = kDensityDepths[s->forms.density];
+  out->solve_loads = kDensityDepths[s->forms.solve];
+  out->xsph_loads = kXsphDepthList[s->forms.xsph];
+  out->decided = s->tune_state == 2 ? uint32_t(s->tune_source) : 0u;
+  out->bucket = std::get<1>(tune_key(s));
+  for (int k = 0; k < 3; k++)
+    for (int c = 0; c < kNumLoadDepths; c++) out->ms[k][c] = s->tune_ms[k][c];
+  return FS_OK;
+}
+
+int fs_set_kernel_forms(FsSim *s, int density_loads, int solve_loads, int xsph_loads) {
+  CHECK_SIM(s);
+  if (density_loads < 0 && solve_loads < 0 && xsph_loads < 0) {
+    s->tune_state = 0;
+    s->tune_phase = 0;
+    s->tune_source = 0;
+    s->forms = KernelForms{};
+    return FS_OK;
+  }
+  auto index_of = [](const uint32_t *list, int v) {
+    for (int c = 0; c < kNumLoadDepths; c++)
+      if (int(list[c]) == v) return c;
+    return -1;
+  };
+  const int d = index_of(kDensityDepths, density_loads), so = index_of(kDensityDepths, solve_loads),
+            x = index_of(kXsphDepthList, xsph_loads);
+  if (d < 0 || so < 0 || x < 0)
+    return fail(FS_E_INVALID_ARGUMENT,
+                "fs_set_kernel_forms: depths must be in {0, 4, 8, 16} (density, solve) and "
+                "{1, 4, 8, 16} (xsph), or all -1");
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (s->tune_state == 1 && !capturing(s)) {
+    // measured steps in flight: let them finish before their events are reused
+    FS_CUDA(cudaEventSynchronize(s->tune_ev[kTuneSteps - 1][8]), "kernel-form measurement");
+  }
+  s->forms.density = uint8_t(d);
+  s->forms.solve = uint8_t(so);
+  s->forms.xsph = uint8_t(x);
+  s->tune_state = 2;
+  s->tune_source = 3;
+  return FS_OK;
+}
+
+int fs_kernel_forms_table(FsKernelFormsEntry *out, uint32_t capacity, uint32_t *count) {
+  if (!count) return fail(FS_E_INVALID_ARGUMENT, "fs_kernel_forms_table: null count");
+  std::lock_guard<std::mutex> lk(g_forms_mu);
+  *count = uint32_t(g_forms_table.size());
+  if (!out) return FS_OK;
+  uint32_t k = 0;
+  for (const auto &kv : g_forms_table) {
+    if (k >= capacity) break;
+    FsKernelFormsEntry &e = out[k++];
+    std::memset(&e, 0, sizeof(e));
+    e.device = uint32_t(std::get<0>(kv.first));
+    e.bucket = std::get<1>(kv.first);
+    e.many_scenes = std::get<2>(kv.first);
+    e.iterations = std::get<3>(kv.first);
+    e.density_loads = kDensityDepths[kv.second.forms.density];
+    e.solve_loads = kDensityDepths[kv.second.forms.solve];
+    e.xsph_loads = kXsphDepthList[kv.second.forms.xsph];
+    for (int p = 0; p < 3; p++)
+      for (int c = 0; c < kNumLoadDepths; c++) e.ms[p][c] = kv.second.ms[p][c];
+  }
   return FS_OK;
 }
 
@@ -761,6 +901,7 @@ int fs_prepare_steps(FsSim *s, uint32_t nsteps) {
   CHECK_SIM(s);
   int rc;
   if ((rc = set_device(s))) return rc;
+  if (!capturing(s)) tune_lookup(s);
   if ((rc = tune_decide(s))) return rc;  // capture with the final choice
   if (nsteps < 2 || s->timing) return FS_OK;
   const uint32_t chunks = (nsteps + kMaxGraphSteps - 1) / kMaxGraphSteps;
@@ -933,12 +1074,13 @@ int fs_frames(FsSim *s, uint32_t substeps, uint32_t frames) {
   int rc;
   if ((rc = set_device(s))) return rc;
   if (frames == 0) return FS_OK;
+  if (!capturing(s)) tune_lookup(s);
   if ((rc = tune_decide(s))) return rc;
   s->steps_done += uint64_t(substeps) * frames;
   StepGraph &g = s->frame_graph;
   if (!(g.exec && g.steps == substeps && g.n_canon == s->hb.n_canon &&
         g.n_sorted == s->hb.n_sorted && g.iters == s->iterations && g.stream == s->stream &&
-        g.batched_loads == s->batched_loads)) {
+        g.forms == s->forms.key())) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = StepGraph{};
     cudaGraph_t graph = nullptr;
@@ -968,7 +1110,7 @@ int fs_frames(FsSim *s, uint32_t substeps, uint32_t frames) {
     g.n_sorted = s->hb.n_sorted;
     g.iters = s->iterations;
     g.stream = s->stream;
-    g.batched_loads = s->batched_loads;
+    g.forms = s->forms.key();
   }
   for (uint32_t f = 0; f < frames; f++)
     FS_CUDA(cudaGraphLaunch(g.exec, s->stream), "launch frame graph");

@@ -29,24 +29,25 @@ namespace fs {
 namespace {
 
 // Candidate records loaded ahead per lane (batched_loop; <= 1: plain loop).
-// Density and solve have two instantiations: kBatchedLoads records in flight
-// per lane (105 registers), or the plain loop at the higher occupancy its
-// fewer registers allow. Which is faster depends on the workload: on the
-// 1M-particle dam break (clumps of ~10,000) B = 16 takes density 4.11 -> 3.22
-// ms and the four solve iterations 7.22 -> 4.92 ms, on the 256-scene ensemble
-// the plain loop is faster (step 29.3 ms against 33.5). The simulation picks
-// per workload by timing both (DevState::batched_loads, set by fs_step); the
-// results are the same bits either way. XSPH (two records per candidate)
-// uses B = 4.
-constexpr int kBatchedLoads = 16;
-constexpr int kPlainLoads = 0;
-constexpr int kXsphBatch = 4;
-// With batched loads, PCISPH iteration 0 runs on the pressure-carrying
+// Each neighbour pass has one instantiation per load depth in
+// kLoadDepths (density, solve) or kXsphDepths (XSPH, two records per
+// candidate): deeper batches hide more load latency per lane but take more
+// registers, so fewer warps fit an SM. Which depth is fastest depends on the
+// workload (on the 1M-particle dam break, clumps of ~10,000, density at 16
+// records takes 4.11 -> 3.22 ms and the four solve iterations 7.22 -> 4.92
+// ms against the plain loop; on the 256-scene ensemble the plain loop was
+// faster), so the simulation measures them (DevState::load_*, chosen per
+// particle-count bucket by fs_step's tuner). Every depth gives the same bits.
+// With a batched depth, PCISPH iteration 0 runs on the pressure-carrying
 // kernel with every pressure term 0 (written by the predict pass): its terms
 // add +-0 to +0, so the results are the same bits as skipping them, and that
 // kernel keeps its candidate loads batched where the short pressure-free one
 // does not (solve 5.30 -> 4.84 ms on the 1M-particle dam break). The plain
-// form keeps the pressure-free kernel for iteration 0.
+// loop keeps the pressure-free kernel for iteration 0.
+constexpr int kLoadDepths[kNumLoadDepths] = {0, 4, 8, 16};
+constexpr int kXsphDepths[kNumLoadDepths] = {1, 4, 8, 16};
+static_assert(kLoadDepths[3] == int(kDensityDepths[3]) && kXsphDepths[0] == int(kXsphDepthList[0]),
+              "depth lists agree");
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
@@ -238,6 +239,7 @@ __device__ __forceinline__ void density_one(
 // loop (the term is added where 1e-12 < r^2 < h^2, in the shader's order):
 // faster here than walking the hit mask, whose per-hit cost is the walk and
 // two dependent gathers.
+template <int B>
 __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
                                               const float4 *__restrict__ s_vel,
                                               const float4 *__restrict__ nb_pos,
@@ -265,7 +267,7 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
   };
   for (int r = 0; r < R.count; r++) {
     const uint32_t lo = R.lo[r];
-    batched_loop<kXsphBatch>(
+    batched_loop<B>(
         R.hi[r] - lo, [&](uint32_t k) { return PV{__ldg(nb_pos + lo + k), __ldg(nb_vel + lo + k)}; },
         [&](uint32_t, const PV &q) {
       const float4 pj = q.p;
@@ -917,11 +919,12 @@ __global__ void __launch_bounds__(128)
   });
 }
 
+template <int B>
 __global__ void __launch_bounds__(128)
     k_xsph(TaskQueue q, SceneView v, const float4 *__restrict__ s_vel,
            const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
            const uint32_t *__restrict__ begin, float4 *__restrict__ vel_x) {
-  for_warp_tasks(q, [&](uint32_t s) { xsph_one(s, v, s_vel, nb_pos, nb_vel, begin, vel_x); });
+  for_warp_tasks(q, [&](uint32_t s) { xsph_one<B>(s, v, s_vel, nb_pos, nb_vel, begin, vel_x); });
 }
 
 // Threads per block of the force pass: its registers fit 19 warps per SM,
@@ -1314,19 +1317,21 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   }
   if (e != cudaSuccess) return e;
   const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm, d.dens_hits};
-  if (d.batched_loads) {
-    static unsigned blocks = 0;
-    if (!blocks) blocks = persistent_blocks(k_density<kBatchedLoads>, d.sm_count);
-    k_density<kBatchedLoads><<<blocks, 128, 0, st>>>(
-        q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm, nb, d.stats,
-        d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc, d.mask_cap);
-  } else {
-    static unsigned blocks = 0;
-    if (!blocks) blocks = persistent_blocks(k_density<kPlainLoads>, d.sm_count);
-    k_density<kPlainLoads><<<blocks, 128, 0, st>>>(
-        q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm, nb, d.stats,
-        d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc, d.mask_cap);
+#define FS_DENSITY(I_)                                                                      \
+  do {                                                                                      \
+    static unsigned blocks = 0;                                                             \
+    if (!blocks) blocks = persistent_blocks(k_density<kLoadDepths[I_]>, d.sm_count);        \
+    k_density<kLoadDepths[I_]><<<blocks, 128, 0, st>>>(                                     \
+        q, d.view(), d.s_pos, d.s_vel, d.cell_begin, d.s_dens, d.s_nrm, nb, d.stats,        \
+        d.mask_words, d.mask_off, d.mask_hits, d.mask_alloc, d.mask_cap);                   \
+  } while (0)
+  switch (d.load_density) {
+    case 1: FS_DENSITY(1); break;
+    case 2: FS_DENSITY(2); break;
+    case 3: FS_DENSITY(3); break;
+    default: FS_DENSITY(0); break;
   }
+#undef FS_DENSITY
   if (dedupe)
     k_dedupe_copy<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.rep_of, d.s_vel, d.s_dens,
                                                       d.s_nrm, nb, d.mask_off, d.mask_hits,
@@ -1339,9 +1344,20 @@ cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
   TaskQueue q;
   cudaError_t e = prepare_queue(d, d.warp_order, false, n, 0, st, &q);
   if (e != cudaSuccess) return e;
-  static unsigned blocks = 0;
-  if (!blocks) blocks = persistent_blocks(k_xsph, d.sm_count);
-  k_xsph<<<blocks, 128, 0, st>>>(q, d.view(), d.s_vel, d.nb_pos, d.nb_vel, d.cell_begin, d.vel_x);
+#define FS_XSPH(I_)                                                                          \
+  do {                                                                                       \
+    static unsigned blocks = 0;                                                              \
+    if (!blocks) blocks = persistent_blocks(k_xsph<kXsphDepths[I_]>, d.sm_count);            \
+    k_xsph<kXsphDepths[I_]><<<blocks, 128, 0, st>>>(q, d.view(), d.s_vel, d.nb_pos, d.nb_vel, \
+                                                    d.cell_begin, d.vel_x);                  \
+  } while (0)
+  switch (d.load_xsph) {
+    case 0: FS_XSPH(0); break;
+    case 2: FS_XSPH(2); break;
+    case 3: FS_XSPH(3); break;
+    default: FS_XSPH(1); break;
+  }
+#undef FS_XSPH
   return cudaGetLastError();
 }
 
@@ -1383,23 +1399,41 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
                                                     rho_out, d.pterm[out], d.pred_v, d.stats, \
                                                     ap_out, d.mask_off, hit_out, hit_or);     \
   } while (0)
-#define FS_SOLVE(P_, L_, R_)                                 \
-  do {                                                       \
-    if (d.batched_loads) FS_SOLVE_B(P_, L_, R_, kBatchedLoads, q); \
-    else FS_SOLVE_B(P_, L_, R_, kPlainLoads, q);             \
+#define FS_SOLVE(P_, L_, R_)                                       \
+  do {                                                             \
+    switch (d.load_solve) {                                        \
+      case 1: FS_SOLVE_B(P_, L_, R_, kLoadDepths[1], q); break;    \
+      case 2: FS_SOLVE_B(P_, L_, R_, kLoadDepths[2], q); break;    \
+      case 3: FS_SOLVE_B(P_, L_, R_, kLoadDepths[3], q); break;    \
+      default: FS_SOLVE_B(P_, L_, R_, kLoadDepths[0], q); break;   \
+    }                                                              \
+  } while (0)
+  // the pressure-free iteration-0 kernel only with the plain loop (see
+  // kLoadDepths); a batched depth runs iteration 0 on the pressure kernel
+#define FS_SOLVE0(L_, R_)                                          \
+  do {                                                             \
+    FS_SOLVE_B(false, L_, R_, kLoadDepths[0], q);                  \
   } while (0)
 #define FS_SOLVE_R(P_, L_)            \
   do {                                \
     if (hit_out) FS_SOLVE(P_, L_, true); \
     else FS_SOLVE(P_, L_, false);     \
   } while (0)
-  if (iter == 0 && last && d.batched_loads) FS_SOLVE_R(true, true);
-  else if (iter == 0 && last) FS_SOLVE_R(false, true);
-  else if (iter == 0 && d.batched_loads) FS_SOLVE_R(true, false);
-  else if (iter == 0) FS_SOLVE_R(false, false);
+#define FS_SOLVE0_R(L_)                \
+  do {                                 \
+    if (hit_out) FS_SOLVE0(L_, true);  \
+    else FS_SOLVE0(L_, false);         \
+  } while (0)
+  const bool batched = kLoadDepths[d.load_solve & 3] > 1;
+  if (iter == 0 && last && batched) FS_SOLVE_R(true, true);
+  else if (iter == 0 && last) FS_SOLVE0_R(true);
+  else if (iter == 0 && batched) FS_SOLVE_R(true, false);
+  else if (iter == 0) FS_SOLVE0_R(false);
   else if (last) FS_SOLVE_R(true, true);
   else FS_SOLVE_R(true, false);
+#undef FS_SOLVE0_R
 #undef FS_SOLVE_R
+#undef FS_SOLVE0
 #undef FS_SOLVE
 #undef FS_SOLVE_B
   return cudaGetLastError();

@@ -90,6 +90,19 @@ class FsRigidBodyState(C.Structure):
                 ("wall_stiffness", C.c_float), ("_pad", C.c_uint32)]
 
 
+class FsKernelForms(C.Structure):
+    _fields_ = [("density_loads", C.c_uint32), ("solve_loads", C.c_uint32),
+                ("xsph_loads", C.c_uint32), ("decided", C.c_uint32), ("bucket", C.c_uint32),
+                ("ms", (C.c_float * 4) * 3)]
+
+
+class FsKernelFormsEntry(C.Structure):
+    _fields_ = [("device", C.c_uint32), ("bucket", C.c_uint32), ("many_scenes", C.c_uint32),
+                ("iterations", C.c_uint32), ("density_loads", C.c_uint32),
+                ("solve_loads", C.c_uint32), ("xsph_loads", C.c_uint32), ("_pad", C.c_uint32),
+                ("ms", (C.c_float * 4) * 3)]
+
+
 class GpuGridParams(C.Structure):
     _fields_ = [("grid_size_x", C.c_uint32), ("grid_size_y", C.c_uint32),
                 ("grid_size_z", C.c_uint32), ("total_cells", C.c_uint32),
@@ -141,7 +154,8 @@ class FsSceneInfo(C.Structure):
 STRUCT_SIZES = {
     GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
     GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48, FsSceneInfo: 80,
-    GpuMcGridParams: 48, FsRigidBodyState: 80, GpuSprayParams: 80,
+    GpuMcGridParams: 48, FsRigidBodyState: 80, GpuSprayParams: 80, FsKernelForms: 68,
+    FsKernelFormsEntry: 80,
 }
 for _t, _n in STRUCT_SIZES.items():
     assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))
@@ -204,6 +218,9 @@ SIGNATURES = {
     "fs_prefix_scan_noalloc": (C.c_int, [_vp, _vp, _u32, _vp, _vp]),
     "fs_export_particles_aos": (C.c_int, [_vp, _u32, C.c_int, _vp, _u32]),
     "fs_load_batching": (C.c_int, [_vp, _P(C.c_int), _P(C.c_int)]),
+    "fs_kernel_forms": (C.c_int, [_vp, _vp]),
+    "fs_set_kernel_forms": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    "fs_kernel_forms_table": (C.c_int, [_vp, _u32, _P(_u32)]),
     "fs_selftest_arithmetic": (C.c_int, [C.c_int, _P(C.c_ulonglong)]),
     "fs_selftest_scan_wait": (C.c_int, [_vp, C.c_int, _vp]),
     "fs_selftest_fp32_rate": (C.c_int, [C.c_int, _P(C.c_double)]),

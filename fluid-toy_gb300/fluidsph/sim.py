@@ -148,6 +148,22 @@ class SphSimulation3DGrid:
         check(self._lib.fs_load_batching(self._h, C.byref(b), C.byref(d)))
         return bool(b.value), bool(d.value)
 
+    def kernel_forms(self) -> dict:
+        """The neighbour passes' load depths and how they were chosen
+        (fs_kernel_forms; waits for a pending measurement)."""
+        f = abi.FsKernelForms()
+        check(self._lib.fs_kernel_forms(self._h, C.byref(f)))
+        return {"density_loads": f.density_loads, "solve_loads": f.solve_loads,
+                "xsph_loads": f.xsph_loads,
+                "decided": ("pending", "measured", "table", "set")[f.decided],
+                "bucket": f.bucket, "ms": [list(row) for row in f.ms]}
+
+    def set_kernel_forms(self, density_loads: int = -1, solve_loads: int = -1,
+                         xsph_loads: int = -1) -> None:
+        """Fix the load depths (no measurement, no host wait); all -1 to tune."""
+        check(self._lib.fs_set_kernel_forms(self._h, int(density_loads), int(solve_loads),
+                                            int(xsph_loads)))
+
     def export_particles_aos(self, device_ptr: int, count: int, sorted: bool = False,
                              scene: int = 0) -> None:
         """Write `count` 64-byte SphParticle3D records (canonical, or sorted
@@ -319,3 +335,18 @@ class SphBatch3DGrid(SphSimulation3DGrid):
     def upload_scene_particles(self, scene: int, particles: np.ndarray) -> None:
         p = abi.as_particles(particles)
         check(self._lib.fs_batch_upload_scene(self._h, int(scene), p.ctypes.data, len(p)))
+
+
+def kernel_forms_table() -> list[dict]:
+    """The process-wide per-bucket table of load depths (fs_kernel_forms_table)."""
+    lib = abi.load()
+    n = C.c_uint32()
+    check(lib.fs_kernel_forms_table(None, 0, C.byref(n)))
+    arr = (abi.FsKernelFormsEntry * max(n.value, 1))()
+    check(lib.fs_kernel_forms_table(arr, n.value, C.byref(n)))
+    return [{"bucket": e.bucket, "many_scenes": bool(e.many_scenes), "iterations": e.iterations,
+             "density_loads": e.density_loads, "solve_loads": e.solve_loads,
+             "xsph_loads": e.xsph_loads,
+             "ms": {"density": [round(x, 3) for x in e.ms[0]], "xsph": [round(x, 3) for x in e.ms[1]],
+                    "solve": [round(x, 3) for x in e.ms[2]]}}
+            for e in arr[:n.value]]

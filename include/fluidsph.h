@@ -327,14 +327,46 @@ int fs_step(FsSim *sim, uint32_t nsteps);
 /* No counterpart in the reference. Capture now the graphs a later
  * fs_step(sim, nsteps) uses, so that call only launches. */
 int fs_prepare_steps(FsSim *sim, uint32_t nsteps);
-/* Which form of the density and PCISPH-solve kernels the simulation runs:
- * batched candidate loads (16 records in flight per lane) or the plain loop
- * at higher occupancy. Both give the same bits; their speed depends on the
- * workload, so once the simulation has run 8 steps its next four steps run
- * both forms between events (whatever the fs_step call sizes), the next
- * fs_step / fs_prepare_steps / fs_frames call waits for them once and the
- * faster form is kept. decided = 0 until then (the plain form runs). */
+/* No counterpart in the reference. The neighbour passes (density, XSPH,
+ * PCISPH solve) each exist in four forms that differ only in how many
+ * candidate records a lane loads ahead (the load depth: 0 = the plain loop,
+ * 4, 8 or 16 for density and solve; 1, 4, 8 or 16 for XSPH). Every form gives
+ * the same bits; which is fastest depends on the workload (deeper batches hide
+ * more latency per lane but fit fewer warps on an SM), so a project-written
+ * autotuner chooses per particle-count bucket: the bucket is
+ * (floor(log2 hashed particles), one scene or many, PCISPH iterations). A
+ * simulation whose bucket is already in the process-wide table takes its
+ * depths at once; otherwise, once it has run 8 steps, its next 8 steps run
+ * each depth twice (0, 1, 2, 3, 3, 2, 1, 0) with events around the three
+ * passes, whatever the fs_step call sizes, and the next fs_step /
+ * fs_prepare_steps / fs_frames call BLOCKS THE HOST ONCE until those 8 steps
+ * have run on the GPU; each pass then keeps its fastest depth, which also
+ * enters the table. Callers that must never block call fs_set_kernel_forms
+ * first. fs_load_batching: batched = 1 when the density or solve pass runs
+ * with batched loads, decided = 1 once the depths are fixed. */
 int fs_load_batching(FsSim *sim, int *batched, int *decided);
+typedef struct FsKernelForms {
+    uint32_t density_loads, solve_loads, xsph_loads; /* load depths in use        */
+    uint32_t decided;  /* 0 pending, 1 measured by this simulation, 2 from the
+                          table (an earlier simulation of the bucket), 3 set by
+                          fs_set_kernel_forms                                   */
+    uint32_t bucket;   /* floor(log2 hashed particles)                          */
+    float ms[3][4];    /* measured ms (density, XSPH, solve) per depth index, 0
+                          unless measured by this simulation                    */
+} FsKernelForms;
+/* The simulation's forms (waits for a pending measurement, like fs_step). */
+int fs_kernel_forms(FsSim *sim, FsKernelForms *out);
+/* Fix the forms (no measurement, no host wait), or all -1 to tune again.
+ * Depths outside the lists above return FS_E_INVALID_ARGUMENT. */
+int fs_set_kernel_forms(FsSim *sim, int density_loads, int solve_loads, int xsph_loads);
+typedef struct FsKernelFormsEntry {
+    uint32_t device, bucket, many_scenes, iterations;
+    uint32_t density_loads, solve_loads, xsph_loads, _pad;
+    float ms[3][4];    /* the measured ms the depths were chosen by             */
+} FsKernelFormsEntry;
+/* The process-wide table: *count = entries; up to `capacity` copied to out
+ * (out may be NULL to query the count). */
+int fs_kernel_forms_table(FsKernelFormsEntry *out, uint32_t capacity, uint32_t *count);
 
 /* update_* uploads, sph_3d_grid.rs:1446-1473. Ordered before later steps. */
 int fs_update_sph_params(FsSim *sim, const GpuSphParams3D *params);
