@@ -73,10 +73,19 @@ struct FsAdj {
   // one segment of tape + reverse accumulators + cotangents
   void *work = nullptr;
   size_t work_bytes = 0;
-  uint32_t work_N = 0, work_G = 0, work_K = 0, work_every = 0, work_scenes = 0, work_segs = 0;
-  // tape buffers: segs segments of `every` recorded steps, slot b * every + t
+  uint32_t work_N = 0, work_G = 0, work_K = 0, work_every = 0, work_scenes = 0, work_segs = 0,
+           work_bufs = 0;
+  // tape buffers: bufs buffers of `every` recorded steps, slot b * every + t
   std::vector<TapeSlot> tape;
-  uint32_t segs = 1;             // segment buffers (the forward records the last segs segments)
+  uint32_t segs = 1;             // segments the forward records (the last segs)
+  // With strict checkpointing (segs == 1) and two or more segments, a second
+  // buffer lets the backward re-run segment s-1 on `side` while segment s is
+  // reversed on the simulation's stream (bufs = 2); else bufs = segs.
+  uint32_t bufs = 1;
+  bool pipe_wanted = false;      // the next workspace should hold the second buffer
+  bool pipe_failed = false;      // it did not fit once: no second buffer
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_rec[2] = {}, ev_free[2] = {};
   uint64_t tape_budget = 0;      // bytes the caller allows for tape buffers (0: one segment)
   uint32_t seg_limit = ~0u;      // 1 after the budget's buffers failed to allocate
   std::vector<int64_t> buf_seg;  // checkpoint segment each buffer holds (-1: none)
@@ -144,7 +153,7 @@ uint64_t segment_bytes(const FsAdj *a) {
 void carve_work(FsAdj *a, char *base, size_t *bytes) {
   Carve c{base};
   const size_t N = a->N, G = a->G;
-  a->tape.assign(size_t(a->segs) * a->every, TapeSlot{});
+  a->tape.assign(size_t(a->bufs) * a->every, TapeSlot{});
   for (TapeSlot &t : a->tape) carve_slot(c, t, N, G, a->K);
   AdjView &v = a->av;
   v.gx = c.take<float4>(N);
@@ -169,8 +178,11 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
 }
 
 int ensure_work(FsAdj *a) {
+  const uint32_t want_bufs =
+      a->segs + ((a->segs == 1 && a->pipe_wanted && !a->pipe_failed) ? 1u : 0u);
   if (a->work && a->work_N == a->N && a->work_G == a->G && a->work_K == a->K &&
-      a->work_every == a->every && a->work_scenes == a->scenes && a->work_segs == a->segs)
+      a->work_every == a->every && a->work_scenes == a->scenes && a->work_segs == a->segs &&
+      a->work_bufs == want_bufs)
     return FS_OK;
   FsSim *s = a->sim;
   if (a->work) {
@@ -178,14 +190,17 @@ int ensure_work(FsAdj *a) {
     cudaFree(a->work);
     a->work = nullptr;
   }
+  a->bufs = want_bufs;
   carve_work(a, nullptr, &a->work_bytes);
-  if (cudaMalloc(&a->work, a->work_bytes) != cudaSuccess && a->segs > 1) {
-    // the budget's extra tape segments do not fit: fall back to one (until
-    // the budget changes)
+  if (cudaMalloc(&a->work, a->work_bytes) != cudaSuccess && a->bufs > 1) {
+    // the budget's extra tape segments, or the pipelining buffer, do not
+    // fit: fall back to one (until the budget changes)
     cudaGetLastError();
     a->work = nullptr;
+    if (a->segs > 1) a->seg_limit = 1;
+    else a->pipe_failed = true;
     a->segs = 1;
-    a->seg_limit = 1;
+    a->bufs = 1;
     carve_work(a, nullptr, &a->work_bytes);
   }
   if (!a->work) FS_CUDA(cudaMalloc(&a->work, a->work_bytes), "allocate adjoint workspace");
@@ -198,7 +213,8 @@ int ensure_work(FsAdj *a) {
   a->work_K = a->K;
   a->work_every = a->every;
   a->work_segs = a->segs;
-  a->buf_seg.assign(a->segs, -1);
+  a->work_bufs = a->bufs;
+  a->buf_seg.assign(a->bufs, -1);
   a->work_scenes = a->scenes;
   return FS_OK;
 }
@@ -355,6 +371,17 @@ int fs_adj_create(FsSim *sim, uint32_t checkpoint_every, FsAdj **out) {
   if (!a) return fail(FS_E_CAPACITY, "fs_adj_create: out of host memory");
   a->sim = sim;
   a->every = checkpoint_every;
+  if (cudaSetDevice(sim->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&a->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_rec[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_rec[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_free[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->ev_free[1], cudaEventDisableTiming) != cudaSuccess) {
+    const cudaError_t e = cudaGetLastError();
+    fs_adj_destroy(a);
+    return cuda_fail(e, "fs_adj_create: side stream and events");
+  }
   *out = a;
   return FS_OK;
 }
@@ -379,6 +406,12 @@ int fs_adj_destroy(FsAdj *a) {
     cudaSetDevice(a->sim->device);
     cudaStreamSynchronize(a->sim->stream);
   }
+  if (a->side) {
+    cudaStreamSynchronize(a->side);
+    cudaStreamDestroy(a->side);
+  }
+  for (cudaEvent_t e : {a->ev_start, a->ev_rec[0], a->ev_rec[1], a->ev_free[0], a->ev_free[1]})
+    if (e) cudaEventDestroy(e);
   free_adj(a);
   delete a;
   return FS_OK;
@@ -423,8 +456,9 @@ int fs_adj_forward(FsAdj *a, uint32_t nsteps) {
                                                       uint64_t(a->seg_limit)}));
     a->segs = uint32_t(want);
   }
+  a->pipe_wanted = a->segs == 1 && nck >= 2;
   if ((rc = ensure_work(a))) return rc;
-  a->buf_seg.assign(a->segs, -1);
+  a->buf_seg.assign(a->bufs, -1);
   // the reverse pass starts with the last segments: the last `segs` record
   // their tapes on the way instead of being re-run there
   const uint32_t first_rec = nck > a->segs ? nck - a->segs : 0u;
@@ -619,33 +653,90 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
   }
   const uint32_t nck = (a->steps + a->every - 1) / a->every;
   const SceneView base = s->d.view();
+  // restore segment seg's checkpoint and re-run it, recording into buffer b
+  auto rerun = [&](uint32_t seg, uint32_t b) -> int {
+    const uint32_t len = std::min(a->every, a->steps - seg * a->every);
+    a->buf_seg[b] = -1;
+    const float4 *ck = a->ck + size_t(seg) * 2 * N;
+    int r;
+    if ((r = copy_state(s, s->d.p_pos, s->d.p_vel, ck, ck + N, N))) return r;
+    for (uint32_t t = 0; t < len; t++) {
+      const DevState dv = recording_state(a, a->tape[size_t(b) * a->every + t]);
+      if ((r = enqueue_step(s, false, &dv))) return r;
+    }
+    a->buf_seg[b] = int64_t(seg);
+    return FS_OK;
+  };
+  // Pipelined (strict checkpointing with the second buffer): segment seg-1 is
+  // re-run on the side stream into the other buffer while seg is reversed on
+  // the simulation's stream. The re-run touches only the simulation's state
+  // and step buffers and its own tape buffer; the reversal reads only its tape
+  // buffer, the cotangents and the accumulators, so the two are independent
+  // apart from the buffer hand-over, which events order: the reversal of a
+  // buffer waits for its re-run (ev_rec), and a re-run into a buffer waits for
+  // the reversal that last read it (ev_free).
+  const bool pipe = a->bufs == 2 && a->segs == 1 && nck >= 2;
+  cudaStream_t main_stream = s->stream;
+  auto rerun_side = [&](uint32_t seg, uint32_t b) -> int {
+    FS_CUDA(cudaStreamWaitEvent(a->side, a->ev_free[b], 0), "order the re-run");
+    s->stream = a->side;
+    const int r = rerun(seg, b);
+    s->stream = main_stream;
+    if (r) return r;
+    FS_CUDA(cudaEventRecord(a->ev_rec[b], a->side), "order the re-run");
+    return FS_OK;
+  };
+  bool on_side[2] = {false, false};
+  if (pipe) {
+    // the side stream starts after everything queued before the backward
+    // (the loss reads the final state the first re-run overwrites)
+    FS_CUDA(cudaEventRecord(a->ev_start, main_stream), "order the re-run");
+    FS_CUDA(cudaStreamWaitEvent(a->side, a->ev_start, 0), "order the re-run");
+    // buffers carry no pending reversal yet
+    FS_CUDA(cudaEventRecord(a->ev_free[0], main_stream), "order the re-run");
+    FS_CUDA(cudaEventRecord(a->ev_free[1], main_stream), "order the re-run");
+  }
   for (uint32_t seg = nck; seg-- > 0;) {
     const uint32_t len = std::min(a->every, a->steps - seg * a->every);
     uint32_t b = 0;
-    while (b < a->segs && a->buf_seg[b] != int64_t(seg)) b++;
-    if (b == a->segs) {
-      // restore the segment's checkpoint and re-run it, recording into
-      // buffer 0 (whose segment, if any, has been reversed already)
-      b = 0;
-      a->buf_seg[0] = -1;
-      const float4 *ck = a->ck + size_t(seg) * 2 * N;
-      if ((rc = copy_state(s, s->d.p_pos, s->d.p_vel, ck, ck + N, N))) return rc;
-      for (uint32_t t = 0; t < len; t++) {
-        const DevState dv = recording_state(a, a->tape[t]);
-        if ((rc = enqueue_step(s, false, &dv))) return rc;
+    while (b < a->bufs && a->buf_seg[b] != int64_t(seg)) b++;
+    if (b == a->bufs) {
+      if (pipe) {
+        // only the last segment can be missing here (the forward did not
+        // record it); the others were started on the side stream below
+        b = 0;
+        if ((rc = rerun_side(seg, b))) return rc;
+        on_side[b] = true;
+      } else {
+        // buffer 0's segment, if any, has been reversed already
+        b = 0;
+        if ((rc = rerun(seg, b))) return rc;
       }
-      a->buf_seg[0] = int64_t(seg);
+    }
+    if (pipe && on_side[b]) {
+      FS_CUDA(cudaStreamWaitEvent(main_stream, a->ev_rec[b], 0), "order the reversal");
+      on_side[b] = false;
     }
     const TapeSlot *seg_tape = a->tape.data() + size_t(b) * a->every;
+    if (a->lanes == 0) {
+      // tuned on the segment's last step before the next re-run is queued,
+      // so that nothing else runs while the candidates are timed
+      SceneView v = base;
+      v.scene_of_slot = seg_tape[len - 1].sos;
+      const int L = tune_lanes(a, v, tape_view(seg_tape[len - 1], K));
+      if (L < 0) return L;
+      a->lanes = L;
+    }
+    if (pipe && seg >= 1) {
+      // start the next segment's re-run into the other buffer
+      const uint32_t o = b ^ 1u;
+      if ((rc = rerun_side(seg - 1, o))) return rc;
+      on_side[o] = true;
+    }
     for (uint32_t t = len; t-- > 0;) {
       const TapeSlot &slot = seg_tape[t];
       SceneView v = base;
       v.scene_of_slot = slot.sos;
-      if (a->lanes == 0) {
-        const int L = tune_lanes(a, v, tape_view(slot, K));
-        if (L < 0) return L;
-        a->lanes = L;
-      }
       const int nxt = a->cur ^ 1;
       FS_CUDA(launch_adj_step(v, tape_view(slot, K), a->av, a->cot[a->cur][0], a->cot[a->cur][1],
                               a->cot[nxt][0], a->cot[nxt][1], s->d.dir_tab, s->d.dir_half, N,
@@ -653,6 +744,7 @@ int fs_adj_backward(FsAdj *a, float *dl_dpos0, float *dl_dvel0, int on_device,
               "reverse step");
       a->cur = nxt;
     }
+    if (pipe) FS_CUDA(cudaEventRecord(a->ev_free[b], main_stream), "order the re-run");
   }
   // outputs
   const float4 *g[2] = {a->cot[a->cur][0], a->cot[a->cur][1]};
