@@ -10,10 +10,13 @@
 namespace fs {
 
 // Load depths (candidate records in flight per lane) each neighbour pass is
-// instantiated for; see kLoadDepths / kXsphDepths in sph_kernels.cu.
-constexpr int kNumLoadDepths = 4;
-constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16};
-constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16};
+// instantiated for; see kLoadDepths / kXsphDepths in sph_kernels.cu. 32 is the
+// staged form (a warp's chunk of 32 records in shared memory); the density
+// pass has no staged form and is tuned over the first four only.
+constexpr int kNumLoadDepths = 5;
+constexpr int kDensityCandidates = 4;
+constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
+constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16, 32};
 
 // The neighbour passes' load-depth choice of a simulation (indices into the
 // lists above).

@@ -397,7 +397,7 @@ int tune_decide(FsSim *s) {
   }
   uint8_t best[3] = {0, 0, 0};
   for (int k = 0; k < 3; k++)
-    for (int c = 1; c < kNumLoadDepths; c++)
+    for (int c = 1; c < (k == 0 ? kDensityCandidates : kNumLoadDepths); c++)
       if (ms[k][c] < ms[k][best[k]]) best[k] = uint8_t(c);
   s->forms.density = best[0];
   s->forms.xsph = best[1];
@@ -858,14 +858,16 @@ int fs_set_kernel_forms(FsSim *s, int density_loads, int solve_loads, int xsph_l
             x = index_of(kXsphDepthList, xsph_loads);
   if (d < 0 || so < 0 || x < 0)
     return fail(FS_E_INVALID_ARGUMENT,
-                "fs_set_kernel_forms: depths must be in {0, 4, 8, 16} (density, solve) and "
-                "{1, 4, 8, 16} (xsph), or all -1");
+                "fs_set_kernel_forms: depths must be in {0, 4, 8, 16} (density), "
+                "{0, 4, 8, 16, 32} (solve) and {1, 4, 8, 16, 32} (xsph), or all -1");
   int rc;
   if ((rc = set_device(s))) return rc;
   if (s->tune_state == 1 && !capturing(s)) {
     // measured steps in flight: let them finish before their events are reused
     FS_CUDA(cudaEventSynchronize(s->tune_ev[kTuneSteps - 1][8]), "kernel-form measurement");
   }
+  if (d == kDensityCandidates)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_set_kernel_forms: the density pass has no staged form");
   s->forms.density = uint8_t(d);
   s->forms.solve = uint8_t(so);
   s->forms.xsph = uint8_t(x);

@@ -44,10 +44,69 @@ namespace {
 // kernel keeps its candidate loads batched where the short pressure-free one
 // does not (solve 5.30 -> 4.84 ms on the 1M-particle dam break). The plain
 // loop keeps the pressure-free kernel for iteration 0.
-constexpr int kLoadDepths[kNumLoadDepths] = {0, 4, 8, 16};
-constexpr int kXsphDepths[kNumLoadDepths] = {1, 4, 8, 16};
+constexpr int kLoadDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
+constexpr int kXsphDepths[kNumLoadDepths] = {1, 4, 8, 16, 32};
 static_assert(kLoadDepths[3] == int(kDensityDepths[3]) && kXsphDepths[0] == int(kXsphDepthList[0]),
               "depth lists agree");
+// The staged form (load depth kStagedLoads; XSPH and the PCISPH solve): in a
+// warp whose 32 lanes are all in one cell (the same neighbour runs: the dense
+// clumps, where the time goes), candidate records go through shared memory in
+// chunks of 32, each lane loading one record of the next chunk while the warp
+// works on the current one: the latency hiding of 32 records in flight per
+// lane at the registers of one. Every lane still visits its candidates in the
+// shaders' order, so the bits are those of the other forms; other warps run
+// the plain loop. (Streaming the union of the runs of lanes in x-adjacent
+// cells, each lane taking only its own candidates, was measured slower: the
+// lanes idle over the union's extra cell.)
+constexpr int kStagedLoads = 32;
+
+// Whether every lane of the warp is active with the same runs (one cell).
+__device__ __forceinline__ bool warp_same_runs(bool active, const Runs &R) {
+  if (!__all_sync(0xffffffffu, active)) return false;
+  const int c0 = __shfl_sync(0xffffffffu, R.count, 0);
+  const uint32_t rows0 = __shfl_sync(0xffffffffu, R.rows, 0);
+  if (!__all_sync(0xffffffffu, R.count == c0 && R.rows == rows0)) return false;
+  bool same = true;
+  for (int r = 0; r < 9; r++) {
+    if (r >= c0) break;
+    same = same && R.lo[r] == __shfl_sync(0xffffffffu, R.lo[r], 0) &&
+           R.hi[r] == __shfl_sync(0xffffffffu, R.hi[r], 0);
+  }
+  return __all_sync(0xffffffffu, same);
+}
+
+// Position in the chunk sequence of a set of runs: for each run in order,
+// chunks of up to 32 consecutive candidates from its start.
+struct StagedChunks {
+  int r;
+  uint32_t base, cnt;
+  bool valid;
+  __device__ __forceinline__ explicit StagedChunks(const Runs &U) : r(0), base(0), cnt(0) {
+    valid = false;
+    for (; r < U.count; r++)
+      if (U.hi[r] > U.lo[r]) {
+        base = U.lo[r];
+        cnt = min(32u, U.hi[r] - base);
+        valid = true;
+        break;
+      }
+  }
+  __device__ __forceinline__ void advance(const Runs &U) {
+    if (base + 32u < U.hi[r]) {
+      base += 32u;
+      cnt = min(32u, U.hi[r] - base);
+      return;
+    }
+    valid = false;
+    for (r++; r < U.count; r++)
+      if (U.hi[r] > U.lo[r]) {
+        base = U.lo[r];
+        cnt = min(32u, U.hi[r] - base);
+        valid = true;
+        return;
+      }
+  }
+};
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
 #pragma unroll
@@ -246,6 +305,67 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
                                               const float4 *__restrict__ nb_vel,
                                               const uint32_t *__restrict__ begin,
                                               float4 *__restrict__ vel_x) {
+  // the pair term, shared by the forms (xsph.wgsl:106-135)
+  auto term = [](float3 pos_i, float3 vel_i, float h2, float scale_d, float3 &corr, float4 pj,
+                 float4 vj) {
+    const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
+    const float r_sq = rx * rx + ry * ry + rz * rz;
+    const bool hit = r_sq < h2 && r_sq > 1e-12f;
+    const float diff = h2 - r_sq;
+    const float w = scale_d * diff * diff * diff;
+    const float3 c = corr + vj.w * (xyz(vj) - vel_i) * w;
+    corr = hit ? c : corr;
+  };
+  if constexpr (B == kStagedLoads) {
+    // staged (see kStagedLoads): warps whose lanes share one cell
+    __shared__ float4 st_p[4][32], st_v[4][32];
+    const bool act = s < v.b->n_sorted;
+    const DevUniforms *U = v.u + (act ? v.scene_of_slot[s] : 0u);
+    const GpuSphParams3D &P = U->sph;
+    const bool work = act && P.xsph_epsilon > 0.0f;
+    Runs R;
+    R.count = 0;
+    R.total = 0;
+    R.words = 0;
+    float3 pos_i = f3(0.f, 0.f, 0.f);
+    if (work) {
+      pos_i = xyz(nb_pos[s]);
+      neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
+    }
+    if (warp_same_runs(work, R)) {
+      const float4 vi4 = s_vel[s];
+      const float3 vel_i = xyz(vi4);
+      const float h2 = P.kernel_radius_sq;
+      const float scale_d = 315.0f / (64.0f * PI_F * P.kernel_radius_pow9);
+      const unsigned lane = threadIdx.x & 31u;
+      float4 *sp = st_p[threadIdx.x >> 5], *sv = st_v[threadIdx.x >> 5];
+      float3 corr = f3(0.f, 0.f, 0.f);
+      StagedChunks ch(R);
+      float4 pf_p = make_float4(0.f, 0.f, 0.f, 0.f), pf_v = pf_p;
+      if (ch.valid && lane < ch.cnt) {
+        pf_p = __ldg(nb_pos + ch.base + lane);
+        pf_v = __ldg(nb_vel + ch.base + lane);
+      }
+      while (ch.valid) {
+        const uint32_t cnt = ch.cnt;
+        const float4 cur_p = pf_p, cur_v = pf_v;
+        ch.advance(R);
+        if (ch.valid && lane < ch.cnt) {
+          pf_p = __ldg(nb_pos + ch.base + lane);
+          pf_v = __ldg(nb_vel + ch.base + lane);
+        }
+        __syncwarp();  // the previous chunk's readers are done
+        sp[lane] = cur_p;
+        sv[lane] = cur_v;
+        __syncwarp();
+#pragma unroll 4
+        for (uint32_t k = 0; k < cnt; k++) term(pos_i, vel_i, h2, scale_d, corr, sp[k], sv[k]);
+      }
+      const float3 vn = vel_i + P.xsph_epsilon * corr;
+      vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
+      return;
+    }
+  }
   if (s >= v.b->n_sorted) return;
   const DevUniforms *U = v.u + v.scene_of_slot[s];
   const GpuSphParams3D &P = U->sph;
@@ -267,19 +387,9 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
   };
   for (int r = 0; r < R.count; r++) {
     const uint32_t lo = R.lo[r];
-    batched_loop<B>(
+    batched_loop<(B == kStagedLoads ? 1 : B)>(
         R.hi[r] - lo, [&](uint32_t k) { return PV{__ldg(nb_pos + lo + k), __ldg(nb_vel + lo + k)}; },
-        [&](uint32_t, const PV &q) {
-      const float4 pj = q.p;
-      const float4 vj = q.v;
-      const float rx = pos_i.x - pj.x, ry = pos_i.y - pj.y, rz = pos_i.z - pj.z;
-      const float r_sq = rx * rx + ry * ry + rz * rz;
-      const bool hit = r_sq < h2 && r_sq > 1e-12f;
-      const float diff = h2 - r_sq;
-      const float w = scale_d * diff * diff * diff;
-      const float3 c = corr + vj.w * (xyz(vj) - vel_i) * w;
-      corr = hit ? c : corr;
-    });
+        [&](uint32_t, const PV &q) { term(pos_i, vel_i, h2, scale_d, corr, q.p, q.v); });
   }
   const float3 vn = vel_i + eps * corr;
   vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
@@ -515,19 +625,26 @@ __device__ __forceinline__ void solve_one(
   R.count = 0;
   R.total = 0;
   R.words = 0;
+  // staged form: per warp, one chunk of 32 candidate records (block of 128)
+  __shared__ float4 st_xp[B == kStagedLoads ? 4 : 1][32];
+  __shared__ float st_pt[B == kStagedLoads ? 4 : 1][32];
+  float3 pos_i = f3(0.f, 0.f, 0.f);
+  if (active) {
+    pos_i = xyz(s_pos[s]);  // current position decides the cells
+    neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
+  }
+  bool uniform = false;
+  if constexpr (B == kStagedLoads) uniform = warp_same_runs(active, R);
   if (active) {
     const float4 self_xp = xp_in[s];
     const float3 pred_pos = xyz(self_xp);
     const float old_p = self_xp.w;
-    const float3 pos_i = xyz(s_pos[s]);  // current position decides the cells
-    neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
     float pred_density = 0.0f;
     float3 a_p = f3(0.f, 0.f, 0.f);
     // old_p / (sd * sd) with sd = max(rho_in[s], 1), written by the previous
     // iteration (read only when there is pressure)
     const float self_term = HAS_PRESSURE ? pterm_in[s] : 0.0f;
-    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
-      const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
+    auto pressure_term = [&](float3 r_vec, float r_sq, float pt) {  // pt = np / (nd * nd)
       const float3 nr = -r_vec;
       // correctly rounded fast square root, reciprocal and quotients, one
       // range check for the pair (IEEE operations outside it)
@@ -544,20 +661,80 @@ __device__ __forceinline__ void solve_one(
       const float grad = scale_g * dg * dg;
       a_p = a_p + (-mass * (self_term + pt) * grad) * dir;
     };
+    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
+      pressure_term(r_vec, r_sq, __ldg(pterm_in + j));
+    };
     uint32_t *hit_words = nullptr;
     if (RECORD) {
       const uint32_t off = mask_off[s];
       hit_words = off == MASK_NONE ? nullptr : hit_out + off;
     }
     uint32_t widx = 0u;
+    if constexpr (B == kStagedLoads) {
+      if (uniform) {
+        // staged: every lane of the warp has these runs; chunks of 32
+        // records go through shared memory, lane l loading record l of the
+        // next chunk while the warp works on the current one
+        StagedChunks ch(R);
+        float4 pf_xp = make_float4(0.f, 0.f, 0.f, 0.f);
+        float pf_pt = 0.0f;
+        const unsigned lane = threadIdx.x & 31u;
+        if (ch.valid && lane < ch.cnt) {
+          pf_xp = __ldg(xp_in + ch.base + lane);
+          if (HAS_PRESSURE) pf_pt = __ldg(pterm_in + ch.base + lane);
+        }
+        float4 *sx = st_xp[threadIdx.x >> 5];
+        float *sp = st_pt[threadIdx.x >> 5];
+        while (ch.valid) {
+          const uint32_t cnt = ch.cnt;
+          const float4 cur_xp = pf_xp;
+          const float cur_pt = pf_pt;
+          ch.advance(R);
+          if (ch.valid && lane < ch.cnt) {
+            pf_xp = __ldg(xp_in + ch.base + lane);
+            if (HAS_PRESSURE) pf_pt = __ldg(pterm_in + ch.base + lane);
+          }
+          __syncwarp();  // the previous chunk's readers are done
+          sx[lane] = cur_xp;
+          if (HAS_PRESSURE) sp[lane] = cur_pt;
+          __syncwarp();
+          uint32_t chunk = 0u, hitw = 0u;
+#pragma unroll 4
+          for (uint32_t k = 0; k < cnt; k++) {
+            const float4 nb = sx[k];
+            const float3 r_vec = pred_pos - xyz(nb);
+            const float r_sq = dot3(r_vec, r_vec);
+            if (r_sq < h2) {
+              hits++;
+              const float diff = h2 - r_sq;
+              pred_density += mass * (scale_d * diff * diff * diff);
+              if (HAS_PRESSURE && r_sq > 1e-12f) chunk |= 1u << k;
+              if (RECORD) hitw |= 1u << k;
+            }
+          }
+          if (RECORD) {
+            if (hit_words) hit_words[widx] = hit_or ? (hit_words[widx] | hitw) : hitw;
+            widx++;
+          }
+          if (HAS_PRESSURE) {
+            while (chunk) {
+              const uint32_t k = uint32_t(__ffs(chunk) - 1);
+              chunk &= chunk - 1u;
+              const float3 r_vec = pred_pos - xyz(sx[k]);
+              pressure_term(r_vec, dot3(r_vec, r_vec), sp[k]);
+            }
+          }
+        }
+      }
+    }
     // candidates in chunks of up to 32: the predicted density is summed while
     // testing; the pressure hits of the chunk go to a per-lane bitmask that
     // each lane then walks (its own hits only, ascending)
-    for (int r = 0; r < R.count; r++) {
+    for (int r = 0; r < ((B == kStagedLoads && uniform) ? 0 : R.count); r++) {
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
         uint32_t chunk = 0u, hitw = 0u;
-        batched_loop<B>(
+        batched_loop<(B == kStagedLoads ? 0 : B)>(
             cnt, [&](uint32_t k) { return __ldg(xp_in + base + k); },
             [&](uint32_t k, const float4 nb) {
               const float3 r_vec = pred_pos - xyz(nb);
@@ -1328,7 +1505,8 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
   switch (d.load_density) {
     case 1: FS_DENSITY(1); break;
     case 2: FS_DENSITY(2); break;
-    case 3: FS_DENSITY(3); break;
+    case 3:
+    case 4: FS_DENSITY(3); break;  // no staged density form
     default: FS_DENSITY(0); break;
   }
 #undef FS_DENSITY
@@ -1355,6 +1533,7 @@ cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
     case 0: FS_XSPH(0); break;
     case 2: FS_XSPH(2); break;
     case 3: FS_XSPH(3); break;
+    case 4: FS_XSPH(4); break;
     default: FS_XSPH(1); break;
   }
 #undef FS_XSPH
@@ -1405,6 +1584,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
       case 1: FS_SOLVE_B(P_, L_, R_, kLoadDepths[1], q); break;    \
       case 2: FS_SOLVE_B(P_, L_, R_, kLoadDepths[2], q); break;    \
       case 3: FS_SOLVE_B(P_, L_, R_, kLoadDepths[3], q); break;    \
+      case 4: FS_SOLVE_B(P_, L_, R_, kLoadDepths[4], q); break;    \
       default: FS_SOLVE_B(P_, L_, R_, kLoadDepths[0], q); break;   \
     }                                                              \
   } while (0)
@@ -1424,7 +1604,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     if (hit_out) FS_SOLVE0(L_, true);  \
     else FS_SOLVE0(L_, false);         \
   } while (0)
-  const bool batched = kLoadDepths[d.load_solve & 3] > 1;
+  const bool batched = kLoadDepths[d.load_solve < kNumLoadDepths ? d.load_solve : 0] > 1;
   if (iter == 0 && last && batched) FS_SOLVE_R(true, true);
   else if (iter == 0 && last) FS_SOLVE0_R(true);
   else if (iter == 0 && batched) FS_SOLVE_R(true, false);

@@ -15,7 +15,7 @@ import numpy as np
 
 from .build import LIB_PATH
 
-FS_ABI_VERSION = 0x00010054
+FS_ABI_VERSION = 0x00010055
 FS_OK = 0
 FS_STAGE_COUNT = 10
 FS_STAT_COUNT = 5
@@ -93,14 +93,14 @@ class FsRigidBodyState(C.Structure):
 class FsKernelForms(C.Structure):
     _fields_ = [("density_loads", C.c_uint32), ("solve_loads", C.c_uint32),
                 ("xsph_loads", C.c_uint32), ("decided", C.c_uint32), ("bucket", C.c_uint32),
-                ("ms", (C.c_float * 4) * 3)]
+                ("ms", (C.c_float * 5) * 3)]
 
 
 class FsKernelFormsEntry(C.Structure):
     _fields_ = [("device", C.c_uint32), ("bucket", C.c_uint32), ("many_scenes", C.c_uint32),
                 ("iterations", C.c_uint32), ("density_loads", C.c_uint32),
                 ("solve_loads", C.c_uint32), ("xsph_loads", C.c_uint32), ("_pad", C.c_uint32),
-                ("ms", (C.c_float * 4) * 3)]
+                ("ms", (C.c_float * 5) * 3)]
 
 
 class GpuGridParams(C.Structure):
@@ -154,8 +154,8 @@ class FsSceneInfo(C.Structure):
 STRUCT_SIZES = {
     GpuSphParams3D: 64, GpuContainerGeometry: 128, GpuGravity: 16, GpuMouseForce: 48,
     GpuRigidBody: 96, GpuRigidBodyAccum: 32, GpuGridParams: 48, FsSceneInfo: 80,
-    GpuMcGridParams: 48, FsRigidBodyState: 80, GpuSprayParams: 80, FsKernelForms: 68,
-    FsKernelFormsEntry: 80,
+    GpuMcGridParams: 48, FsRigidBodyState: 80, GpuSprayParams: 80, FsKernelForms: 80,
+    FsKernelFormsEntry: 92,
 }
 for _t, _n in STRUCT_SIZES.items():
     assert C.sizeof(_t) == _n, (_t.__name__, C.sizeof(_t))

@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010054u
+#define FS_ABI_VERSION 0x00010055u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -328,18 +328,21 @@ int fs_step(FsSim *sim, uint32_t nsteps);
  * fs_step(sim, nsteps) uses, so that call only launches. */
 int fs_prepare_steps(FsSim *sim, uint32_t nsteps);
 /* No counterpart in the reference. The neighbour passes (density, XSPH,
- * PCISPH solve) each exist in four forms that differ only in how many
+ * PCISPH solve) each exist in several forms that differ only in how many
  * candidate records a lane loads ahead (the load depth: 0 = the plain loop,
- * 4, 8 or 16 for density and solve; 1, 4, 8 or 16 for XSPH). Every form gives
+ * 4, 8 or 16 for density and solve; 1, 4, 8 or 16 for XSPH; 32 = the staged
+ * form of XSPH and solve, in which a warp whose lanes share one cell moves
+ * chunks of 32 records through shared memory, each lane loading one record
+ * of the next chunk). Every form gives
  * the same bits; which is fastest depends on the workload (deeper batches hide
  * more latency per lane but fit fewer warps on an SM), so a project-written
  * autotuner chooses per particle-count bucket: the bucket is
  * (floor(log2 hashed particles), one scene or many, PCISPH iterations). A
  * simulation whose bucket is already in the process-wide table takes its
- * depths at once; otherwise, once it has run 8 steps, its next 8 steps run
- * each depth twice (0, 1, 2, 3, 3, 2, 1, 0) with events around the three
+ * depths at once; otherwise, once it has run 8 steps, its next 10 steps run
+ * each depth twice (0, 1, 2, 3, 4, 4, 3, 2, 1, 0) with events around the three
  * passes, whatever the fs_step call sizes, and the next fs_step /
- * fs_prepare_steps / fs_frames call BLOCKS THE HOST ONCE until those 8 steps
+ * fs_prepare_steps / fs_frames call BLOCKS THE HOST ONCE until those 10 steps
  * have run on the GPU; each pass then keeps its fastest depth, which also
  * enters the table. Callers that must never block call fs_set_kernel_forms
  * first. fs_load_batching: batched = 1 when the density or solve pass runs
@@ -351,8 +354,9 @@ typedef struct FsKernelForms {
                           table (an earlier simulation of the bucket), 3 set by
                           fs_set_kernel_forms                                   */
     uint32_t bucket;   /* floor(log2 hashed particles)                          */
-    float ms[3][4];    /* measured ms (density, XSPH, solve) per depth index, 0
-                          unless measured by this simulation                    */
+    float ms[3][5];    /* measured ms (density, XSPH, solve) per depth index
+                          (depths 0/1, 4, 8, 16, 32), 0 unless measured by this
+                          simulation                                            */
 } FsKernelForms;
 /* The simulation's forms (waits for a pending measurement, like fs_step). */
 int fs_kernel_forms(FsSim *sim, FsKernelForms *out);
@@ -362,7 +366,7 @@ int fs_set_kernel_forms(FsSim *sim, int density_loads, int solve_loads, int xsph
 typedef struct FsKernelFormsEntry {
     uint32_t device, bucket, many_scenes, iterations;
     uint32_t density_loads, solve_loads, xsph_loads, _pad;
-    float ms[3][4];    /* the measured ms the depths were chosen by             */
+    float ms[3][5];    /* the measured ms the depths were chosen by             */
 } FsKernelFormsEntry;
 /* The process-wide table: *count = entries; up to `capacity` copied to out
  * (out may be NULL to query the count). */

@@ -80,7 +80,7 @@ def test_coincident_particles(fslib, oracle_mod, sc):
     """Groups of particles at bit-identical positions (the density pass
     computes one per group and copies it): groups inside one 32-slot warp,
     groups spanning warps and cells, and a large corner clump, stepped with
-    every load depth of the density/solve kernels (measured on steps 8-15)."""
+    every load depth of the neighbour passes (measured on steps 8-17)."""
     import dataclasses
     scene = sc.small_scene(12, 10, 8, seed=5)
     p = scene.particles.copy()
@@ -96,10 +96,10 @@ def test_coincident_particles(fslib, oracle_mod, sc):
     scene = dataclasses.replace(scene, particles=p)
     sim, orc = _run_pair(scene, 1, oracle_mod)
     _compare(sim, orc, n, "coincident step 1")
-    for _ in range(16):
+    for _ in range(18):
         sim.step(1)
         orc.step(1)
-    _compare(sim, orc, n, "coincident step 17")
+    _compare(sim, orc, n, "coincident step 19")
     assert sim.load_batching()[1]
 
 

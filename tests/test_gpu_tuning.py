@@ -1,5 +1,5 @@
 """The neighbour passes' load-depth autotuner (fs_kernel_forms and the
-per-bucket table): the measurement runs on steps 8-15 whatever the fs_step
+per-bucket table): the measurement runs on steps 8-17 whatever the fs_step
 call sizes, each pass keeps its fastest depth, a later simulation of the same
 particle-count bucket takes the table's depths without measuring, and every
 depth gives the same bits (so simulations with any fixed depths, or measured
@@ -11,8 +11,9 @@ from helpers import assert_same_floats, gpu_sim_for_scene
 
 pytestmark = pytest.mark.gpu
 
-DEPTHS = (0, 4, 8, 16)
-XSPH_DEPTHS = (1, 4, 8, 16)
+DEPTHS = (0, 4, 8, 16)                # density
+SOLVE_DEPTHS = (0, 4, 8, 16, 32)      # 32: the staged form
+XSPH_DEPTHS = (1, 4, 8, 16, 32)
 
 
 def _scene():
@@ -34,16 +35,16 @@ def test_forms_tuned_per_bucket_and_results_unchanged():
     a.step(7)
     assert a.kernel_forms()["decided"] == "pending"  # not measured before step 8
     assert a.load_batching() == (False, False)
-    a.step(12)                                         # steps 8-15 measured inside
+    a.step(12)                                         # steps 8-17 measured inside
     f = a.kernel_forms()
     assert f["decided"] == "measured"
-    assert f["density_loads"] in DEPTHS and f["solve_loads"] in DEPTHS
+    assert f["density_loads"] in DEPTHS and f["solve_loads"] in SOLVE_DEPTHS
     assert f["xsph_loads"] in XSPH_DEPTHS
     assert all(t > 0 for row in f["ms"] for t in row)  # every depth of every pass timed
-    # the kept depth is each pass's fastest
+    # the kept depth is each pass's fastest (the density pass over its four)
     for k, key, lst in ((0, "density_loads", DEPTHS), (1, "xsph_loads", XSPH_DEPTHS),
-                        (2, "solve_loads", DEPTHS)):
-        assert lst[int(np.argmin(f["ms"][k]))] == f[key]
+                        (2, "solve_loads", SOLVE_DEPTHS)):
+        assert lst[int(np.argmin(f["ms"][k][:len(lst)]))] == f[key]
     entry = [e for e in kernel_forms_table()
              if e["bucket"] == f["bucket"] and e["iterations"] == 7 and not e["many_scenes"]]
     assert len(entry) == 1 and entry[0]["density_loads"] == f["density_loads"]
@@ -57,7 +58,8 @@ def test_forms_tuned_per_bucket_and_results_unchanged():
     b.close()
     ref = _state(a)
     # every depth, fixed for the whole run, and one mixed choice: the same bits
-    for dens, solve, xsph in [(d, d, x) for d, x in zip(DEPTHS, XSPH_DEPTHS)] + [(0, 16, 8)]:
+    for dens, solve, xsph in [(d, d, x) for d, x in zip(DEPTHS, XSPH_DEPTHS)] + \
+            [(0, 16, 8), (16, 32, 32), (0, 32, 1)]:
         c = gpu_sim_for_scene(sc)
         c.set_kernel_forms(dens, solve, xsph)
         for _ in range(19):
@@ -75,7 +77,9 @@ def test_set_kernel_forms_rejects_unknown_depths(fslib):
     with pytest.raises(Exception):
         sim.set_kernel_forms(3, 4, 4)
     with pytest.raises(Exception):
-        sim.set_kernel_forms(4, 4, 0)   # XSPH depths are 1, 4, 8, 16
+        sim.set_kernel_forms(4, 4, 0)   # XSPH depths are 1, 4, 8, 16, 32
+    with pytest.raises(Exception):
+        sim.set_kernel_forms(32, 4, 4)  # the density pass has no staged form
     sim.set_kernel_forms(16, 0, 1)
     sim.set_kernel_forms()              # back to tuning
     assert sim.kernel_forms()["decided"] in ("pending", "table")
