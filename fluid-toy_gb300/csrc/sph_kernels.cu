@@ -66,11 +66,16 @@ __device__ __forceinline__ bool warp_same_runs(bool active, const Runs &R) {
   const int c0 = __shfl_sync(0xffffffffu, R.count, 0);
   const uint32_t rows0 = __shfl_sync(0xffffffffu, R.rows, 0);
   if (!__all_sync(0xffffffffu, R.count == c0 && R.rows == rows0)) return false;
+  // every lane executes every shuffle (no short-circuit around them: a
+  // full-mask shuffle that some lanes skip is undefined)
   bool same = true;
+#pragma unroll
   for (int r = 0; r < 9; r++) {
-    if (r >= c0) break;
-    same = same && R.lo[r] == __shfl_sync(0xffffffffu, R.lo[r], 0) &&
-           R.hi[r] == __shfl_sync(0xffffffffu, R.hi[r], 0);
+    const bool in = r < c0;  // the same on every lane (counts are equal)
+    const uint32_t lo = in ? R.lo[r] : 0u, hi = in ? R.hi[r] : 0u;
+    const uint32_t lo0 = __shfl_sync(0xffffffffu, lo, 0);
+    const uint32_t hi0 = __shfl_sync(0xffffffffu, hi, 0);
+    same = same & (lo == lo0) & (hi == hi0);
   }
   return __all_sync(0xffffffffu, same);
 }
