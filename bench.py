@@ -36,10 +36,11 @@ for _p in (ROOT / "fluid-toy_gb300", ROOT):
 import numpy as np  # noqa: E402
 
 METRIC = "particle-steps/s"
-# A simulation measures its two density/solve kernel forms on its steps 8-11
-# and keeps the faster (same results either way); warm-ups run past that, so
+# A simulation whose particle-count bucket is not yet in the process-wide
+# table measures its neighbour passes' load depths on its steps 8-17 and keeps
+# the fastest per pass (same results either way); warm-ups run past that, so
 # timed regions use the chosen kernels (the reported warm-up is the count run).
-WARMUP_PAST_TUNING = 16
+WARMUP_PAST_TUNING = 20
 
 
 def kernels_per_step(iterations: int) -> int:
@@ -593,7 +594,7 @@ def run_adjoint(args, dist: Dist) -> dict | None:
     stream = torch.cuda.Stream(device=dev)
     sim = fresh()
     sim.set_stream(stream.cuda_stream)
-    # warm-up past the simulation's load-batching measurement (steps 8-11),
+    # warm-up past the simulation's load-depth measurement (steps 8-17),
     # back to the initial state, then the graphs with the chosen kernels
     sim.step(max(args.warmup, WARMUP_PAST_TUNING))
     sim.upload_particles(sc.particles)

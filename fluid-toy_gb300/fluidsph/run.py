@@ -1,14 +1,15 @@
 """Headless runner: step one of the seeded workloads through the C ABI.
 
-    python fluid-toy_gb300/fluidsph/run.py --config 1 --steps 12 [--graph] [--warmup 16]
-    python fluid-toy_gb300/fluidsph/run.py --batch --steps 10 --warmup 16
+    python fluid-toy_gb300/fluidsph/run.py --config 1 --steps 12 [--graph] [--warmup 20]
+    python fluid-toy_gb300/fluidsph/run.py --batch --steps 10 --warmup 20
     python fluid-toy_gb300/fluidsph/run.py --identify --iterations 2
 
 Each step is one fs_step(sim, 1) call (one launch per kernel, the form that
 profilers can address launch by launch) unless --graph replays them as one
 captured graph. Prints the particle count, steps and wall time. --warmup
-steps run first (a simulation measures its two density/solve kernel forms on
-its steps 8-11 and keeps the faster from then on); the measured steps run
+steps run first (a simulation measures its neighbour passes' load depths on
+its steps 8-17 and keeps the fastest from then on, unless its particle-count
+bucket is already in the process-wide table); the measured steps run
 inside the NVTX range `steps` (when torch is importable).
 
 --batch runs the 256-scene ensemble of scenes.config2 as one SphBatch3DGrid

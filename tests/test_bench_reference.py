@@ -1,5 +1,5 @@
 """bench.py's reference arm on CPU: the oracle timed on the host cores after
-the same warm-up as the GPU arm (at least 16 steps), printed as one JSON line
+the same warm-up as the GPU arm (at least 20 steps), printed as one JSON line
 with the arm's keys, without the product library loaded. Runs the
 49,600-particle dam break (configuration 0) to stay quick."""
 import json
@@ -20,14 +20,14 @@ def test_reference_arm_json_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference"
     assert d["metric"] == "particle-steps/s" and d["higher_is_better"] is True
-    # the GPU arm warms up max(--warmup, 16) steps; so does this arm
-    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 16
+    # the GPU arm warms up max(--warmup, 20) steps; so does this arm
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 20
     assert d["config"]["particles"] == 49600
-    assert d["config"]["steps_timed"] == "17..17"
-    assert d["config"]["gpu_arm_steps_timed"] == "17..18"
+    assert d["config"]["steps_timed"] == "21..21"
+    assert d["config"]["gpu_arm_steps_timed"] == "21..22"
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
-    assert "steps 17..17" in cb["sample"]
+    assert "steps 21..21" in cb["sample"]
     # the oracle only: the product library is never mapped into the arm
     assert "oracle/liboracle.so" in d["libraries_loaded"]
     assert not any("libfluidsph" in f for f in d["libraries_loaded"]), d["libraries_loaded"]
