@@ -11,10 +11,11 @@ namespace fs {
 
 // Load depths (candidate records in flight per lane) each neighbour pass is
 // instantiated for; see kLoadDepths / kXsphDepths in sph_kernels.cu. 32 is the
-// staged form (a warp's chunk of 32 records in shared memory); the density
-// pass has no staged form and is tuned over the first four only.
+// staged form of XSPH (a warp's chunk of 32 records in shared memory); the
+// density and solve passes have no staged form and are tuned over the first
+// four only.
 constexpr int kNumLoadDepths = 5;
-constexpr int kDensityCandidates = 4;
+constexpr int kPlainCandidates = 4;
 constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
 constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16, 32};
 

@@ -397,7 +397,7 @@ int tune_decide(FsSim *s) {
   }
   uint8_t best[3] = {0, 0, 0};
   for (int k = 0; k < 3; k++)
-    for (int c = 1; c < (k == 0 ? kDensityCandidates : kNumLoadDepths); c++)
+    for (int c = 1; c < (k == 1 ? kNumLoadDepths : kPlainCandidates); c++)  // XSPH: staged too
       if (ms[k][c] < ms[k][best[k]]) best[k] = uint8_t(c);
   s->forms.density = best[0];
   s->forms.xsph = best[1];
@@ -418,8 +418,9 @@ int tune_steps(FsSim *s, uint32_t &nsteps) {
   while (nsteps > 0 && s->tune_state == 0 && s->steps_done >= kTuneAfterSteps) {
     const int p = s->tune_phase;
     const int c = tune_candidate(p);
-    KernelForms f;
-    f.density = f.solve = f.xsph = uint8_t(c);
+    KernelForms f;  // depth 32 (the last candidate) is XSPH's alone
+    f.xsph = uint8_t(c);
+    f.density = f.solve = uint8_t(c < kPlainCandidates ? c : kPlainCandidates - 1);
     const int rc = enqueue_step(s, false, nullptr, &f, s->tune_ev[p]);
     if (rc) return rc;
     s->steps_done++;
@@ -858,16 +859,17 @@ int fs_set_kernel_forms(FsSim *s, int density_loads, int solve_loads, int xsph_l
             x = index_of(kXsphDepthList, xsph_loads);
   if (d < 0 || so < 0 || x < 0)
     return fail(FS_E_INVALID_ARGUMENT,
-                "fs_set_kernel_forms: depths must be in {0, 4, 8, 16} (density), "
-                "{0, 4, 8, 16, 32} (solve) and {1, 4, 8, 16, 32} (xsph), or all -1");
+                "fs_set_kernel_forms: depths must be in {0, 4, 8, 16} (density, solve) "
+                "and {1, 4, 8, 16, 32} (xsph), or all -1");
   int rc;
   if ((rc = set_device(s))) return rc;
   if (s->tune_state == 1 && !capturing(s)) {
     // measured steps in flight: let them finish before their events are reused
     FS_CUDA(cudaEventSynchronize(s->tune_ev[kTuneSteps - 1][8]), "kernel-form measurement");
   }
-  if (d == kDensityCandidates)
-    return fail(FS_E_INVALID_ARGUMENT, "fs_set_kernel_forms: the density pass has no staged form");
+  if (d >= kPlainCandidates || so >= kPlainCandidates)
+    return fail(FS_E_INVALID_ARGUMENT,
+                "fs_set_kernel_forms: the density and solve passes have no staged form");
   s->forms.density = uint8_t(d);
   s->forms.solve = uint8_t(so);
   s->forms.xsph = uint8_t(x);

@@ -48,7 +48,7 @@ constexpr int kLoadDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
 constexpr int kXsphDepths[kNumLoadDepths] = {1, 4, 8, 16, 32};
 static_assert(kLoadDepths[3] == int(kDensityDepths[3]) && kXsphDepths[0] == int(kXsphDepthList[0]),
               "depth lists agree");
-// The staged form (load depth kStagedLoads; XSPH and the PCISPH solve): in a
+// The staged form (load depth kStagedLoads, XSPH): in a
 // warp whose 32 lanes are all in one cell (the same neighbour runs: the dense
 // clumps, where the time goes), candidate records go through shared memory in
 // chunks of 32, each lane loading one record of the next chunk while the warp
@@ -57,7 +57,9 @@ static_assert(kLoadDepths[3] == int(kDensityDepths[3]) && kXsphDepths[0] == int(
 // shaders' order, so the bits are those of the other forms; other warps run
 // the plain loop. (Streaming the union of the runs of lanes in x-adjacent
 // cells, each lane taking only its own candidates, was measured slower: the
-// lanes idle over the union's extra cell.)
+// lanes idle over the union's extra cell. A staged form of the PCISPH solve
+// was measured slower than its batched loads on every workload and is not
+// built: 6.1 against 4.8 ms per step on the 1M-particle dam break.)
 constexpr int kStagedLoads = 32;
 
 // Whether every lane of the warp is active with the same runs (one cell).
@@ -630,17 +632,10 @@ __device__ __forceinline__ void solve_one(
   R.count = 0;
   R.total = 0;
   R.words = 0;
-  // staged form: per warp, one chunk of 32 candidate records (block of 128)
-  __shared__ float4 st_xp[B == kStagedLoads ? 4 : 1][32];
-  __shared__ float st_pt[B == kStagedLoads ? 4 : 1][32];
   float3 pos_i = f3(0.f, 0.f, 0.f);
   if (active) {
     pos_i = xyz(s_pos[s]);  // current position decides the cells
     neighbor_runs(pos_i, U->grid, begin + U->c_offset, R);
-  }
-  bool uniform = false;
-  if constexpr (B == kStagedLoads) uniform = warp_same_runs(active, R);
-  if (active) {
     const float4 self_xp = xp_in[s];
     const float3 pred_pos = xyz(self_xp);
     const float old_p = self_xp.w;
@@ -649,7 +644,8 @@ __device__ __forceinline__ void solve_one(
     // old_p / (sd * sd) with sd = max(rho_in[s], 1), written by the previous
     // iteration (read only when there is pressure)
     const float self_term = HAS_PRESSURE ? pterm_in[s] : 0.0f;
-    auto pressure_term = [&](float3 r_vec, float r_sq, float pt) {  // pt = np / (nd * nd)
+    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
+      const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
       const float3 nr = -r_vec;
       // correctly rounded fast square root, reciprocal and quotients, one
       // range check for the pair (IEEE operations outside it)
@@ -666,80 +662,20 @@ __device__ __forceinline__ void solve_one(
       const float grad = scale_g * dg * dg;
       a_p = a_p + (-mass * (self_term + pt) * grad) * dir;
     };
-    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
-      pressure_term(r_vec, r_sq, __ldg(pterm_in + j));
-    };
     uint32_t *hit_words = nullptr;
     if (RECORD) {
       const uint32_t off = mask_off[s];
       hit_words = off == MASK_NONE ? nullptr : hit_out + off;
     }
     uint32_t widx = 0u;
-    if constexpr (B == kStagedLoads) {
-      if (uniform) {
-        // staged: every lane of the warp has these runs; chunks of 32
-        // records go through shared memory, lane l loading record l of the
-        // next chunk while the warp works on the current one
-        StagedChunks ch(R);
-        float4 pf_xp = make_float4(0.f, 0.f, 0.f, 0.f);
-        float pf_pt = 0.0f;
-        const unsigned lane = threadIdx.x & 31u;
-        if (ch.valid && lane < ch.cnt) {
-          pf_xp = __ldg(xp_in + ch.base + lane);
-          if (HAS_PRESSURE) pf_pt = __ldg(pterm_in + ch.base + lane);
-        }
-        float4 *sx = st_xp[threadIdx.x >> 5];
-        float *sp = st_pt[threadIdx.x >> 5];
-        while (ch.valid) {
-          const uint32_t cnt = ch.cnt;
-          const float4 cur_xp = pf_xp;
-          const float cur_pt = pf_pt;
-          ch.advance(R);
-          if (ch.valid && lane < ch.cnt) {
-            pf_xp = __ldg(xp_in + ch.base + lane);
-            if (HAS_PRESSURE) pf_pt = __ldg(pterm_in + ch.base + lane);
-          }
-          __syncwarp();  // the previous chunk's readers are done
-          sx[lane] = cur_xp;
-          if (HAS_PRESSURE) sp[lane] = cur_pt;
-          __syncwarp();
-          uint32_t chunk = 0u, hitw = 0u;
-#pragma unroll 4
-          for (uint32_t k = 0; k < cnt; k++) {
-            const float4 nb = sx[k];
-            const float3 r_vec = pred_pos - xyz(nb);
-            const float r_sq = dot3(r_vec, r_vec);
-            if (r_sq < h2) {
-              hits++;
-              const float diff = h2 - r_sq;
-              pred_density += mass * (scale_d * diff * diff * diff);
-              if (HAS_PRESSURE && r_sq > 1e-12f) chunk |= 1u << k;
-              if (RECORD) hitw |= 1u << k;
-            }
-          }
-          if (RECORD) {
-            if (hit_words) hit_words[widx] = hit_or ? (hit_words[widx] | hitw) : hitw;
-            widx++;
-          }
-          if (HAS_PRESSURE) {
-            while (chunk) {
-              const uint32_t k = uint32_t(__ffs(chunk) - 1);
-              chunk &= chunk - 1u;
-              const float3 r_vec = pred_pos - xyz(sx[k]);
-              pressure_term(r_vec, dot3(r_vec, r_vec), sp[k]);
-            }
-          }
-        }
-      }
-    }
     // candidates in chunks of up to 32: the predicted density is summed while
     // testing; the pressure hits of the chunk go to a per-lane bitmask that
     // each lane then walks (its own hits only, ascending)
-    for (int r = 0; r < ((B == kStagedLoads && uniform) ? 0 : R.count); r++) {
+    for (int r = 0; r < R.count; r++) {
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
         uint32_t chunk = 0u, hitw = 0u;
-        batched_loop<(B == kStagedLoads ? 0 : B)>(
+        batched_loop<B>(
             cnt, [&](uint32_t k) { return __ldg(xp_in + base + k); },
             [&](uint32_t k, const float4 nb) {
               const float3 r_vec = pred_pos - xyz(nb);
@@ -1589,7 +1525,6 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
       case 1: FS_SOLVE_B(P_, L_, R_, kLoadDepths[1], q); break;    \
       case 2: FS_SOLVE_B(P_, L_, R_, kLoadDepths[2], q); break;    \
       case 3: FS_SOLVE_B(P_, L_, R_, kLoadDepths[3], q); break;    \
-      case 4: FS_SOLVE_B(P_, L_, R_, kLoadDepths[4], q); break;    \
       default: FS_SOLVE_B(P_, L_, R_, kLoadDepths[0], q); break;   \
     }                                                              \
   } while (0)
@@ -1609,7 +1544,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     if (hit_out) FS_SOLVE0(L_, true);  \
     else FS_SOLVE0(L_, false);         \
   } while (0)
-  const bool batched = kLoadDepths[d.load_solve < kNumLoadDepths ? d.load_solve : 0] > 1;
+  const bool batched = kLoadDepths[d.load_solve < kPlainCandidates ? d.load_solve : 0] > 1;
   if (iter == 0 && last && batched) FS_SOLVE_R(true, true);
   else if (iter == 0 && last) FS_SOLVE0_R(true);
   else if (iter == 0 && batched) FS_SOLVE_R(true, false);

@@ -331,9 +331,9 @@ int fs_prepare_steps(FsSim *sim, uint32_t nsteps);
  * PCISPH solve) each exist in several forms that differ only in how many
  * candidate records a lane loads ahead (the load depth: 0 = the plain loop,
  * 4, 8 or 16 for density and solve; 1, 4, 8 or 16 for XSPH; 32 = the staged
- * form of XSPH and solve, in which a warp whose lanes share one cell moves
- * chunks of 32 records through shared memory, each lane loading one record
- * of the next chunk). Every form gives
+ * form of XSPH, in which a warp whose lanes share one cell moves chunks of 32
+ * records through shared memory, each lane loading one record of the next
+ * chunk). Every form gives
  * the same bits; which is fastest depends on the workload (deeper batches hide
  * more latency per lane but fit fewer warps on an SM), so a project-written
  * autotuner chooses per particle-count bucket: the bucket is

@@ -12,8 +12,8 @@ from helpers import assert_same_floats, gpu_sim_for_scene
 pytestmark = pytest.mark.gpu
 
 DEPTHS = (0, 4, 8, 16)                # density
-SOLVE_DEPTHS = (0, 4, 8, 16, 32)      # 32: the staged form
-XSPH_DEPTHS = (1, 4, 8, 16, 32)
+SOLVE_DEPTHS = (0, 4, 8, 16)
+XSPH_DEPTHS = (1, 4, 8, 16, 32)       # 32: the staged form
 
 
 def _scene():
@@ -41,7 +41,7 @@ def test_forms_tuned_per_bucket_and_results_unchanged():
     assert f["density_loads"] in DEPTHS and f["solve_loads"] in SOLVE_DEPTHS
     assert f["xsph_loads"] in XSPH_DEPTHS
     assert all(t > 0 for row in f["ms"] for t in row)  # every depth of every pass timed
-    # the kept depth is each pass's fastest (the density pass over its four)
+    # the kept depth is each pass's fastest (density and solve over their four)
     for k, key, lst in ((0, "density_loads", DEPTHS), (1, "xsph_loads", XSPH_DEPTHS),
                         (2, "solve_loads", SOLVE_DEPTHS)):
         assert lst[int(np.argmin(f["ms"][k][:len(lst)]))] == f[key]
@@ -59,7 +59,7 @@ def test_forms_tuned_per_bucket_and_results_unchanged():
     ref = _state(a)
     # every depth, fixed for the whole run, and one mixed choice: the same bits
     for dens, solve, xsph in [(d, d, x) for d, x in zip(DEPTHS, XSPH_DEPTHS)] + \
-            [(0, 16, 8), (16, 32, 32), (0, 32, 1)]:
+            [(0, 16, 8), (16, 16, 32), (0, 0, 32)]:
         c = gpu_sim_for_scene(sc)
         c.set_kernel_forms(dens, solve, xsph)
         for _ in range(19):
@@ -80,6 +80,8 @@ def test_set_kernel_forms_rejects_unknown_depths(fslib):
         sim.set_kernel_forms(4, 4, 0)   # XSPH depths are 1, 4, 8, 16, 32
     with pytest.raises(Exception):
         sim.set_kernel_forms(32, 4, 4)  # the density pass has no staged form
+    with pytest.raises(Exception):
+        sim.set_kernel_forms(4, 32, 4)  # nor has the solve
     sim.set_kernel_forms(16, 0, 1)
     sim.set_kernel_forms()              # back to tuning
     assert sim.kernel_forms()["decided"] in ("pending", "table")
