@@ -12,6 +12,11 @@ its steps 8-17 and keeps the fastest from then on, unless its particle-count
 bucket is already in the process-wide table); the measured steps run
 inside the NVTX range `steps` (when torch is importable).
 
+--lattice NX NY NZ replaces the configuration's lattice (same box, spacing and
+parameters: e.g. 64 64 64 = 262,144 particles, a case small enough for
+full-set profiles of the dam break); --forms D X S fixes the neighbour passes'
+load depths (density, XSPH, solve; fs_set_kernel_forms) instead of tuning them.
+
 --batch runs the 256-scene ensemble of scenes.config2 as one SphBatch3DGrid
 (one launch per stage for all scenes) instead of a single scene.
 
@@ -129,6 +134,10 @@ def main(argv=None) -> int:
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--identify", action="store_true")
     ap.add_argument("--iterations", type=int, default=2)
+    ap.add_argument("--lattice", type=int, nargs=3, default=None,
+                    help="NX NY NZ lattice in the configuration's box")
+    ap.add_argument("--forms", type=int, nargs=3, default=None,
+                    help="fixed load depths: density xsph solve")
     ap.add_argument("--scenes", type=int, default=64, help="--identify: scenes (the first n)")
     ap.add_argument("--rollout-steps", type=int, default=150, help="--identify: steps")
     ap.add_argument("--every", type=int, default=15, help="--identify: checkpoint interval")
@@ -151,11 +160,18 @@ def main(argv=None) -> int:
         b.close()
         return 0
     sc = scenes.CONFIGS[a.config]()
+    if a.lattice:
+        nx, ny, nz = a.lattice
+        sc.particles = scenes.lattice_block(nx, ny, nz, sc.box)
+        sc.sph.num_particles = len(sc.particles)
+        sc.name = f"{sc.name}_lattice_{nx}x{ny}x{nz}"
     sim = SphSimulation3DGrid(sc.particles, sc.sph, sc.geom, device=a.device)
     sim.update_gravity(sc.gravity)
     sim.set_pcisph_iterations(sc.iterations)
     if sc.rigid is not None:
         sim.update_rigid_body(sc.rigid)
+    if a.forms:
+        sim.set_kernel_forms(a.forms[0], a.forms[2], a.forms[1])
     secs = run_steps(sim, a.steps, a.warmup, a.graph)
     print(f"{sc.name}: {sc.n} particles, {a.steps} steps, {secs:.3f} s")
     sim.close()
