@@ -19,6 +19,12 @@ constexpr int kPlainCandidates = 4;
 constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
 constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16, 32};
 
+// Work-order scratch words (DevState::order_hist), zeroed each step: the
+// bucket counts and cursors of the 33 work buckets, the small-coordinate
+// flag of the positions, and one per PCISPH level of predicted positions.
+constexpr int SMALL_LEVEL_FLAGS = 64;
+constexpr int ORDER_HIST_WORDS = 2 * 33 + 1 + SMALL_LEVEL_FLAGS;
+
 // The neighbour passes' load-depth choice of a simulation (indices into the
 // lists above).
 struct KernelForms {
@@ -132,7 +138,9 @@ struct DevState {
   // density, XSPH and solve; a slot permutation by hit count for force.
   uint32_t *warp_order;            // [M / 32] warp ids
   uint8_t *warp_bucket;            // [M / 32] work bucket of each warp
-  uint32_t *order_hist;            // bucket counts, then bucket cursors
+  uint32_t *order_hist;            // [ORDER_HIST_WORDS] bucket counts, bucket cursors,
+                                   // then the step's small-coordinate flags: positions,
+                                   // then each PCISPH level's predicted positions
   uint32_t *perm_hit;              // [M] sorted slots by decreasing hit count
   uint16_t *work_key;              // [M] hit-count bucket of each sorted slot
   uint32_t *key_hist;              // [3 * KEY_BUCKETS]: counts, bases, cursors

@@ -145,7 +145,7 @@ void carve(FsSim *s, char *base, size_t *bytes) {
   d.mask_hits = c.take<uint32_t>(M);
   d.warp_order = c.take<uint32_t>((M + 31) / 32);
   d.warp_bucket = c.take<uint8_t>((M + 31) / 32);
-  d.order_hist = c.take<uint32_t>(2 * 33);
+  d.order_hist = c.take<uint32_t>(ORDER_HIST_WORDS);
   d.perm_hit = c.take<uint32_t>(M);
   d.work_key = c.take<uint16_t>(M);
   d.key_hist = c.take<uint32_t>(3 * KEY_BUCKETS);

@@ -402,6 +402,24 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
   vel_x[s] = make_float4(vn.x, vn.y, vn.z, vi4.w);
 }
 
+// ---- small coordinates --------------------------------------------------------
+// A position coordinate c with 0 < |c| < 2^-34. When no particle has one,
+// every nonzero coordinate difference of two particles is >= 2^-57 in
+// magnitude (both coordinates are zero or multiples of 2^-57, or they have
+// opposite signs), so the passes that divide those differences by r skip
+// their per-pair lower-bound checks. k_warp_work flags the positions each
+// step; the producer of each PCISPH level of predicted positions (force +
+// predict for level 0, solve iteration k for level k + 1) flags that level
+// (levels from SMALL_LEVEL_FLAGS - 1 on share the last word, which only
+// makes their readers check more).
+__device__ __forceinline__ bool small_coord(float c) {
+  const float a = fabsf(c);
+  return a < 0x1p-34f && a != 0.0f;
+}
+__device__ __forceinline__ void flag_small_coords(float3 x, uint32_t *flag) {
+  if (small_coord(x.x) || small_coord(x.y) || small_coord(x.z)) atomicOr(flag, 1u);
+}
+
 // ---- force + PCISPH predict ---------------------------------------------------
 // Two hits per walk iteration: their terms are computed side by side (three
 // measured no faster).
@@ -415,9 +433,10 @@ __device__ __forceinline__ void force_predict_one(
                     const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
-                    const uint32_t *__restrict__ mask_off, float4 *__restrict__ anp,
-                    float4 *__restrict__ pred_xp, float *__restrict__ pred_rho,
-                    float *__restrict__ pterm0) {
+                    const uint32_t *__restrict__ mask_off,
+                    const uint32_t *__restrict__ small_flag, uint32_t *__restrict__ small_xp,
+                    float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
+                    float *__restrict__ pred_rho, float *__restrict__ pterm0) {
   if (s >= v.b->n_sorted) return;
   const DevUniforms *U = v.u + v.scene_of_slot[s];
   const GpuSphParams3D &P = U->sph;
@@ -427,7 +446,15 @@ __device__ __forceinline__ void force_predict_one(
   const float near_k = P.near_stiffness, visc = P.viscosity, rho0 = P.rest_density;
   const float min_dist = h * 0.1f;
   const float y_min_dist = __frcp_rn(min_dist);
-  const bool min_dist_ok = rcp_den_ok(min_dist);
+  const float two_rho0 = 2.0f * rho0;
+  // Operand ranges that hold for every pair the walk visits. The walked pairs
+  // are the density pass's hits, 1e-12 < r^2 < h^2 (the same r^2 bit for bit:
+  // the same positions and expression), so with h^2 < 2^59 the values r^2, r
+  // and the viscosity denominator r^2 + 0.01 h^2 lie in [2^-60, 2^60).
+  // Densities and near densities are clamped to >= 1, so the near-pressure
+  // denominator and the density sum are >= 2 and need only an upper bound.
+  // What is checked per pair: the numerators and those two upper bounds.
+  const bool fast_particle = h2 < 0x1p59f && rcp_den_ok(min_dist) && fast_num_ok(two_rho0);
   const float3 pos_i = xyz(s_pos[s]);
   const float3 vel_i = xyz(vel_x[s]);
   const float2 di = s_dens[s];
@@ -453,7 +480,7 @@ __device__ __forceinline__ void force_predict_one(
     float3 v;    // viscosity term
     float3 c1;   // cohesion term
     float3 c2;   // normal-difference term
-    bool close, visc, ok;
+    bool close, ok;
   };
   auto load = [&](uint32_t j) {
     return Rec{__ldg(nb_pos + j), __ldg(nb_vel + j), __ldg(nb_nrm + j)};
@@ -461,18 +488,11 @@ __device__ __forceinline__ void force_predict_one(
   // The pair's terms, with the correctly rounded fast reciprocal, square
   // root and quotients (FAST; t.ok reports whether every operand was in
   // their validated range) or with the IEEE operations.
-  auto terms_impl = [&](uint32_t j, const Rec &q, auto fast) {
+  auto terms_impl = [&](uint32_t j, const Rec &q, auto fast, auto dv_check) {
     constexpr bool FAST = decltype(fast)::value;
+    constexpr bool DV_CHECK = decltype(dv_check)::value;
     Terms t;
-    bool ok = true;
-    auto div = [&](float a, float b) -> float {
-      if constexpr (FAST) {
-        ok = ok && fast_num_ok(a) && fast_ok(b);
-        return markstein(a, b, rcp_fast(b));
-      } else {
-        return a / b;
-      }
-    };
+    bool ok = fast_particle;
     const float3 pos_j = xyz(q.p);
     const float3 vel_j = xyz(q.v);
     const float3 n_j = xyz(q.n);
@@ -480,9 +500,7 @@ __device__ __forceinline__ void force_predict_one(
     const float r_sq = dot3(r_vec, r_vec);
     float rr, y_rr;
     if constexpr (FAST) {
-      ok = fast_ok(r_sq);
       rr = sqrt_fast(r_sq);
-      ok = ok && fast_ok(rr);
       y_rr = rcp_fast(rr);
     } else {
       rr = sqrtf(r_sq);
@@ -494,44 +512,74 @@ __device__ __forceinline__ void force_predict_one(
     // (pos_j - pos_i) / rr with one shared reciprocal, bit-identical; and
     // pos_j - pos_i is -r_vec exactly (IEEE subtraction is sign-symmetric).
     const float dvx = -r_vec.x, dvy = -r_vec.y, dvz = -r_vec.z;
-    float3 dir_far;
-    float q_sep;
+    float3 dir;
     if constexpr (FAST) {
-      dir_far = f3(markstein(dvx, rr, y_rr), markstein(dvy, rr, y_rr), markstein(dvz, rr, y_rr));
-      q_sep = markstein(rr, min_dist, y_min_dist);
-      ok = ok && min_dist_ok && fast_num_ok(dvx) && fast_num_ok(dvy) && fast_num_ok(dvz);
+      dir = f3(markstein(dvx, rr, y_rr), markstein(dvy, rr, y_rr), markstein(dvz, rr, y_rr));
+      // the components' magnitudes are below r < 2^30; without DV_CHECK no
+      // position has a coordinate 0 < |c| < 2^-34, so they are also 0 or
+      // >= 2^-57
+      if constexpr (DV_CHECK)
+        ok = ok && fast_num_lo_ok(dvx) && fast_num_lo_ok(dvy) && fast_num_lo_ok(dvz);
     } else {
-      dir_far = f3(dvx / rr, dvy / rr, dvz / rr);
-      q_sep = rr / min_dist;
+      dir = f3(dvx / rr, dvy / rr, dvz / rr);
     }
-    const int d = int(s) - int(j);
-    const bool tabulated = d >= -dir_half && d <= dir_half;
-    float3 dir_close = dir_far;
-    if (t.close && tabulated) dir_close = xyz(__ldg(dir_tab + (d + dir_half)));
-    if (t.close && !tabulated)
-      dir_close = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
-    const float3 dir = t.close ? dir_close : dir_far;
+    // r < 0.1 h (rare: a few pairs per particle even in the clumps): the
+    // slot-difference direction and the separation term
+    // (sph_force_3d_grid.wgsl:160-176)
+    t.sep = f3(0.f, 0.f, 0.f);
+    if (t.close) {
+      const int d = int(s) - int(j);
+      if (d >= -dir_half && d <= dir_half)
+        dir = xyz(__ldg(dir_tab + (d + dir_half)));
+      else
+        dir = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
+      const float q_sep = FAST ? markstein(rr, min_dist, y_min_dist) : rr / min_dist;
+      const float sep = 200.0f * (1.0f - q_sep);
+      t.sep = (-sep) * dir;
+    }
     const float density_j = q.p.w;       // max(density_j, 1)
     const float near_density_j = q.n.w;  // max(near density_j, 1)
     const float near_pressure_j = near_k * near_density_j;
     const float dg = h - rr;
     const float grad = scale_g * dg * dg;
-    t.p = div(-mass * (near_pressure_i + near_pressure_j), 2.0f * density_i * near_density_j) *
-          dir * grad;
-    const float sep = 200.0f * (1.0f - q_sep);
-    t.sep = (-sep) * dir;
+    const float np_num = -mass * (near_pressure_i + near_pressure_j);
+    const float np_den = 2.0f * density_i * near_density_j;
     const float3 v_ij = vel_i - vel_j;
     const float v_dot_x = dot3(v_ij, r_vec);
-    const float mu = div(h * v_dot_x, r_sq + 0.01f * h2);
-    const float avg_density = (density_i + density_j) * 0.5f;
-    const float pi_visc = div(-visc * mu, avg_density);
-    t.v = (-mass * pi_visc * grad) * dir;
-    t.visc = v_dot_x < 0.0f;
-    const float K_ij = div(2.0f * rho0, density_i + density_j);
+    const float mu_num = h * v_dot_x;
+    const float mu_den = r_sq + 0.01f * h2;
+    const float dsum = density_i + density_j;
+    const float avg_density = dsum * 0.5f;
+    float np_q, mu, pi_visc, K_ij;
+    if constexpr (FAST) {
+      // 1 / avg_density is 2 / dsum: with y = RN(1 / dsum), 2 y = RN(1 / avg_density)
+      // exactly (dsum in [2, 2^60): the halving and doubling are exact)
+      const float y_sum = rcp_fast(dsum);
+      np_q = markstein(np_num, np_den, rcp_fast(np_den));
+      mu = markstein(mu_num, mu_den, rcp_fast(mu_den));
+      const float pi_num = -visc * mu;
+      pi_visc = markstein(pi_num, avg_density, 2.0f * y_sum);
+      K_ij = markstein(two_rho0, dsum, y_sum);
+      ok = ok && fast_num_ok(np_num) && np_den < 0x1p60f && fast_num_ok(mu_num) &&
+           fast_num_ok(pi_num) && dsum < 0x1p60f;
+    } else {
+      np_q = np_num / np_den;
+      mu = mu_num / mu_den;
+      pi_visc = (-visc * mu) / avg_density;
+      K_ij = two_rho0 / dsum;
+    }
+    t.p = np_q * dir * grad;
+    // the viscosity term where v_ij . r_ij < 0, else (+0) * dir: adding a
+    // zero leaves the sum's bits (the sums start at +0 and an RN sum is -0
+    // only when both operands are), so the shader's branch is one select
+    const float visc_c = v_dot_x < 0.0f ? -mass * pi_visc * grad : 0.0f;
+    t.v = visc_c * dir;
+    // akinci_cohesion_kernel: r >= h/2: s_c dg^3 r^3; else s_c (2 dg^3 r^3 -
+    // h^6/64), each product chain in the shader's order from its first factor
     const float r3 = rr * rr * rr;
-    const float coh_far = scale_c * dg * dg * dg * r3;
-    const float coh_near = scale_c * (2.0f * dg * dg * dg * r3 - P.kernel_radius_pow6 / 64.0f);
-    const float coh = rr >= h * 0.5f ? coh_far : coh_near;
+    const bool coh_far = rr >= h * 0.5f;
+    const float coh_chain = (coh_far ? scale_c : 2.0f) * dg * dg * dg * r3;
+    const float coh = coh_far ? coh_chain : scale_c * (coh_chain - P.kernel_radius_pow6 / 64.0f);
     t.c1 = (mass * K_ij * coh) * dir;
     t.c2 = (mass * K_ij) * (n_i - n_j);
     t.ok = ok;
@@ -539,40 +587,46 @@ __device__ __forceinline__ void force_predict_one(
   };
   // the fast form, recomputed with IEEE operations when an operand is out of
   // range (never on ordinary inputs: one rarely taken branch per pair)
-  auto terms = [&](uint32_t j, const Rec &q) {
-    Terms t = terms_impl(j, q, std::true_type{});
-    if (!t.ok) t = terms_impl(j, q, std::false_type{});
+  auto terms = [&](uint32_t j, const Rec &q, auto dv_check) {
+    Terms t = terms_impl(j, q, std::true_type{}, dv_check);
+    if (!t.ok) t = terms_impl(j, q, std::false_type{}, dv_check);
     return t;
   };
   auto add = [&](const Terms &t) {
     a_p = a_p + t.p;
-    const float3 a_p_sep = a_p + t.sep;
-    a_p = t.close ? a_p_sep : a_p;
-    const float3 a_v_new = a_v + t.v;
-    a_v = t.visc ? a_v_new : a_v;
+    if (t.close) a_p = a_p + t.sep;
+    a_v = a_v + t.v;
     a_c = a_c + t.c1;
     a_c = a_c - t.c2;
   };
-  auto body = [&](uint32_t j) { add(terms(j, load(j))); };
   const uint32_t off = mask_off[s];
-  if (off != MASK_NONE) {
+  // the mask walk, with or without the direction numerators' checks (the
+  // step-wide small-coordinate flag decides, the same for every particle)
+  auto walk = [&](auto dv_check) {
+    auto body = [&](uint32_t j) { add(terms(j, load(j), dv_check)); };
+    MaskWalk m;
+    m.init(R, mask_words + off);
     if (kForceHitPairs) {
-      MaskWalk m;
-      m.init(R, mask_words + off);
       uint32_t j0, j1;
       while (m.next(R, j0)) {
         if (!m.next(R, j1)) {
           body(j0);
           break;
         }
-        const Terms t0 = terms(j0, load(j0));
-        const Terms t1 = terms(j1, load(j1));
+        const Terms t0 = terms(j0, load(j0), dv_check);
+        const Terms t1 = terms(j1, load(j1), dv_check);
         add(t0);
         add(t1);
       }
     } else {
       walk_mask(R, mask_words + off, body);
     }
+  };
+  if (off != MASK_NONE) {
+    if (__ldg(small_flag) == 0u)
+      walk(std::false_type{});
+    else
+      walk(std::true_type{});
   } else {
     for_each_hit(
         R,
@@ -582,7 +636,7 @@ __device__ __forceinline__ void force_predict_one(
           const float r_sq = rx * rx + ry * ry + rz * rz;
           return r_sq < h2 && r_sq > 1e-12f;
         },
-        body);
+        [&](uint32_t j) { add(terms(j, load(j), std::true_type{})); });
   }
   a_c = a_c * P.surface_tension;
   const float3 a_g = xyz(U->gravity.direction);
@@ -592,6 +646,7 @@ __device__ __forceinline__ void force_predict_one(
   const float3 v_star = vel_i + dt * a;
   const float3 x_star = pos_i + dt * v_star;
   pred_xp[s] = make_float4(x_star.x, x_star.y, x_star.z, 0.0f);
+  flag_small_coords(x_star, small_xp);
   pred_rho[s] = 0.0f;
   pterm0[s] = 0.0f;  // iteration 0's pressure terms (see launch_solve)
 }
@@ -620,7 +675,8 @@ __device__ __forceinline__ void solve_one(
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
-            uint32_t *__restrict__ hit_out, bool hit_or) {
+            uint32_t *__restrict__ hit_out, bool hit_or, const uint32_t *__restrict__ small_in,
+            uint32_t *__restrict__ small_out) {
   const bool active = s < v.b->n_sorted;
   const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
@@ -644,17 +700,24 @@ __device__ __forceinline__ void solve_one(
     // old_p / (sd * sd) with sd = max(rho_in[s], 1), written by the previous
     // iteration (read only when there is pressure)
     const float self_term = HAS_PRESSURE ? pterm_in[s] : 0.0f;
-    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
+    const bool fast_h2 = h2 < 0x1p59f;
+    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq, auto dv_check) {
       const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
       const float3 nr = -r_vec;
       // correctly rounded fast square root, reciprocal and quotients, one
-      // range check for the pair (IEEE operations outside it)
+      // range check for the pair (IEEE operations outside it). The pair is a
+      // hit, 1e-12 < r^2 < h^2, so with h^2 < 2^59 r^2 and r are in the
+      // validated range and |nr| < r; the numerators' lower bound is checked
+      // per pair unless no predicted position of this level has a coordinate
+      // 0 < |c| < 2^-34 (then every nonzero component is >= 2^-57).
       float rr = sqrt_fast(r_sq);
       const float y_rr = rcp_fast(rr);
       float3 dir = f3(markstein(nr.x, rr, y_rr), markstein(nr.y, rr, y_rr),
                       markstein(nr.z, rr, y_rr));
-      if (!(fast_ok(r_sq) && fast_ok(rr) && fast_num_ok(nr.x) && fast_num_ok(nr.y) &&
-            fast_num_ok(nr.z))) {
+      bool ok = fast_h2;
+      if constexpr (decltype(dv_check)::value)
+        ok = ok && fast_num_lo_ok(nr.x) && fast_num_lo_ok(nr.y) && fast_num_lo_ok(nr.z);
+      if (!ok) {
         rr = sqrtf(r_sq);
         dir = f3(nr.x / rr, nr.y / rr, nr.z / rr);
       }
@@ -667,10 +730,11 @@ __device__ __forceinline__ void solve_one(
       const uint32_t off = mask_off[s];
       hit_words = off == MASK_NONE ? nullptr : hit_out + off;
     }
-    uint32_t widx = 0u;
     // candidates in chunks of up to 32: the predicted density is summed while
     // testing; the pressure hits of the chunk go to a per-lane bitmask that
     // each lane then walks (its own hits only, ascending)
+    auto run = [&](auto dv_check) {
+    uint32_t widx = 0u;
     for (int r = 0; r < R.count; r++) {
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
         const uint32_t cnt = min(32u, R.hi[r] - base);
@@ -698,11 +762,16 @@ __device__ __forceinline__ void solve_one(
             chunk &= chunk - 1u;
             const float4 nb = __ldg(xp_in + j);
             const float3 r_vec = pred_pos - xyz(nb);
-            pressure(j, r_vec, dot3(r_vec, r_vec));
+            pressure(j, r_vec, dot3(r_vec, r_vec), dv_check);
           }
         }
       }
     }
+    };
+    if (HAS_PRESSURE && __ldg(small_in) == 0u)
+      run(std::false_type{});
+    else
+      run(std::true_type{});
     const float density_error = fmaxf(0.0f, pred_density - P.rest_density);
     const float new_p = old_p + P.pcisph_delta * density_error;
     const float dt = P.dt;
@@ -718,6 +787,7 @@ __device__ __forceinline__ void solve_one(
     } else {
       const float3 x_star = pos_i + dt * v_star;
       xp_out[s] = make_float4(x_star.x, x_star.y, x_star.z, new_p);
+      flag_small_coords(x_star, small_out);
       rho_out[s] = pred_density;
       const float nd = fmaxf(pred_density, 1.0f);
       pterm_out[s] = new_p / (nd * nd);
@@ -780,25 +850,32 @@ __device__ __forceinline__ void flush_buckets(const uint32_t (&h)[NB], uint32_t 
 // in a bucket floor(log2(max candidates of its particles)) + 1 and counts the
 // buckets; k_scatter_order writes the warps bucket by bucket, heaviest bucket
 // first (the order inside a bucket is immaterial). k_warp_work also keeps
-// each slot's candidate count (the density dedupe's tasks and statistics).
+// each slot's candidate count (the density dedupe's tasks and statistics) and
+// sets the positions' small-coordinate flag.
 constexpr int ORDER_BUCKETS = 33;
+static_assert(ORDER_HIST_WORDS == 2 * ORDER_BUCKETS + 1 + SMALL_LEVEL_FLAGS, "order_hist layout");
 __global__ void __launch_bounds__(256)
     k_warp_work(SceneView v, const float4 *__restrict__ s_pos,
                 const uint32_t *__restrict__ begin, uint8_t *__restrict__ warp_bucket,
-                uint32_t *__restrict__ hist, uint32_t *__restrict__ cand) {
+                uint32_t *__restrict__ hist, uint32_t *__restrict__ cand,
+                uint32_t *__restrict__ small_flag) {
   __shared__ uint32_t h[ORDER_BUCKETS];
   if (threadIdx.x < unsigned(ORDER_BUCKETS)) h[threadIdx.x] = 0u;
   __syncthreads();
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t total = 0u;
   const bool active = s < v.b->n_sorted;
+  bool small = false;
   if (active) {
     const DevUniforms *U = v.u + v.scene_of_slot[s];
+    const float4 p = s_pos[s];
+    small = small_coord(p.x) || small_coord(p.y) || small_coord(p.z);
     Runs R;
-    neighbor_runs(xyz(s_pos[s]), U->grid, begin + U->c_offset, R);
+    neighbor_runs(xyz(p), U->grid, begin + U->c_offset, R);
     total = R.total;
     cand[s] = total;
   }
+  if (__any_sync(0xffffffffu, small) && (threadIdx.x & 31u) == 0u) atomicOr(small_flag, 1u);
   const uint32_t m = __reduce_max_sync(0xffffffffu, total);
   if ((threadIdx.x & 31u) == 0u && active) {
     const uint32_t b = 32u - uint32_t(__clz(m));
@@ -1056,17 +1133,23 @@ __global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
                     const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
-                    const uint32_t *__restrict__ mask_off, float4 *__restrict__ anp,
-                    float4 *__restrict__ pred_xp, float *__restrict__ pred_rho,
-                    float *__restrict__ pterm0) {
+                    const uint32_t *__restrict__ mask_off,
+                    const uint32_t *__restrict__ small_flag, uint32_t *__restrict__ small_xp,
+                    float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
+                    float *__restrict__ pred_rho, float *__restrict__ pterm0) {
   for_warp_tasks(q, [&](uint32_t s) {
     force_predict_one(s, v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm, vel_x, begin, dir_tab,
-                      dir_half, mask_words, mask_off, anp, pred_xp, pred_rho, pterm0);
+                      dir_half, mask_words, mask_off, small_flag, small_xp, anp, pred_xp,
+                      pred_rho, pterm0);
   });
 }
 
+// The batched forms (B >= 8) are bounded to four blocks per SM (up to 128
+// registers): left to itself the compiler spilled their record buffers once
+// the pressure walk came in two forms. The others keep the compiler's choice
+// (a minimum of 0 blocks leaves the bound unset).
 template <bool HAS_PRESSURE, bool LAST, bool RECORD, int B>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, B >= 8 ? 4 : 0)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
@@ -1074,11 +1157,12 @@ __global__ void __launch_bounds__(128)
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
-            uint32_t *__restrict__ hit_out, bool hit_or) {
+            uint32_t *__restrict__ hit_out, bool hit_or, const uint32_t *__restrict__ small_in,
+            uint32_t *__restrict__ small_out) {
   for_warp_tasks(q, [&](uint32_t s) {
     solve_one<HAS_PRESSURE, LAST, RECORD, B>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
                                           rho_out, pterm_out, v_out, stats, ap_out, mask_off,
-                                          hit_out, hit_or);
+                                          hit_out, hit_or, small_in, small_out);
   });
 }
 
@@ -1352,6 +1436,12 @@ cudaError_t launch_dir_table(const DevState &d, cudaStream_t st) {
 
 namespace {
 // Persistent grid: as many resident blocks as the kernel's occupancy allows.
+// the small-coordinate flags in order_hist (see flag_small_coords)
+uint32_t *position_small_flag(const DevState &d) { return d.order_hist + 2 * ORDER_BUCKETS; }
+uint32_t *level_small_flag(const DevState &d, int level) {
+  return d.order_hist + 2 * ORDER_BUCKETS + 1 + std::min(level, SMALL_LEVEL_FLAGS - 1);
+}
+
 template <class K>
 unsigned persistent_blocks(K kernel, int sm_count, int threads = 128) {
   int per_sm = 0;
@@ -1381,10 +1471,11 @@ cudaError_t order_by_keys(const DevState &d, uint32_t n, uint32_t *perm, cudaStr
 
 cudaError_t launch_order_warps(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(d.order_hist, 0, sizeof(uint32_t) * 2 * ORDER_BUCKETS, st);
+  cudaError_t e = cudaMemsetAsync(d.order_hist, 0, sizeof(uint32_t) * ORDER_HIST_WORDS, st);
   if (e != cudaSuccess) return e;
   k_warp_work<<<blocks_for(n, 256), 256, 0, st>>>(d.view(), d.s_pos, d.cell_begin, d.warp_bucket,
-                                                  d.order_hist, d.dens_cand);
+                                                  d.order_hist, d.dens_cand,
+                                                  position_small_flag(d));
   const uint32_t nwarps = (n + 31u) / 32u;
   k_scatter_order<<<blocks_for(nwarps, 256), 256, 0, st>>>(d.view(), d.warp_bucket, d.order_hist,
                                                            d.order_hist + ORDER_BUCKETS,
@@ -1493,7 +1584,9 @@ cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st)
   k_force_predict<<<blocks, kForceThreads, 0, st>>>(q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm,
                                           d.s_dens, d.s_nrm, d.vel_x,
                                           d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
-                                          d.mask_off, d.anp, xp_out, rho_out, d.pterm[0]);
+                                          d.mask_off, position_small_flag(d),
+                                          level_small_flag(d, 0), d.anp, xp_out, rho_out,
+                                          d.pterm[0]);
   return cudaGetLastError();
 }
 
@@ -1507,6 +1600,8 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
   uint32_t *hit_out = d.rec_hits;
   const bool hit_or = iter > 0;
+  const uint32_t *small_in = level_small_flag(d, iter);
+  uint32_t *small_out = level_small_flag(d, iter + 1);
   TaskQueue q;
   cudaError_t e = prepare_queue(d, d.warp_order, false, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
@@ -1517,7 +1612,8 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     k_solve<P_, L_, R_, B_><<<blocks, 128, 0, st>>>(Q_, d.view(), d.s_pos, d.vel_x, d.anp,     \
                                                     d.cell_begin, xp_in, d.pterm[in], xp_out, \
                                                     rho_out, d.pterm[out], d.pred_v, d.stats, \
-                                                    ap_out, d.mask_off, hit_out, hit_or);     \
+                                                    ap_out, d.mask_off, hit_out, hit_or,      \
+                                                    small_in, small_out);                     \
   } while (0)
 #define FS_SOLVE(P_, L_, R_)                                       \
   do {                                                             \

@@ -205,6 +205,34 @@ def test_xsph_off_and_outside_particles(fslib, oracle_mod, sc):
     _compare(sim, orc, scene.n, "xsph off / outside")
 
 
+def test_small_coordinates(fslib, oracle_mod, sc):
+    """Positions with a coordinate 0 < |c| < 2^-34 switch the force pass to
+    its checked direction numerators for that step, and pairs whose
+    coordinate difference is below 2^-60 take the IEEE operations: a group of
+    particles on the x = 0 and z = 0 planes and at tiny offsets from them
+    (1e-30 .. 1e-12, both signs), within h of each other, then the same
+    scene's later steps (the offsets grow out of the range)."""
+    scene = sc.small_scene(seed=4)
+    p = scene.particles
+    n = scene.n
+    rng = np.random.default_rng(3)
+    centre = p[n // 2, 0:3].copy()
+    tiny = np.array([0.0, 1e-30, -1e-30, 3e-25, -7e-20, 1e-19, -2e-18, 5e-15, 1e-12, -1e-12],
+                    np.float32)
+    k = 0
+    for i in range(n // 2 - 40, n // 2 + 40, 2):
+        p[i, 0] = tiny[k % len(tiny)]
+        p[i, 2] = tiny[(k * 3 + 1) % len(tiny)]
+        p[i, 1] = centre[1] + np.float32(0.01) * np.float32(rng.uniform(-1, 1))
+        k += 1
+    sim, orc = _run_pair(scene, 1, oracle_mod)
+    _compare(sim, orc, n, "small coordinates step 1")
+    for _ in range(4):
+        sim.step(1)
+        orc.step(1)
+    _compare(sim, orc, n, "small coordinates step 5")
+
+
 def test_empty_and_spawn(fslib, oracle_mod, sc):
     from fluidsph.sim import SphSimulation3DGrid
     scene = sc.make_scene("empty", np.zeros((0, 16), np.float32), (1, 1, 1))
