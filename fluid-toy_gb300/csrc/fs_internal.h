@@ -20,10 +20,9 @@ constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
 constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16, 32};
 
 // Work-order scratch words (DevState::order_hist), zeroed each step: the
-// bucket counts and cursors of the 33 work buckets, the small-coordinate
-// flag of the positions, and one per PCISPH level of predicted positions.
-constexpr int SMALL_LEVEL_FLAGS = 64;
-constexpr int ORDER_HIST_WORDS = 2 * 33 + 1 + SMALL_LEVEL_FLAGS;
+// bucket counts and cursors of the 33 work buckets, then the positions'
+// small-coordinate flag.
+constexpr int ORDER_HIST_WORDS = 2 * 33 + 1;
 
 // The neighbour passes' load-depth choice of a simulation (indices into the
 // lists above).
@@ -139,8 +138,7 @@ struct DevState {
   uint32_t *warp_order;            // [M / 32] warp ids
   uint8_t *warp_bucket;            // [M / 32] work bucket of each warp
   uint32_t *order_hist;            // [ORDER_HIST_WORDS] bucket counts, bucket cursors,
-                                   // then the step's small-coordinate flags: positions,
-                                   // then each PCISPH level's predicted positions
+                                   // then the step's small-coordinate flag
   uint32_t *perm_hit;              // [M] sorted slots by decreasing hit count
   uint16_t *work_key;              // [M] hit-count bucket of each sorted slot
   uint32_t *key_hist;              // [3 * KEY_BUCKETS]: counts, bases, cursors

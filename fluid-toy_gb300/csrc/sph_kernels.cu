@@ -406,18 +406,11 @@ __device__ __forceinline__ void xsph_one(uint32_t s, SceneView v,
 // A position coordinate c with 0 < |c| < 2^-34. When no particle has one,
 // every nonzero coordinate difference of two particles is >= 2^-57 in
 // magnitude (both coordinates are zero or multiples of 2^-57, or they have
-// opposite signs), so the passes that divide those differences by r skip
-// their per-pair lower-bound checks. k_warp_work flags the positions each
-// step; the producer of each PCISPH level of predicted positions (force +
-// predict for level 0, solve iteration k for level k + 1) flags that level
-// (levels from SMALL_LEVEL_FLAGS - 1 on share the last word, which only
-// makes their readers check more).
+// opposite signs), so the force pass, which divides those differences by r,
+// skips their per-pair lower-bound checks. k_warp_work sets the step's flag.
 __device__ __forceinline__ bool small_coord(float c) {
   const float a = fabsf(c);
   return a < 0x1p-34f && a != 0.0f;
-}
-__device__ __forceinline__ void flag_small_coords(float3 x, uint32_t *flag) {
-  if (small_coord(x.x) || small_coord(x.y) || small_coord(x.z)) atomicOr(flag, 1u);
 }
 
 // ---- force + PCISPH predict ---------------------------------------------------
@@ -434,9 +427,9 @@ __device__ __forceinline__ void force_predict_one(
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
                     const uint32_t *__restrict__ mask_off,
-                    const uint32_t *__restrict__ small_flag, uint32_t *__restrict__ small_xp,
-                    float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
-                    float *__restrict__ pred_rho, float *__restrict__ pterm0) {
+                    const uint32_t *__restrict__ small_flag, float4 *__restrict__ anp,
+                    float4 *__restrict__ pred_xp, float *__restrict__ pred_rho,
+                    float *__restrict__ pterm0) {
   if (s >= v.b->n_sorted) return;
   const DevUniforms *U = v.u + v.scene_of_slot[s];
   const GpuSphParams3D &P = U->sph;
@@ -514,7 +507,10 @@ __device__ __forceinline__ void force_predict_one(
     const float dvx = -r_vec.x, dvy = -r_vec.y, dvz = -r_vec.z;
     float3 dir;
     if constexpr (FAST) {
-      dir = f3(markstein(dvx, rr, y_rr), markstein(dvy, rr, y_rr), markstein(dvz, rr, y_rr));
+      // (markstein_nz: every quotient of the pair only scales terms of the
+      // three sums a_p, a_v, a_c, which start at +0)
+      dir = f3(markstein_nz(dvx, rr, y_rr), markstein_nz(dvy, rr, y_rr),
+               markstein_nz(dvz, rr, y_rr));
       // the components' magnitudes are below r < 2^30; without DV_CHECK no
       // position has a coordinate 0 < |c| < 2^-34, so they are also 0 or
       // >= 2^-57
@@ -533,7 +529,7 @@ __device__ __forceinline__ void force_predict_one(
         dir = xyz(__ldg(dir_tab + (d + dir_half)));
       else
         dir = fallback_dir_eval(float(s - U->s_offset) - float(j - U->s_offset));
-      const float q_sep = FAST ? markstein(rr, min_dist, y_min_dist) : rr / min_dist;
+      const float q_sep = FAST ? markstein_nz(rr, min_dist, y_min_dist) : rr / min_dist;
       const float sep = 200.0f * (1.0f - q_sep);
       t.sep = (-sep) * dir;
     }
@@ -555,11 +551,11 @@ __device__ __forceinline__ void force_predict_one(
       // 1 / avg_density is 2 / dsum: with y = RN(1 / dsum), 2 y = RN(1 / avg_density)
       // exactly (dsum in [2, 2^60): the halving and doubling are exact)
       const float y_sum = rcp_fast(dsum);
-      np_q = markstein(np_num, np_den, rcp_fast(np_den));
-      mu = markstein(mu_num, mu_den, rcp_fast(mu_den));
+      np_q = markstein_nz(np_num, np_den, rcp_fast(np_den));
+      mu = markstein_nz(mu_num, mu_den, rcp_fast(mu_den));
       const float pi_num = -visc * mu;
-      pi_visc = markstein(pi_num, avg_density, 2.0f * y_sum);
-      K_ij = markstein(two_rho0, dsum, y_sum);
+      pi_visc = markstein_nz(pi_num, avg_density, 2.0f * y_sum);
+      K_ij = markstein_nz(two_rho0, dsum, y_sum);
       ok = ok && fast_num_ok(np_num) && np_den < 0x1p60f && fast_num_ok(mu_num) &&
            fast_num_ok(pi_num) && dsum < 0x1p60f;
     } else {
@@ -646,7 +642,6 @@ __device__ __forceinline__ void force_predict_one(
   const float3 v_star = vel_i + dt * a;
   const float3 x_star = pos_i + dt * v_star;
   pred_xp[s] = make_float4(x_star.x, x_star.y, x_star.z, 0.0f);
-  flag_small_coords(x_star, small_xp);
   pred_rho[s] = 0.0f;
   pterm0[s] = 0.0f;  // iteration 0's pressure terms (see launch_solve)
 }
@@ -675,8 +670,7 @@ __device__ __forceinline__ void solve_one(
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
-            uint32_t *__restrict__ hit_out, bool hit_or, const uint32_t *__restrict__ small_in,
-            uint32_t *__restrict__ small_out) {
+            uint32_t *__restrict__ hit_out, bool hit_or) {
   const bool active = s < v.b->n_sorted;
   const DevUniforms *U = v.u + (active ? v.scene_of_slot[s] : 0u);
   const GpuSphParams3D &P = U->sph;
@@ -701,23 +695,21 @@ __device__ __forceinline__ void solve_one(
     // iteration (read only when there is pressure)
     const float self_term = HAS_PRESSURE ? pterm_in[s] : 0.0f;
     const bool fast_h2 = h2 < 0x1p59f;
-    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq, auto dv_check) {
+    auto pressure = [&](uint32_t j, float3 r_vec, float r_sq) {
       const float pt = __ldg(pterm_in + j);  // np / (nd * nd)
       const float3 nr = -r_vec;
       // correctly rounded fast square root, reciprocal and quotients, one
       // range check for the pair (IEEE operations outside it). The pair is a
       // hit, 1e-12 < r^2 < h^2, so with h^2 < 2^59 r^2 and r are in the
-      // validated range and |nr| < r; the numerators' lower bound is checked
-      // per pair unless no predicted position of this level has a coordinate
-      // 0 < |c| < 2^-34 (then every nonzero component is >= 2^-57).
+      // validated range and |nr| < r: only the numerators' lower bound is
+      // checked per pair.
       float rr = sqrt_fast(r_sq);
       const float y_rr = rcp_fast(rr);
-      float3 dir = f3(markstein(nr.x, rr, y_rr), markstein(nr.y, rr, y_rr),
-                      markstein(nr.z, rr, y_rr));
-      bool ok = fast_h2;
-      if constexpr (decltype(dv_check)::value)
-        ok = ok && fast_num_lo_ok(nr.x) && fast_num_lo_ok(nr.y) && fast_num_lo_ok(nr.z);
-      if (!ok) {
+      // (markstein_nz: the direction only scales terms of a_p, which starts
+      // at +0)
+      float3 dir = f3(markstein_nz(nr.x, rr, y_rr), markstein_nz(nr.y, rr, y_rr),
+                      markstein_nz(nr.z, rr, y_rr));
+      if (!(fast_h2 && fast_num_lo_ok(nr.x) && fast_num_lo_ok(nr.y) && fast_num_lo_ok(nr.z))) {
         rr = sqrtf(r_sq);
         dir = f3(nr.x / rr, nr.y / rr, nr.z / rr);
       }
@@ -733,7 +725,6 @@ __device__ __forceinline__ void solve_one(
     // candidates in chunks of up to 32: the predicted density is summed while
     // testing; the pressure hits of the chunk go to a per-lane bitmask that
     // each lane then walks (its own hits only, ascending)
-    auto run = [&](auto dv_check) {
     uint32_t widx = 0u;
     for (int r = 0; r < R.count; r++) {
       for (uint32_t base = R.lo[r]; base < R.hi[r]; base += 32u) {
@@ -762,16 +753,11 @@ __device__ __forceinline__ void solve_one(
             chunk &= chunk - 1u;
             const float4 nb = __ldg(xp_in + j);
             const float3 r_vec = pred_pos - xyz(nb);
-            pressure(j, r_vec, dot3(r_vec, r_vec), dv_check);
+            pressure(j, r_vec, dot3(r_vec, r_vec));
           }
         }
       }
     }
-    };
-    if (HAS_PRESSURE && __ldg(small_in) == 0u)
-      run(std::false_type{});
-    else
-      run(std::true_type{});
     const float density_error = fmaxf(0.0f, pred_density - P.rest_density);
     const float new_p = old_p + P.pcisph_delta * density_error;
     const float dt = P.dt;
@@ -787,7 +773,6 @@ __device__ __forceinline__ void solve_one(
     } else {
       const float3 x_star = pos_i + dt * v_star;
       xp_out[s] = make_float4(x_star.x, x_star.y, x_star.z, new_p);
-      flag_small_coords(x_star, small_out);
       rho_out[s] = pred_density;
       const float nd = fmaxf(pred_density, 1.0f);
       pterm_out[s] = new_p / (nd * nd);
@@ -853,7 +838,7 @@ __device__ __forceinline__ void flush_buckets(const uint32_t (&h)[NB], uint32_t 
 // each slot's candidate count (the density dedupe's tasks and statistics) and
 // sets the positions' small-coordinate flag.
 constexpr int ORDER_BUCKETS = 33;
-static_assert(ORDER_HIST_WORDS == 2 * ORDER_BUCKETS + 1 + SMALL_LEVEL_FLAGS, "order_hist layout");
+static_assert(ORDER_HIST_WORDS == 2 * ORDER_BUCKETS + 1, "order_hist layout");
 __global__ void __launch_bounds__(256)
     k_warp_work(SceneView v, const float4 *__restrict__ s_pos,
                 const uint32_t *__restrict__ begin, uint8_t *__restrict__ warp_bucket,
@@ -1134,22 +1119,17 @@ __global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
                     const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
                     int dir_half, const uint32_t *__restrict__ mask_words,
                     const uint32_t *__restrict__ mask_off,
-                    const uint32_t *__restrict__ small_flag, uint32_t *__restrict__ small_xp,
-                    float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
-                    float *__restrict__ pred_rho, float *__restrict__ pterm0) {
+                    const uint32_t *__restrict__ small_flag, float4 *__restrict__ anp,
+                    float4 *__restrict__ pred_xp, float *__restrict__ pred_rho,
+                    float *__restrict__ pterm0) {
   for_warp_tasks(q, [&](uint32_t s) {
     force_predict_one(s, v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm, vel_x, begin, dir_tab,
-                      dir_half, mask_words, mask_off, small_flag, small_xp, anp, pred_xp,
-                      pred_rho, pterm0);
+                      dir_half, mask_words, mask_off, small_flag, anp, pred_xp, pred_rho, pterm0);
   });
 }
 
-// The batched forms (B >= 8) are bounded to four blocks per SM (up to 128
-// registers): left to itself the compiler spilled their record buffers once
-// the pressure walk came in two forms. The others keep the compiler's choice
-// (a minimum of 0 blocks leaves the bound unset).
 template <bool HAS_PRESSURE, bool LAST, bool RECORD, int B>
-__global__ void __launch_bounds__(128, B >= 8 ? 4 : 0)
+__global__ void __launch_bounds__(128)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
@@ -1157,12 +1137,11 @@ __global__ void __launch_bounds__(128, B >= 8 ? 4 : 0)
             float *__restrict__ rho_out, float *__restrict__ pterm_out,
             float4 *__restrict__ v_out, unsigned long long *__restrict__ stats,
             float4 *__restrict__ ap_out, const uint32_t *__restrict__ mask_off,
-            uint32_t *__restrict__ hit_out, bool hit_or, const uint32_t *__restrict__ small_in,
-            uint32_t *__restrict__ small_out) {
+            uint32_t *__restrict__ hit_out, bool hit_or) {
   for_warp_tasks(q, [&](uint32_t s) {
     solve_one<HAS_PRESSURE, LAST, RECORD, B>(s, v, s_pos, vel_x, anp, begin, xp_in, pterm_in, xp_out,
                                           rho_out, pterm_out, v_out, stats, ap_out, mask_off,
-                                          hit_out, hit_or, small_in, small_out);
+                                          hit_out, hit_or);
   });
 }
 
@@ -1436,11 +1415,8 @@ cudaError_t launch_dir_table(const DevState &d, cudaStream_t st) {
 
 namespace {
 // Persistent grid: as many resident blocks as the kernel's occupancy allows.
-// the small-coordinate flags in order_hist (see flag_small_coords)
+// the positions' small-coordinate flag in order_hist (see small_coord)
 uint32_t *position_small_flag(const DevState &d) { return d.order_hist + 2 * ORDER_BUCKETS; }
-uint32_t *level_small_flag(const DevState &d, int level) {
-  return d.order_hist + 2 * ORDER_BUCKETS + 1 + std::min(level, SMALL_LEVEL_FLAGS - 1);
-}
 
 template <class K>
 unsigned persistent_blocks(K kernel, int sm_count, int threads = 128) {
@@ -1584,9 +1560,8 @@ cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st)
   k_force_predict<<<blocks, kForceThreads, 0, st>>>(q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm,
                                           d.s_dens, d.s_nrm, d.vel_x,
                                           d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
-                                          d.mask_off, position_small_flag(d),
-                                          level_small_flag(d, 0), d.anp, xp_out, rho_out,
-                                          d.pterm[0]);
+                                          d.mask_off, position_small_flag(d), d.anp, xp_out,
+                                          rho_out, d.pterm[0]);
   return cudaGetLastError();
 }
 
@@ -1600,8 +1575,6 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
   float4 *ap_out = d.rec_ap ? d.rec_ap[iter] : nullptr;
   uint32_t *hit_out = d.rec_hits;
   const bool hit_or = iter > 0;
-  const uint32_t *small_in = level_small_flag(d, iter);
-  uint32_t *small_out = level_small_flag(d, iter + 1);
   TaskQueue q;
   cudaError_t e = prepare_queue(d, d.warp_order, false, n, 2 + (iter % (TASK_COUNTERS - 3)), st, &q);
   if (e != cudaSuccess) return e;
@@ -1612,8 +1585,7 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
     k_solve<P_, L_, R_, B_><<<blocks, 128, 0, st>>>(Q_, d.view(), d.s_pos, d.vel_x, d.anp,     \
                                                     d.cell_begin, xp_in, d.pterm[in], xp_out, \
                                                     rho_out, d.pterm[out], d.pred_v, d.stats, \
-                                                    ap_out, d.mask_off, hit_out, hit_or,      \
-                                                    small_in, small_out);                     \
+                                                    ap_out, d.mask_off, hit_out, hit_or);     \
   } while (0)
 #define FS_SOLVE(P_, L_, R_)                                       \
   do {                                                             \
