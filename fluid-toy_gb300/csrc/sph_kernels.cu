@@ -38,12 +38,11 @@ namespace {
 // ms against the plain loop; on the 256-scene ensemble the plain loop was
 // faster), so the simulation measures them (DevState::load_*, chosen per
 // particle-count bucket by fs_step's tuner). Every depth gives the same bits.
-// With a batched depth, PCISPH iteration 0 runs on the pressure-carrying
-// kernel with every pressure term 0 (written by the predict pass): its terms
-// add +-0 to +0, so the results are the same bits as skipping them, and that
-// kernel keeps its candidate loads batched where the short pressure-free one
-// does not (solve 5.30 -> 4.84 ms on the 1M-particle dam break). The plain
-// loop keeps the pressure-free kernel for iteration 0.
+// PCISPH iteration 0 runs on the pressure-free kernel at every depth (its
+// pressures are all 0, the skipped sum is +0 exactly); its batched forms are
+// bounded to four blocks per SM, without which the compiler serialised their
+// loads (solve 4.78 -> 4.65 ms on the 1M-particle dam break against running
+// iteration 0 on the pressure kernel with zero terms).
 constexpr int kLoadDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
 constexpr int kXsphDepths[kNumLoadDepths] = {1, 4, 8, 16, 32};
 static_assert(kLoadDepths[3] == int(kDensityDepths[3]) && kXsphDepths[0] == int(kXsphDepthList[0]),
@@ -1128,8 +1127,12 @@ __global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
   });
 }
 
+// The pressure-free batched forms (iteration 0) are bounded to four blocks
+// per SM (up to 128 registers): left to itself the compiler gave them fewer
+// registers than their record buffers need and serialised the loads. A
+// minimum of 0 blocks leaves the bound unset.
 template <bool HAS_PRESSURE, bool LAST, bool RECORD, int B>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, (!HAS_PRESSURE && B > 1) ? 4 : 0)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
             const float4 *__restrict__ vel_x, const float4 *__restrict__ anp,
             const uint32_t *__restrict__ begin, const float4 *__restrict__ xp_in,
@@ -1596,32 +1599,18 @@ cudaError_t launch_solve(const DevState &d, uint32_t n, int iter, int last, cuda
       default: FS_SOLVE_B(P_, L_, R_, kLoadDepths[0], q); break;   \
     }                                                              \
   } while (0)
-  // the pressure-free iteration-0 kernel only with the plain loop (see
-  // kLoadDepths); a batched depth runs iteration 0 on the pressure kernel
-#define FS_SOLVE0(L_, R_)                                          \
-  do {                                                             \
-    FS_SOLVE_B(false, L_, R_, kLoadDepths[0], q);                  \
-  } while (0)
 #define FS_SOLVE_R(P_, L_)            \
   do {                                \
     if (hit_out) FS_SOLVE(P_, L_, true); \
     else FS_SOLVE(P_, L_, false);     \
   } while (0)
-#define FS_SOLVE0_R(L_)                \
-  do {                                 \
-    if (hit_out) FS_SOLVE0(L_, true);  \
-    else FS_SOLVE0(L_, false);         \
-  } while (0)
-  const bool batched = kLoadDepths[d.load_solve < kPlainCandidates ? d.load_solve : 0] > 1;
-  if (iter == 0 && last && batched) FS_SOLVE_R(true, true);
-  else if (iter == 0 && last) FS_SOLVE0_R(true);
-  else if (iter == 0 && batched) FS_SOLVE_R(true, false);
-  else if (iter == 0) FS_SOLVE0_R(false);
+  // iteration 0 reads the predict output, where every pressure is 0: the
+  // pressure-free kernel
+  if (iter == 0 && last) FS_SOLVE_R(false, true);
+  else if (iter == 0) FS_SOLVE_R(false, false);
   else if (last) FS_SOLVE_R(true, true);
   else FS_SOLVE_R(true, false);
-#undef FS_SOLVE0_R
 #undef FS_SOLVE_R
-#undef FS_SOLVE0
 #undef FS_SOLVE
 #undef FS_SOLVE_B
   return cudaGetLastError();
