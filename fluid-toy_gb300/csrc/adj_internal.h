@@ -35,7 +35,15 @@ struct AdjView {
   float4 *gn;     // d/d Akinci normal
   float2 *grho;   // d/d density (raw, after the XSPH reverse), d/d near density
   float *gp;      // d/d pressure carried between PCISPH levels
-  float4 *gu[2];  // per level: d/d pressure acceleration (pre-clamp), d/d next density
+  // per level, two float4 per particle (ping-pong between levels): the
+  // level's (x*, p / max(rho*, 1)^2), then (d/d pressure acceleration
+  // (pre-clamp), d/d next density); a neighbour's pair of records is one
+  // 32-byte load site in the level's reverse
+  float4 *lv[2];
+  // [5 N]: each particle's inputs to the force reverse (x, max(rho, 1);
+  // vhat, max(rho_near, 1); v; n; d/d non-pressure acceleration), written by
+  // level 0's reverse so that a neighbour is one 80-byte load site
+  float4 *frec;
   double *gparam; // [scenes][3]: viscosity, stiffness, surface_tension (FP64)
   double *gparam2;  // [scenes][2]: near_stiffness, pcisph_delta (FP64)
   double2 *gpart; // [N] canonical: each particle's share of d/d (viscosity, surface tension)

@@ -144,6 +144,16 @@ __device__ __forceinline__ void flag_outside(uint32_t *err, bool inside) {
   if (!inside) atomicOr(err, ERR_ADJ_OUTSIDE_GRID);
 }
 
+// Level k's record of particle s (see AdjView::lv): its predicted position,
+// p / max(rho*, 1)^2 and the cotangents u, rhat.
+__device__ __forceinline__ void put_level_record(float4 *lv, uint32_t s, const TapeView &t, int k,
+                                                 float3 u, float rhat) {
+  const float4 x = t.xp[k][s];
+  const float rt = fmaxf(t.rho[k][s], 1.0f);
+  lv[2 * size_t(s)] = make_float4(x.x, x.y, x.z, x.w / (rt * rt));
+  lv[2 * size_t(s) + 1] = f4(u, rhat);
+}
+
 // ---- integrate + finalize --------------------------------------------------------
 __global__ void __launch_bounds__(128)
     k_adj_integrate(SceneView v, TapeView t, AdjView a, const float4 *__restrict__ xbar_in,
@@ -221,7 +231,7 @@ __global__ void __launch_bounds__(128)
   a.gx[s] = f4(xb, 0.f);
   a.gvhat[s] = f4(vfb, 0.f);
   a.ga[s] = f4(dt * vfb, 0.f);
-  a.gu[(K - 1) & 1][s] = f4(apb, 0.f);
+  put_level_record(a.lv[(K - 1) & 1], s, t, K - 1, apb, 0.f);
   a.gp[s] = 0.f;
   a.gv[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   a.grho[s] = make_float2(0.f, 0.f);
@@ -230,15 +240,17 @@ __global__ void __launch_bounds__(128)
 
 // ---- one PCISPH iteration (level k) ------------------------------------------------
 // Level k's recorded arrays come as arguments (xpk = x*^k with p^k, rhok =
-// rho*^k, ap_prev = iteration k-1's pressure acceleration before the clamp).
+// rho*^k, ap_prev = iteration k-1's pressure acceleration before the clamp);
+// lv_in holds level k's records (AdjView::lv), from which the neighbours'
+// values are read, and lv_out receives level k-1's.
 template <int L>
 __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const SceneView &v,
                                               const TapeView &t, const AdjView &a,
                                               const float4 *__restrict__ xpk,
                                               const float *__restrict__ rhok,
                                               const float4 *__restrict__ ap_prev,
-                                              const float4 *__restrict__ gu_in,
-                                              float4 *__restrict__ gu_out, int k, int K) {
+                                              const float4 *__restrict__ lv_in,
+                                              float4 *__restrict__ lv_out, int k, int K) {
   const bool active = q < v.b->n_sorted;
   const uint32_t qq = active ? q : 0u;
   const DevUniforms *U = v.u + t.scene_of_slot[qq];
@@ -255,7 +267,7 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
     const float scale_g = 45.0f / (PI_F * P.kernel_radius_pow6);
     const float3 xq = f3of(xq4);
     const float cq = pq / (rt_q * rt_q);
-    const float4 uq4 = gu_in[q];
+    const float4 uq4 = lv_in[2 * size_t(q) + 1];
     const float3 uq = f3of(uq4);
     const float rhat_q = uq4.w;
     const bool has_rho = k < K - 1;  // level K's density and pressure are unused
@@ -269,15 +281,15 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
     for_hits_sub<L>(
         R, t, q, sub,
         [&](uint32_t j) {
-          const float3 r = xq - f3of(__ldg(xpk + j));
+          const float3 r = xq - f3of(__ldg(lv_in + 2 * size_t(j)));
           return dot3(r, r) < h2;
         },
         [&](uint32_t j) {
-          const float4 xj4 = __ldg(xpk + j);
+          const float4 xj4 = __ldg(lv_in + 2 * size_t(j));  // x*_j, c_j
           const float3 r = xq - f3of(xj4);
           const float r2 = dot3(r, r);
           const bool in = r2 < h2;
-          const float4 uj4 = __ldg(gu_in + j);
+          const float4 uj4 = __ldg(lv_in + 2 * size_t(j) + 1);
           if (has_rho) {
             const float diff = h2 - r2;
             xsb = in ? mad3(xsb, c_rho * diff * diff * (rhat_q + uj4.w), r) : xsb;
@@ -285,8 +297,7 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
           if (has_p) {
             // evaluated for every hit, kept for 1e-12 < r^2 < h^2
             const bool ns = in && r2 > MIN_R2;
-            const float rt_j = fmaxf(__ldg(rhok + j), 1.0f);
-            const float cij = cq + xj4.w / (rt_j * rt_j);
+            const float cij = cq + xj4.w;
             const float rr = sqrtf(ns ? r2 : 1.0f);
             const float inv_rr = 1.0f / rr;
             const float3 e = r * inv_rr;
@@ -318,23 +329,34 @@ __device__ __forceinline__ void adj_solve_one(uint32_t q, uint32_t sub, const Sc
     const float max_accel = 0.25f * h / (dt * dt);
     const float3 apb = clamp_adjoint(f3of(ap_prev[q]), dt * vstar_b, max_accel);
     const float rhat = rb + (rho_q > P.rest_density ? P.pcisph_delta * p_bar : 0.0f);
-    gu_out[q] = f4(apb, rhat);
+    put_level_record(lv_out, q, t, k - 1, apb, rhat);
     a.gp[q] = p_bar;
     // p^k = p^(k-1) + delta max(0, rho*^k - rho0): the particle's share of
     // d/d delta at this level (pcisph_solve.wgsl's density_error)
     const float density_error = fmaxf(0.0f, rho_q - P.rest_density);
     a.gpart2[t.s2o[q]].y += double(p_bar) * double(density_error);
   }
-  // k == 0: predict, x*^0 = x + dt v*^0, v*^0 = vhat + dt a (done above)
+  // k == 0: predict, x*^0 = x + dt v*^0, v*^0 = vhat + dt a (done above);
+  // the non-pressure acceleration's cotangent is final: the force reverse's
+  // record of q
+  if (k == 0) {
+    const float2 d = t.dens[q];
+    float4 *fr = a.frec + 5 * size_t(q);
+    fr[0] = f4(f3of(t.pos[q]), fmaxf(d.x, 1.0f));
+    fr[1] = f4(f3of(t.vhat[q]), fmaxf(d.y, 1.0f));
+    fr[2] = t.vel[q];
+    fr[3] = t.nrm[q];
+    fr[4] = a.ga[q];
+  }
 }
 
 template <int L>
 __global__ void __launch_bounds__(128)
     k_adj_solve(TaskQueue tq, SceneView v, TapeView t, AdjView a, const float4 *__restrict__ xpk,
                 const float *__restrict__ rhok, const float4 *__restrict__ ap_prev,
-                const float4 *__restrict__ gu_in, float4 *__restrict__ gu_out, int k, int K) {
+                const float4 *__restrict__ lv_in, float4 *__restrict__ lv_out, int k, int K) {
   for_warp_tasks_sub<L>(tq, [&](uint32_t q, uint32_t sub) {
-    adj_solve_one<L>(q, sub, v, t, a, xpk, rhok, ap_prev, gu_in, gu_out, k, K);
+    adj_solve_one<L>(q, sub, v, t, a, xpk, rhok, ap_prev, lv_in, lv_out, k, K);
   });
 }
 
@@ -484,17 +506,22 @@ __device__ __forceinline__ float3 close_dir(const float4 *dir_tab, int dir_half,
   return fallback_dir_eval(float(si - s_off) - float(sj - s_off));
 }
 
-__device__ __forceinline__ ForceSide force_side(const TapeView &t, uint32_t i, float3 x) {
+// Particle i's side from its record (AdjView::frec); rho > 1 exactly when
+// max(rho, 1) > 1. w receives its cotangent of the non-pressure acceleration.
+__device__ __forceinline__ ForceSide force_side(const float4 *frec, uint32_t i, float3 &w) {
+  const float4 *fr = frec + 5 * size_t(i);
+  const float4 r0 = __ldg(fr), r1 = __ldg(fr + 1), r2 = __ldg(fr + 2), r3 = __ldg(fr + 3),
+               r4 = __ldg(fr + 4);
   ForceSide S;
-  S.x = x;
-  S.vhat = f3of(__ldg(t.vhat + i));
-  S.vpre = f3of(__ldg(t.vel + i));
-  S.n = f3of(__ldg(t.nrm + i));
-  const float2 d = __ldg(t.dens + i);
-  S.rb = fmaxf(d.x, 1.0f);
-  S.rnb = fmaxf(d.y, 1.0f);
-  S.m = d.x > 1.0f;
-  S.mn = d.y > 1.0f;
+  S.x = f3of(r0);
+  S.vhat = f3of(r1);
+  S.vpre = f3of(r2);
+  S.n = f3of(r3);
+  S.rb = r0.w;
+  S.rnb = r1.w;
+  S.m = r0.w > 1.0f;
+  S.mn = r1.w > 1.0f;
+  w = f3of(r4);
   return S;
 }
 
@@ -512,8 +539,8 @@ __device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const Sc
     const DevUniforms *U = v.u + scene;
     const ForceConst c = force_const(U->sph);
     const float h2 = U->sph.kernel_radius_sq;
-    const ForceSide Q = force_side(t, q, f3of(t.pos[q]));
-    const float3 wq = f3of(a.ga[q]);
+    float3 wq;
+    const ForceSide Q = force_side(a.frec, q, wq);
     Runs R;
     flag_outside(a.err, runs_checked(Q.x, U->grid, t.cell_begin + U->c_offset, R));
     for_hits_sub<L>(
@@ -524,12 +551,11 @@ __device__ __forceinline__ void adj_force_one(uint32_t q, uint32_t sub, const Sc
           return r2 < h2 && r2 > MIN_R2;
         },
         [&](uint32_t j) {
-          const float3 xj = f3of(__ldg(t.pos + j));
-          const float3 r = Q.x - xj;
+          float3 wj;
+          const ForceSide Jn = force_side(a.frec, j, wj);
+          const float3 r = Q.x - Jn.x;
           const float r2 = dot3(r, r);
-          const ForceSide Jn = force_side(t, j, xj);
           const PairGeom g = pair_geom(r, r2, c);
-          const float3 wj = f3of(__ldg(a.ga + j));
           float3 ec_qj = f3(0.f, 0.f, 0.f), ec_jq = f3(0.f, 0.f, 0.f);
           if (g.close) {
             ec_qj = close_dir(dir_tab, dir_half, q, j, U->s_offset);
@@ -937,8 +963,8 @@ cudaError_t adj_gathers(const SceneView &v, const TapeView &t, const AdjView &a,
   };
   for (int k = K - 1; k >= 0; k--)
     k_adj_solve<L><<<b.solve, 128, 0, st>>>(queue(k), v, t, a, t.xp[k], t.rho[k],
-                                            k >= 1 ? t.ap[k - 1] : nullptr, a.gu[k & 1],
-                                            a.gu[(k + 1) & 1], k, K);
+                                            k >= 1 ? t.ap[k - 1] : nullptr, a.lv[k & 1],
+                                            a.lv[(k + 1) & 1], k, K);
   k_adj_force<L><<<b.force, 128, 0, st>>>(hit_queue(K), v, t, a, dir_tab, dir_half);
   k_adj_xsph<L><<<b.xsph, 128, 0, st>>>(queue(K + 1), v, t, a);
   k_adj_density<L><<<b.density, 128, 0, st>>>(queue(K + 2), v, t, a);

@@ -163,8 +163,9 @@ void carve_work(FsAdj *a, char *base, size_t *bytes) {
   v.gn = c.take<float4>(N);
   v.grho = c.take<float2>(N);
   v.gp = c.take<float>(N);
-  v.gu[0] = c.take<float4>(N);
-  v.gu[1] = c.take<float4>(N);
+  v.lv[0] = c.take<float4>(2 * size_t(N));
+  v.lv[1] = c.take<float4>(2 * size_t(N));
+  v.frec = c.take<float4>(5 * size_t(N));
   v.gparam = c.take<double>(3 * size_t(a->scenes));
   v.gparam2 = c.take<double>(2 * size_t(a->scenes));
   v.gpart = c.take<double2>(N);
