@@ -675,7 +675,11 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, 
     hb = batch([with_(s.sph, **h) for s, h in zip(scenes, hidden)])
     hr = DifferentiableRollout(hb, every)
     hr.forward(steps)
-    targets = [hr.final_splat(grids[k], scenes[k].geom, scene=k) for k in range(len(scenes))]
+    # the targets stay on the device; the losses of all scenes are taken in
+    # one call (one grid build of the final state, one read-back)
+    targets = [torch.from_numpy(hr.final_splat(grids[k], scenes[k].geom, scene=k)).to(dev)
+               for k in range(len(scenes))]
+    geoms = [s.geom for s in scenes]
     hr.close()
     hb.close()
     params = [with_(s.sph) for s in scenes]
@@ -698,8 +702,7 @@ def _identify(scenes, hidden, steps, every, iters, grid_size, dev, timed=False, 
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         r.forward(steps)
-        loss = sum(r.splat_mse_loss(grids[k], scenes[k].geom, targets[k], scene=k)
-                   for k in range(len(scenes)))
+        loss = sum(r.splat_mse_losses(grids, geoms, targets).tolist())
         r.backward(scenes=len(scenes))
         g = r.param_gradients(scenes=len(scenes))[:, cols]
         torch.cuda.synchronize(dev)

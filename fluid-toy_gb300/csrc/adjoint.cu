@@ -97,7 +97,7 @@ struct FsAdj {
   // loss scratch
   float *field = nullptr, *target = nullptr, *gg = nullptr;
   double *loss = nullptr, *partial = nullptr;
-  size_t vox_cap = 0;
+  size_t vox_cap = 0, loss_cap = 0;
   int lanes = 0;  // lanes per particle of the reverse gathers (autotuned)
   uint32_t *scene_first = nullptr, *scene_count = nullptr;  // device, canonical ranges
 };
@@ -354,6 +354,86 @@ int tune_lanes(FsAdj *a, const SceneView &v, const TapeView &tv) {
   return best;
 }
 
+// The splat-MSE losses of `count` scenes of the recorded rollout's final
+// state: one grid build of the final positions, then per scene the density
+// splat, the loss against its target (grid_size^3 floats, host or device) and
+// the seeded cotangents of its particles (velocity cotangent 0); the losses
+// land in device memory and are read once.
+int splat_mse_losses(FsAdj *a, uint32_t count, const uint32_t *scenes,
+                     const GpuMcGridParams *grids, const GpuContainerGeometry *geoms,
+                     const float *const *targets, int on_device, double *losses,
+                     const char *fn) {
+  FsSim *s = a->sim;
+  if (!a->work) return fail(FS_E_STATE, "%s: no recorded rollout", fn);
+  size_t vox_max = 0;
+  for (uint32_t k = 0; k < count; k++) {
+    if (scenes[k] >= s->scenes())
+      return fail(FS_E_INVALID_ARGUMENT, "%s: scene %u of %u", fn, scenes[k], s->scenes());
+    if (!targets[k]) return fail(FS_E_INVALID_ARGUMENT, "%s: null target", fn);
+    const uint32_t gs = grids[k].grid_size;
+    if (gs == 0 || gs > 1024)
+      return fail(FS_E_INVALID_ARGUMENT, "%s: grid_size %u outside [1, 1024]", fn, gs);
+    const SplatArgs sa = make_splat_args(grids[k], geoms[k], s->hu[scenes[k]].grid);
+    if (sa.cell_radius < 1 || sa.cell_radius > 8)
+      return fail(FS_E_INVALID_ARGUMENT, "%s: splat radius spans %d cells", fn, sa.cell_radius);
+    vox_max = std::max(vox_max, size_t(gs) * gs * gs);
+  }
+  int rc;
+  if ((rc = set_device(s))) return rc;
+  if (a->vox_cap < vox_max || a->loss_cap < count) {
+    const size_t vox = std::max(vox_max, a->vox_cap);
+    const size_t nl = std::max<size_t>({size_t(count), size_t(s->scenes()), a->loss_cap});
+    FS_CUDA(cudaStreamSynchronize(s->stream), "loss scratch");
+    if (a->field) cudaFree(a->field);
+    a->field = nullptr;
+    a->vox_cap = a->loss_cap = 0;
+    const size_t bytes = a256(sizeof(float) * vox) * 3 + a256(sizeof(double) * nl) +
+                         a256(sizeof(double) * (vox / 256 + 1));
+    char *p = nullptr;
+    FS_CUDA(cudaMalloc(&p, bytes), "allocate loss scratch");
+    a->field = reinterpret_cast<float *>(p);
+    a->target = reinterpret_cast<float *>(p + a256(sizeof(float) * vox));
+    a->gg = reinterpret_cast<float *>(p + 2 * a256(sizeof(float) * vox));
+    a->loss = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox));
+    a->partial = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox) +
+                                            a256(sizeof(double) * nl));
+    a->vox_cap = vox;
+    a->loss_cap = nl;
+  }
+  // the final positions, grid-sorted, then per scene its splat and loss
+  if ((rc = enqueue_grid_build(s))) return rc;
+  for (uint32_t k = 0; k < count; k++) {
+    const uint32_t scene = scenes[k];
+    const DevUniforms &u = s->hu[scene];
+    const SplatArgs sa = make_splat_args(grids[k], geoms[k], u.grid);
+    const size_t vox = size_t(grids[k].grid_size) * grids[k].grid_size * grids[k].grid_size;
+    FS_CUDA(launch_density_splat(sa, s->d.s_pos, s->d.cell_begin + u.c_offset, a->field,
+                                 s->stream),
+            "loss splat");
+    const float *target = targets[k];
+    if (!on_device) {
+      FS_CUDA(cudaMemcpyAsync(a->target, targets[k], sizeof(float) * vox,
+                              cudaMemcpyHostToDevice, s->stream),
+              "upload target");
+      target = a->target;
+    }
+    FS_CUDA(launch_splat_mse(sa, a->field, target, a->gg, a->partial, a->loss + k, s->stream),
+            "loss");
+    FS_CUDA(launch_splat_adjoint(sa, s->scene_n[scene], s->d.p_pos + u.p_offset, a->gg,
+                                 a->cot[a->cur][0] + u.p_offset, s->stream),
+            "loss adjoint");
+    FS_CUDA(cudaMemsetAsync(a->cot[a->cur][1] + u.p_offset, 0,
+                            sizeof(float4) * s->scene_n[scene], s->stream),
+            "clear velocity cotangent");
+  }
+  FS_CUDA(cudaMemcpyAsync(losses, a->loss, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                          s->stream),
+          "read losses");
+  if ((rc = check_device_error(s))) return rc;
+  a->seeded = true;
+  return FS_OK;
+}
+
 #define CHECK_ADJ(a) \
   if (!(a) || !(a)->sim) return fail(FS_E_INVALID_ARGUMENT, "%s: null handle", __func__)
 
@@ -554,60 +634,22 @@ int fs_adj_splat_mse_loss(FsAdj *a, uint32_t scene, const GpuMcGridParams *grid,
                           const GpuContainerGeometry *geom, const float *target,
                           int target_on_device, double *loss_out) {
   CHECK_ADJ(a);
-  FsSim *s = a->sim;
   if (!grid || !geom || !target || !loss_out)
     return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: null argument");
-  if (scene >= s->scenes())
-    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: scene %u of %u", scene,
-                s->scenes());
-  if (!a->work) return fail(FS_E_STATE, "fs_adj_splat_mse_loss: no recorded rollout");
-  if (grid->grid_size == 0 || grid->grid_size > 1024)
-    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: grid_size %u outside [1, 1024]",
-                grid->grid_size);
-  int rc;
-  if ((rc = set_device(s))) return rc;
-  const size_t vox = size_t(grid->grid_size) * grid->grid_size * grid->grid_size;
-  if (a->vox_cap < vox) {
-    FS_CUDA(cudaStreamSynchronize(s->stream), "loss scratch");
-    if (a->field) cudaFree(a->field);
-    a->field = nullptr;
-    const size_t bytes = a256(sizeof(float) * vox) * 3 + 256 + a256(sizeof(double) * (vox / 256 + 1));
-    char *p = nullptr;
-    FS_CUDA(cudaMalloc(&p, bytes), "allocate loss scratch");
-    a->field = reinterpret_cast<float *>(p);
-    a->target = reinterpret_cast<float *>(p + a256(sizeof(float) * vox));
-    a->gg = reinterpret_cast<float *>(p + 2 * a256(sizeof(float) * vox));
-    a->loss = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox));
-    a->partial = reinterpret_cast<double *>(p + 3 * a256(sizeof(float) * vox) + 256);
-    a->vox_cap = vox;
-  }
-  const DevUniforms &u = s->hu[scene];
-  const SplatArgs sa = make_splat_args(*grid, *geom, u.grid);
-  if (sa.cell_radius < 1 || sa.cell_radius > 8)
-    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_loss: splat radius spans %d cells",
-                sa.cell_radius);
-  // the final positions, grid-sorted, then the density pass
-  if ((rc = enqueue_grid_build(s))) return rc;
-  FS_CUDA(launch_density_splat(sa, s->d.s_pos, s->d.cell_begin + u.c_offset, a->field,
-                               s->stream),
-          "loss splat");
-  FS_CUDA(cudaMemcpyAsync(a->target, target, sizeof(float) * vox,
-                          target_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                          s->stream),
-          "upload target");
-  FS_CUDA(launch_splat_mse(sa, a->field, a->target, a->gg, a->partial, a->loss, s->stream),
-          "loss");
-  FS_CUDA(launch_splat_adjoint(sa, s->scene_n[scene], s->d.p_pos + u.p_offset, a->gg,
-                               a->cot[a->cur][0] + u.p_offset, s->stream),
-          "loss adjoint");
-  FS_CUDA(cudaMemsetAsync(a->cot[a->cur][1] + u.p_offset, 0, sizeof(float4) * s->scene_n[scene],
-                          s->stream),
-          "clear velocity cotangent");
-  FS_CUDA(cudaMemcpyAsync(loss_out, a->loss, sizeof(double), cudaMemcpyDeviceToHost, s->stream),
-          "read loss");
-  if ((rc = check_device_error(s))) return rc;
-  a->seeded = true;
-  return FS_OK;
+  return splat_mse_losses(a, 1, &scene, grid, geom, &target, target_on_device, loss_out,
+                          "fs_adj_splat_mse_loss");
+}
+
+int fs_adj_splat_mse_losses(FsAdj *a, uint32_t count, const uint32_t *scenes,
+                            const GpuMcGridParams *grids, const GpuContainerGeometry *geoms,
+                            const float *const *targets, int targets_on_device,
+                            double *losses) {
+  CHECK_ADJ(a);
+  if (count == 0) return FS_OK;
+  if (!scenes || !grids || !geoms || !targets || !losses)
+    return fail(FS_E_INVALID_ARGUMENT, "fs_adj_splat_mse_losses: null argument");
+  return splat_mse_losses(a, count, scenes, grids, geoms, targets, targets_on_device, losses,
+                          "fs_adj_splat_mse_losses");
 }
 
 int fs_adj_param_gradients(FsAdj *a, double *out, uint32_t scenes) {

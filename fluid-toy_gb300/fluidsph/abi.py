@@ -15,7 +15,7 @@ import numpy as np
 
 from .build import LIB_PATH
 
-FS_ABI_VERSION = 0x00010055
+FS_ABI_VERSION = 0x00010056
 FS_OK = 0
 FS_STAGE_COUNT = 10
 FS_STAT_COUNT = 5
@@ -252,6 +252,9 @@ SIGNATURES = {
     "fs_adj_set_cotangents": (C.c_int, [_vp, _vp, _vp, C.c_int]),
     "fs_adj_splat_mse_loss": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),
                                         _vp, C.c_int, _P(C.c_double)]),
+    "fs_adj_splat_mse_losses": (C.c_int, [_vp, _u32, _P(_u32), _P(GpuMcGridParams),
+                                          _P(GpuContainerGeometry), _P(_vp), C.c_int,
+                                          _P(C.c_double)]),
     "fs_adj_backward": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp]),
     "fs_adj_param_gradients": (C.c_int, [_vp, _vp, _u32]),
     "fs_adj_final_splat": (C.c_int, [_vp, _u32, _P(GpuMcGridParams), _P(GpuContainerGeometry),

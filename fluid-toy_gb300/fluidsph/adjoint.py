@@ -89,6 +89,28 @@ class DifferentiableRollout:
                                                   C.byref(loss)))
         return loss.value
 
+    def splat_mse_losses(self, mc_params, container_geoms, targets, scenes=None) -> np.ndarray:
+        """splat_mse_loss for several scenes at once (fs_adj_splat_mse_losses:
+        one grid build, one read-back): per scene k its grid mc_params[k],
+        geometry container_geoms[k] and target targets[k] (all numpy arrays or
+        all CUDA tensors); returns the losses."""
+        n = len(targets)
+        sc = list(range(n)) if scenes is None else [int(k) for k in scenes]
+        grids = (type(mc_params[0]) * n)(*mc_params)
+        geoms = (type(container_geoms[0]) * n)(*container_geoms)
+        on_device = all(hasattr(t, "data_ptr") and getattr(t, "is_cuda", False) for t in targets)
+        if on_device:
+            keep = [t.detach().float().contiguous() for t in targets]
+            ptrs = (C.c_void_p * n)(*[t.data_ptr() for t in keep])
+        else:
+            keep = [np.ascontiguousarray(t, np.float32) for t in targets]
+            ptrs = (C.c_void_p * n)(*[t.ctypes.data for t in keep])
+        out = np.zeros(n, np.float64)
+        check(self._lib.fs_adj_splat_mse_losses(
+            self._h, n, (C.c_uint32 * n)(*sc), grids, geoms, ptrs, 1 if on_device else 0,
+            out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     def final_splat(self, mc_params, container_geom, scene: int = 0) -> np.ndarray:
         """Density splat of the recorded rollout's final positions, (gs, gs, gs)."""
         gs = int(mc_params.grid_size)

@@ -103,8 +103,7 @@ def identify(iterations: int, steps: int = 150, every: int = 15, num_scenes: int
         if targets is None:
             targets = [np.zeros_like(r.final_splat(grids[k], scs[k].geom, scene=k))
                        for k in range(len(scs))]
-        for k in range(len(scs)):
-            r.splat_mse_loss(grids[k], scs[k].geom, targets[k], scene=k)
+        r.splat_mse_losses(grids, [s.geom for s in scs], targets)
         t2 = time.perf_counter()
         nv.push(f"bwd{it}")
         r.backward(scenes=len(scs))

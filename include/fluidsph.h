@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010055u
+#define FS_ABI_VERSION 0x00010056u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -646,6 +646,15 @@ int fs_adj_set_cotangents(FsAdj *adj, const float *dl_dpos, const float *dl_dvel
 int fs_adj_splat_mse_loss(FsAdj *adj, uint32_t scene, const GpuMcGridParams *grid,
                           const GpuContainerGeometry *geom, const float *target,
                           int target_on_device, double *loss);
+/* No counterpart in the reference. fs_adj_splat_mse_loss for `count` scenes
+ * at once (scenes[k] with grids[k], geoms[k] and targets[k], all targets on
+ * the host or all on the device): the final positions are grid-sorted once
+ * and the losses are read back once, into losses[0 .. count). Losses and
+ * cotangents are those of the single-scene calls. */
+int fs_adj_splat_mse_losses(FsAdj *adj, uint32_t count, const uint32_t *scenes,
+                            const GpuMcGridParams *grids, const GpuContainerGeometry *geoms,
+                            const float *const *targets, int targets_on_device,
+                            double *losses);
 /* The density splat (fs_density_splat) of the scene's FINAL positions after
  * fs_adj_forward, e.g. to build a target field from a hidden run: host or
  * device memory, grid_size^3 floats. */
