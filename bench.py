@@ -43,14 +43,20 @@ METRIC = "particle-steps/s"
 WARMUP_PAST_TUNING = 20
 
 
-def kernels_per_step(iterations: int) -> int:
+# sorted slots from which the force pass runs without its cooperative kernel
+COOP_MAX_PARTICLES = 262144
+
+
+def kernels_per_step(iterations: int, particles: int) -> int:
     """Kernel launches of one step without rigid-body coupling: hash, scan,
     scatter, sort/gather with the big-cell sort and rank (3), warp work +
     order (2), density dedupe (mark, scan, list, list work, order: 5),
     density, dedupe copy, hit keys, key bases, key scatter, XSPH, force +
-    predict, one solve per PCISPH iteration and finalize + integrate:
-    21 + iterations. The grid clear is a memset, not counted."""
-    return 21 + iterations
+    predict (below COOP_MAX_PARTICLES sorted slots two kernels: the heavy
+    particles cooperatively, then the rest), one solve per PCISPH iteration
+    and finalize + integrate: 21 + iterations (+1). The grid clear is a
+    memset, not counted."""
+    return 21 + iterations + (1 if particles < COOP_MAX_PARTICLES else 0)
 
 
 # algorithmic bytes per particle-step and per stage (SoA, compulsory traffic)
@@ -450,7 +456,7 @@ def run_ours(args, dist: Dist) -> dict | None:
                 "d2h_bytes_per_step": d2h,
                 "pattern": "per step: upload sph/geometry/gravity/rigid-body structs, "
                            "fs_step(1), read rigid-body accumulator (sync)"},
-        "gpu_launches": K * kernels_per_step(scene.iterations),
+        "gpu_launches": K * kernels_per_step(scene.iterations, scene.n),
         "clocks": clk,
     }
     if forms is not None:
@@ -557,7 +563,7 @@ def run_batch(args, dist: Dist) -> dict | None:
                          "pattern": "one SphSimulation3DGrid per scene on one stream, "
                                     "each fs_step(k) graph-replayed, scene after scene"},
         "batched_over_looped": round(value / loop_value, 3) if loop_value else None,
-        "gpu_launches": K * kernels_per_step(scenes[0].iterations),
+        "gpu_launches": K * kernels_per_step(scenes[0].iterations, total),
         "clocks": clk,
     }
 

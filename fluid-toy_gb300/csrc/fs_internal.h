@@ -20,9 +20,11 @@ constexpr uint32_t kDensityDepths[kNumLoadDepths] = {0, 4, 8, 16, 32};
 constexpr uint32_t kXsphDepthList[kNumLoadDepths] = {1, 4, 8, 16, 32};
 
 // Work-order scratch words (DevState::order_hist), zeroed each step: the
-// bucket counts and cursors of the 33 work buckets, then the positions'
-// small-coordinate flag.
-constexpr int ORDER_HIST_WORDS = 2 * 33 + 1;
+// bucket counts and cursors of the 33 work buckets, the positions'
+// small-coordinate flag, a pad word, then the step's in-range pair count
+// (64 bits, 8-byte aligned; the density pass sums it).
+constexpr int ORDER_HIST_WORDS = 2 * 33 + 1 + 1 + 2;
+constexpr int ORDER_HIST_STEP_HITS = 2 * 33 + 2;
 
 // The neighbour passes' load-depth choice of a simulation (indices into the
 // lists above).
@@ -75,6 +77,7 @@ enum StatIndex : int {
   STAT_HIT_NONSELF = 2,   // pairs with 1e-12 < r^2 < h^2
   STAT_CAND_SOLVE = 3,    // candidate tests summed over solve iterations
   STAT_HIT_SOLVE = 4,     // predicted-position pairs with r^2 < h^2
+  STAT_COOP_FORCE = 5,    // particles whose force pass ran cooperatively
   STAT_COUNT = 8
 };
 
@@ -138,7 +141,7 @@ struct DevState {
   uint32_t *warp_order;            // [M / 32] warp ids
   uint8_t *warp_bucket;            // [M / 32] work bucket of each warp
   uint32_t *order_hist;            // [ORDER_HIST_WORDS] bucket counts, bucket cursors,
-                                   // then the step's small-coordinate flag
+                                   // the step's small-coordinate flag and pair count
   uint32_t *perm_hit;              // [M] sorted slots by decreasing hit count
   uint16_t *work_key;              // [M] hit-count bucket of each sorted slot
   uint32_t *key_hist;              // [3 * KEY_BUCKETS]: counts, bases, cursors

@@ -180,6 +180,7 @@ __device__ __forceinline__ void walk_mask(const Runs &R, const uint32_t *words, 
 struct NbrRecords {
   float4 *pos, *vel, *nrm;
   uint32_t *hits;  // per slot: pairs with r^2 < h^2 (statistics of dedupe copies)
+  unsigned long long *step_hits;  // the step's pairs with 1e-12 < r^2 < h^2
 };
 
 __global__ void __launch_bounds__(256) k_dir_table(float4 *__restrict__ tab, int dir_half) {
@@ -293,6 +294,7 @@ __device__ __forceinline__ void density_one(
     atomicAdd(stats + STAT_CAND_DENSITY, cand);
     atomicAdd(stats + STAT_HIT_DENSITY, hsum);
     atomicAdd(stats + STAT_HIT_NONSELF, nsum);
+    atomicAdd(nb.step_hits, nsum);
   }
 }
 
@@ -416,8 +418,26 @@ __device__ __forceinline__ bool small_coord(float c) {
 // Two hits per walk iteration: their terms are computed side by side (three
 // measured no faster).
 constexpr bool kForceHitPairs = true;
+// Threads per block of the force pass: four blocks of 128 per SM (its
+// registers).
+constexpr int kForceThreads = 128;
+// Heavy particles of the force pass go cooperative (a warp each) when their
+// hits exceed kCoopFactor times the step's pairs per resident lane, and at
+// least kCoopMinHits: with few particles (the 32,768-particle rollout, the
+// 49,600-particle dam break) the heaviest lanes' serial walks bound the pass.
+// Measured factors (force ms, 49.6k / 32.8k particles): none 0.44 / 0.29;
+// 2: 0.50 / 0.29; 4: 0.35 / 0.25; 8: 0.54 / 0.25; 16: 0.44 / 0.29. At 1M
+// particles no lane reaches the threshold, and the two-kernel form cost 1%
+// (its rest kernel compiles differently), so large simulations keep the
+// single kernel over every slot.
+constexpr unsigned long long kCoopFactor = 4;
+constexpr uint32_t kCoopMinHits = 128;
+// Simulations of at least this many sorted slots run the force pass without
+// the cooperative path (one kernel over every slot).
+constexpr uint32_t kCoopMaxParticles = 262144;
 // sph_force_3d_grid.wgsl:105-227, then pcisph_predict.wgsl:61-72 for the same
 // particle (sorted order).
+template <bool COOP>
 __device__ __forceinline__ void force_predict_one(
     uint32_t s, SceneView v, const float4 *__restrict__ s_pos,
                     const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
@@ -617,7 +637,66 @@ __device__ __forceinline__ void force_predict_one(
       walk_mask(R, mask_words + off, body);
     }
   };
-  if (off != MASK_NONE) {
+  // Cooperative (a heavy particle, the whole warp on it; every lane has the
+  // same s and a mask): per mask word, lane L computes the terms of candidate
+  // base + L if it is a hit and stores them at the hit's rank in the word;
+  // then lanes 0-8 each carry one accumulator component (a_p, a_v, a_c: x, y,
+  // z) through the word's hits in order, with the additions of the lane walk
+  // (a_p + p, then + sep for close pairs; a_v + v; a_c + c1, then + (-c2),
+  // which is a_c - c2 exactly). Same terms, same order: the same bits.
+  __shared__ float co_terms[kForceThreads / 32][32][20];  // referenced by COOP only
+  auto walk_coop = [&](auto dv_check) {
+    const unsigned lane = threadIdx.x & 31u;
+    float(*ct)[20] = co_terms[threadIdx.x >> 5];
+    const uint32_t *words = mask_words + off;
+    const int kind = int(lane) / 3, comp = int(lane) % 3;  // lanes 0-8
+    float acc = 0.0f;
+    StagedChunks ch(R);
+    uint32_t widx = 0u;
+    while (ch.valid) {
+      const uint32_t base = ch.base;
+      const uint32_t bits = words[widx++];
+      ch.advance(R);
+      if ((bits >> lane) & 1u) {
+        const uint32_t r = uint32_t(__popc(bits & ((1u << lane) - 1u)));
+        const uint32_t j = base + lane;
+        const Terms t = terms(j, load(j), dv_check);
+        float *e = ct[r];
+        e[0] = t.p.x; e[1] = t.p.y; e[2] = t.p.z;
+        e[3] = t.v.x; e[4] = t.v.y; e[5] = t.v.z;
+        e[6] = t.c1.x; e[7] = t.c1.y; e[8] = t.c1.z;
+        e[9] = t.sep.x; e[10] = t.sep.y; e[11] = t.sep.z;
+        e[12] = 0.0f; e[13] = 0.0f; e[14] = 0.0f;
+        e[15] = -t.c2.x; e[16] = -t.c2.y; e[17] = -t.c2.z;
+        e[18] = t.close ? 1.0f : 0.0f;
+      }
+      __syncwarp();
+      if (lane < 9u) {
+        const uint32_t m = uint32_t(__popc(bits));
+        for (uint32_t r = 0; r < m; r++) {
+          const float *e = ct[r];
+          acc = acc + e[lane];
+          const bool second = kind == 2 || (kind == 0 && e[18] != 0.0f);
+          if (second) acc = acc + e[9 + lane];
+        }
+      }
+      __syncwarp();
+    }
+    (void)comp;
+    a_p = f3(__shfl_sync(0xffffffffu, acc, 0), __shfl_sync(0xffffffffu, acc, 1),
+             __shfl_sync(0xffffffffu, acc, 2));
+    a_v = f3(__shfl_sync(0xffffffffu, acc, 3), __shfl_sync(0xffffffffu, acc, 4),
+             __shfl_sync(0xffffffffu, acc, 5));
+    a_c = f3(__shfl_sync(0xffffffffu, acc, 6), __shfl_sync(0xffffffffu, acc, 7),
+             __shfl_sync(0xffffffffu, acc, 8));
+  };
+  if constexpr (COOP) {
+    if (__ldg(small_flag) == 0u)
+      walk_coop(std::false_type{});
+    else
+      walk_coop(std::true_type{});
+    if ((threadIdx.x & 31u) != 0u) return;  // lane 0 writes the particle
+  } else if (off != MASK_NONE) {
     if (__ldg(small_flag) == 0u)
       walk(std::false_type{});
     else
@@ -837,7 +916,8 @@ __device__ __forceinline__ void flush_buckets(const uint32_t (&h)[NB], uint32_t 
 // each slot's candidate count (the density dedupe's tasks and statistics) and
 // sets the positions' small-coordinate flag.
 constexpr int ORDER_BUCKETS = 33;
-static_assert(ORDER_HIST_WORDS == 2 * ORDER_BUCKETS + 1, "order_hist layout");
+static_assert(ORDER_HIST_WORDS == 2 * ORDER_BUCKETS + 4 && ORDER_HIST_STEP_HITS % 2 == 0,
+              "order_hist layout");
 __global__ void __launch_bounds__(256)
     k_warp_work(SceneView v, const float4 *__restrict__ s_pos,
                 const uint32_t *__restrict__ begin, uint8_t *__restrict__ warp_bucket,
@@ -897,8 +977,11 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void __launch_bounds__(KEY_THREADS)
-    k_hit_keys(SceneView v, const uint32_t *__restrict__ mask_hits, uint16_t *__restrict__ key,
-               uint32_t *__restrict__ hist) {
+    k_hit_keys(SceneView v, const uint32_t *__restrict__ mask_hits,
+               const uint32_t *__restrict__ mask_off,
+               const unsigned long long *__restrict__ step_hits, uint32_t coop_lanes,
+               uint16_t *__restrict__ key, uint32_t *__restrict__ hist,
+               unsigned long long *__restrict__ stats) {
   __shared__ uint32_t h[KEY_BUCKETS];
   for (unsigned i = threadIdx.x; i < unsigned(KEY_BUCKETS); i += KEY_THREADS) h[i] = 0u;
   __syncthreads();
@@ -910,16 +993,26 @@ __global__ void __launch_bounds__(KEY_THREADS)
     const uint32_t s = first + k * KEY_THREADS;
     hits[k] = s < n ? mask_hits[s] : 0u;
   }
+  // the cooperative threshold: a slot whose hits exceed kCoopFactor times a
+  // resident lane's share of the step's pairs is on the pass's critical path
+  uint32_t coop_min = 0xffffffffu;
+  if (coop_lanes) {
+    const unsigned long long t = (__ldg(step_hits) * kCoopFactor) / coop_lanes;
+    coop_min = uint32_t(max(min(t, 0xffffffffull), (unsigned long long)kCoopMinHits));
+  }
 #pragma unroll
   for (unsigned k = 0; k < KEY_ITEMS; k++) {
     const uint32_t s = first + k * KEY_THREADS;
-    const uint32_t c = work_key(hits[k]);
+    const bool coop = s < n && hits[k] >= coop_min && mask_off[s] != MASK_NONE;
+    const uint32_t c = coop ? uint32_t(KEY_BUCKETS - 1) : min(work_key(hits[k]), uint32_t(KEY_BUCKETS - 2));
     if (s < n) key[s] = uint16_t(c);
     shared_rank(s < n, c, h);
   }
   __syncthreads();
   for (unsigned i = threadIdx.x; i < unsigned(KEY_BUCKETS); i += KEY_THREADS)
     if (h[i]) atomicAdd(&hist[i], h[i]);
+  if (threadIdx.x == 0u && h[KEY_BUCKETS - 1])
+    atomicAdd(stats + STAT_COOP_FORCE, (unsigned long long)h[KEY_BUCKETS - 1]);
 }
 
 // Exclusive bases of the key buckets, heaviest bucket first (one block).
@@ -1081,6 +1174,7 @@ __global__ void __launch_bounds__(256)
     atomicAdd(stats + STAT_CAND_DENSITY, cs);
     atomicAdd(stats + STAT_HIT_DENSITY, hs);
     atomicAdd(stats + STAT_HIT_NONSELF, nss);
+    atomicAdd(nb.step_hits, nss);
   }
 }
 
@@ -1106,31 +1200,84 @@ __global__ void __launch_bounds__(128)
   for_warp_tasks(q, [&](uint32_t s) { xsph_one<B>(s, v, s_vel, nb_pos, nb_vel, begin, vel_x); });
 }
 
-// Threads per block of the force pass: its registers fit 19 warps per SM,
-// which blocks of 128 threads round down to 16.
-constexpr int kForceThreads = 128;
 
+// The heavy particles, one warp each (cooperative): the first *coop_count
+// slots of the hit permutation. Its own kernel, launched before
+// k_force_predict, so that only it holds the shared memory of the
+// cooperative walk (the other kernel keeps the whole L1).
 __global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
-    k_force_predict(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
-                    const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
-                    const float4 *__restrict__ nb_nrm, const float2 *__restrict__ s_dens,
-                    const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
-                    const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
-                    int dir_half, const uint32_t *__restrict__ mask_words,
+    k_force_coop(TaskQueue q, const uint32_t *__restrict__ coop_count, SceneView v,
+                 const float4 *__restrict__ s_pos, const float4 *__restrict__ nb_pos,
+                 const float4 *__restrict__ nb_vel, const float4 *__restrict__ nb_nrm,
+                 const float2 *__restrict__ s_dens, const float4 *__restrict__ s_nrm,
+                 const float4 *__restrict__ vel_x, const uint32_t *__restrict__ begin,
+                 const float4 *__restrict__ dir_tab, int dir_half,
+                 const uint32_t *__restrict__ mask_words, const uint32_t *__restrict__ mask_off,
+                 const uint32_t *__restrict__ small_flag, float4 *__restrict__ anp,
+                 float4 *__restrict__ pred_xp, float *__restrict__ pred_rho,
+                 float *__restrict__ pterm0) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t nc = min(__ldg(coop_count), q.n);
+  while (true) {
+    uint32_t t = 0u;
+    if (lane == 0u) t = atomicAdd(q.counter, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= nc) break;
+    force_predict_one<true>(__ldg(q.perm + t), v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm,
+                            vel_x, begin, dir_tab, dir_half, mask_words, mask_off, small_flag, anp,
+                            pred_xp, pred_rho, pterm0);
+  }
+}
+
+// Every slot of the hit permutation in tasks of 32 (simulations of
+// kCoopMaxParticles or more, where no lane reaches the cooperative threshold).
+__global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
+    k_force_all(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
+                const float4 *__restrict__ nb_pos, const float4 *__restrict__ nb_vel,
+                const float4 *__restrict__ nb_nrm, const float2 *__restrict__ s_dens,
+                const float4 *__restrict__ s_nrm, const float4 *__restrict__ vel_x,
+                const uint32_t *__restrict__ begin, const float4 *__restrict__ dir_tab,
+                int dir_half, const uint32_t *__restrict__ mask_words,
+                const uint32_t *__restrict__ mask_off, const uint32_t *__restrict__ small_flag,
+                float4 *__restrict__ anp, float4 *__restrict__ pred_xp,
+                float *__restrict__ pred_rho, float *__restrict__ pterm0) {
+  for_warp_tasks(q, [&](uint32_t s) {
+    force_predict_one<false>(s, v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm, vel_x, begin,
+                             dir_tab, dir_half, mask_words, mask_off, small_flag, anp, pred_xp,
+                             pred_rho, pterm0);
+  });
+}
+
+// The other slots of the hit permutation (after the *coop_count cooperative
+// ones), in tasks of 32.
+__global__ void __launch_bounds__(kForceThreads, 512 / kForceThreads)
+    k_force_predict(TaskQueue q, const uint32_t *__restrict__ coop_count, SceneView v,
+                    const float4 *__restrict__ s_pos, const float4 *__restrict__ nb_pos,
+                    const float4 *__restrict__ nb_vel, const float4 *__restrict__ nb_nrm,
+                    const float2 *__restrict__ s_dens, const float4 *__restrict__ s_nrm,
+                    const float4 *__restrict__ vel_x, const uint32_t *__restrict__ begin,
+                    const float4 *__restrict__ dir_tab, int dir_half,
+                    const uint32_t *__restrict__ mask_words,
                     const uint32_t *__restrict__ mask_off,
                     const uint32_t *__restrict__ small_flag, float4 *__restrict__ anp,
                     float4 *__restrict__ pred_xp, float *__restrict__ pred_rho,
                     float *__restrict__ pterm0) {
-  for_warp_tasks(q, [&](uint32_t s) {
-    force_predict_one(s, v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm, vel_x, begin, dir_tab,
-                      dir_half, mask_words, mask_off, small_flag, anp, pred_xp, pred_rho, pterm0);
-  });
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t nc = min(__ldg(coop_count), q.n);
+  const uint32_t ntasks = (q.n - nc + 31u) / 32u;
+  while (true) {
+    uint32_t t = 0u;
+    if (lane == 0u) t = atomicAdd(q.counter, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= ntasks) break;
+    const uint32_t idx = nc + t * 32u + lane;
+    const uint32_t s = idx < q.n ? __ldg(q.perm + idx) : 0xffffffffu;
+    force_predict_one<false>(s, v, s_pos, nb_pos, nb_vel, nb_nrm, s_dens, s_nrm, vel_x, begin,
+                             dir_tab, dir_half, mask_words, mask_off, small_flag, anp, pred_xp,
+                             pred_rho, pterm0);
+  }
 }
 
-// The pressure-free batched forms (iteration 0) are bounded to four blocks
-// per SM (up to 128 registers): left to itself the compiler gave them fewer
-// registers than their record buffers need and serialised the loads. A
-// minimum of 0 blocks leaves the bound unset.
 template <bool HAS_PRESSURE, bool LAST, bool RECORD, int B>
 __global__ void __launch_bounds__(128, (!HAS_PRESSURE && B > 1) ? 4 : 0)
     k_solve(TaskQueue q, SceneView v, const float4 *__restrict__ s_pos,
@@ -1420,6 +1567,10 @@ namespace {
 // Persistent grid: as many resident blocks as the kernel's occupancy allows.
 // the positions' small-coordinate flag in order_hist (see small_coord)
 uint32_t *position_small_flag(const DevState &d) { return d.order_hist + 2 * ORDER_BUCKETS; }
+// the step's in-range pair count in order_hist (summed by the density pass)
+unsigned long long *step_hits(const DevState &d) {
+  return reinterpret_cast<unsigned long long *>(d.order_hist + ORDER_HIST_STEP_HITS);
+}
 
 template <class K>
 unsigned persistent_blocks(K kernel, int sm_count, int threads = 128) {
@@ -1428,6 +1579,12 @@ unsigned persistent_blocks(K kernel, int sm_count, int threads = 128) {
       per_sm < 1)
     per_sm = 1;
   return unsigned(per_sm * sm_count);
+}
+
+unsigned force_blocks(const DevState &d) {
+  static unsigned blocks = 0;
+  if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count, kForceThreads);
+  return blocks;
 }
 
 cudaError_t prepare_queue(const DevState &d, const uint32_t *order, bool slots, uint32_t n,
@@ -1466,8 +1623,10 @@ cudaError_t launch_order_hits(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d.key_hist, 0, sizeof(uint32_t) * 3 * KEY_BUCKETS, st);
   if (e != cudaSuccess) return e;
-  k_hit_keys<<<blocks_for(n, KEY_CHUNK), KEY_THREADS, 0, st>>>(d.view(), d.mask_hits, d.work_key,
-                                                              d.key_hist);
+  k_hit_keys<<<blocks_for(n, KEY_CHUNK), KEY_THREADS, 0, st>>>(
+      d.view(), d.mask_hits, d.mask_off, step_hits(d),
+      n < kCoopMaxParticles ? force_blocks(d) * kForceThreads : 0u, d.work_key, d.key_hist,
+      d.stats);
   return order_by_keys(d, n, d.perm_hit, st);
 }
 
@@ -1504,7 +1663,7 @@ cudaError_t launch_density(const DevState &d, uint32_t n, cudaStream_t st) {
     e = prepare_queue(d, d.warp_order, false, n, TASK_COUNTERS - 1, st, &q);
   }
   if (e != cudaSuccess) return e;
-  const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm, d.dens_hits};
+  const NbrRecords nb{d.nb_pos, d.nb_vel, d.nb_nrm, d.dens_hits, step_hits(d)};
 #define FS_DENSITY(I_)                                                                      \
   do {                                                                                      \
     static unsigned blocks = 0;                                                             \
@@ -1553,18 +1712,34 @@ cudaError_t launch_xsph(const DevState &d, uint32_t n, cudaStream_t st) {
 
 cudaError_t launch_force_predict(const DevState &d, uint32_t n, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  TaskQueue q;
+  TaskQueue q, qc;
   cudaError_t e = prepare_queue(d, d.perm_hit, true, n, 1, st, &q);
   if (e != cudaSuccess) return e;
-  static unsigned blocks = 0;
-  if (!blocks) blocks = persistent_blocks(k_force_predict, d.sm_count, kForceThreads);
+  e = prepare_queue(d, d.perm_hit, true, n, TASK_COUNTERS - 2, st, &qc);
+  if (e != cudaSuccess) return e;
   float4 *xp_out = d.rec_xp ? d.rec_xp[0] : d.pred_xp[0];
   float *rho_out = d.rec_rho ? d.rec_rho[0] : d.pred_rho[0];
-  k_force_predict<<<blocks, kForceThreads, 0, st>>>(q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm,
-                                          d.s_dens, d.s_nrm, d.vel_x,
-                                          d.cell_begin, d.dir_tab, d.dir_half, d.mask_words,
-                                          d.mask_off, position_small_flag(d), d.anp, xp_out,
-                                          rho_out, d.pterm[0]);
+  // the cooperative slots: the count of the top hit-count key
+  const uint32_t *coop_count = d.key_hist + (KEY_BUCKETS - 1);
+  if (n >= kCoopMaxParticles) {
+    static unsigned all_blocks = 0;
+    if (!all_blocks) all_blocks = persistent_blocks(k_force_all, d.sm_count, kForceThreads);
+    k_force_all<<<all_blocks, kForceThreads, 0, st>>>(
+        q, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm, d.s_dens, d.s_nrm, d.vel_x,
+        d.cell_begin, d.dir_tab, d.dir_half, d.mask_words, d.mask_off, position_small_flag(d),
+        d.anp, xp_out, rho_out, d.pterm[0]);
+    return cudaGetLastError();
+  }
+  static unsigned coop_blocks = 0;
+  if (!coop_blocks) coop_blocks = persistent_blocks(k_force_coop, d.sm_count, kForceThreads);
+  k_force_coop<<<coop_blocks, kForceThreads, 0, st>>>(
+      qc, coop_count, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm, d.s_dens, d.s_nrm,
+      d.vel_x, d.cell_begin, d.dir_tab, d.dir_half, d.mask_words, d.mask_off,
+      position_small_flag(d), d.anp, xp_out, rho_out, d.pterm[0]);
+  k_force_predict<<<force_blocks(d), kForceThreads, 0, st>>>(
+      q, coop_count, d.view(), d.s_pos, d.nb_pos, d.nb_vel, d.nb_nrm, d.s_dens, d.s_nrm,
+      d.vel_x, d.cell_begin, d.dir_tab, d.dir_half, d.mask_words, d.mask_off,
+      position_small_flag(d), d.anp, xp_out, rho_out, d.pterm[0]);
   return cudaGetLastError();
 }
 

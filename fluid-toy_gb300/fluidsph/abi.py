@@ -15,10 +15,10 @@ import numpy as np
 
 from .build import LIB_PATH
 
-FS_ABI_VERSION = 0x00010056
+FS_ABI_VERSION = 0x00010057
 FS_OK = 0
 FS_STAGE_COUNT = 10
-FS_STAT_COUNT = 5
+FS_STAT_COUNT = 6
 STAGE_NAMES = ("clear", "hash", "scan", "reorder", "density", "xsph", "force_predict",
                "pcisph_solve", "finalize_integrate", "step")
 

@@ -242,7 +242,8 @@ class SphSimulation3DGrid:
     def neighbor_stats(self, reset: bool = True) -> dict:
         out = (C.c_uint64 * FS_STAT_COUNT)()
         check(self._lib.fs_neighbor_stats(self._h, out, 1 if reset else 0))
-        keys = ("cand_density", "hits_density", "hits_nonself", "cand_solve", "hits_solve")
+        keys = ("cand_density", "hits_density", "hits_nonself", "cand_solve", "hits_solve",
+                "coop_force")
         return {k: int(out[i]) for i, k in enumerate(keys)}
 
 

@@ -33,7 +33,7 @@ extern "C" {
 /* ABI version: bumped whenever a struct layout or signature changes. It also
  * encodes the struct sizes so a caller built against another layout fails in
  * fs_create instead of corrupting memory. */
-#define FS_ABI_VERSION 0x00010056u
+#define FS_ABI_VERSION 0x00010057u
 
 /* ---- status codes -------------------------------------------------------- */
 #define FS_OK 0
@@ -530,8 +530,10 @@ int fs_stage_times(FsSim *sim, double ms[FS_STAGE_COUNT], uint32_t *steps,
  * of the density pass (also the XSPH and force passes' candidates), out[1]
  * density-pass pairs with r^2 < h^2 (self included), out[2] pairs with
  * 1e-12 < r^2 < h^2 (XSPH/force hits), out[3] candidate tests summed over all
- * PCISPH solve iterations, out[4] solve pairs with r^2 < h^2. Synchronises. */
-#define FS_STAT_COUNT 5
+ * PCISPH solve iterations, out[4] solve pairs with r^2 < h^2, out[5] particles
+ * whose force pass ran cooperatively (a warp on one heavy particle; summed
+ * over steps). Synchronises. */
+#define FS_STAT_COUNT 6
 int fs_neighbor_stats(FsSim *sim, uint64_t out[FS_STAT_COUNT], int reset);
 
 /* ---- batched form ----------------------------------------------------------- */

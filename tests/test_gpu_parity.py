@@ -233,6 +233,17 @@ def test_small_coordinates(fslib, oracle_mod, sc):
     _compare(sim, orc, n, "small coordinates step 5")
 
 
+def test_cooperative_force(fslib, oracle_mod, sc):
+    """A small, dense block (1,728 particles, hundreds of neighbours each):
+    its heavy particles exceed the cooperative threshold, so their force pass
+    runs a warp per particle (terms in parallel, sums in the walk's order);
+    every buffer stays bit-exact against the oracle."""
+    scene = sc.small_scene(12, 12, 12, box=(0.2, 0.2, 0.2), seed=6)
+    sim, orc = _run_pair(scene, 3, oracle_mod)
+    assert sim.neighbor_stats()["coop_force"] > 0
+    _compare(sim, orc, scene.n, "cooperative force")
+
+
 def test_empty_and_spawn(fslib, oracle_mod, sc):
     from fluidsph.sim import SphSimulation3DGrid
     scene = sc.make_scene("empty", np.zeros((0, 16), np.float32), (1, 1, 1))
