@@ -418,7 +418,9 @@ def run_ours(args, dist: Dist) -> dict | None:
         r.update({"hbm_gbs": round(hbm_achieved(st), 1),
                   "hbm_frac": round(hbm_achieved(st) / hbm_peak, 4)})
         stage_report[st] = r
-    kernel_name = {"pcisph_solve": "k_solve", "force_predict": "k_force_predict",
+    kernel_name = {"pcisph_solve": "k_solve",
+                   "force_predict": ("k_force_all" if scene.n >= COOP_MAX_PARTICLES
+                                     else "k_force_predict"),
                    "density": "k_density", "xsph": "k_xsph"}.get(dom, dom)
     if dom in flops:
         iters = scene.iterations if dom == "pcisph_solve" else 1
