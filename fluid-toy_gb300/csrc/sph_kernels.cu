@@ -415,8 +415,11 @@ __device__ __forceinline__ bool small_coord(float c) {
 }
 
 // ---- force + PCISPH predict ---------------------------------------------------
-// Two hits per walk iteration: their terms are computed side by side (three
-// measured no faster).
+// Three hits per walk iteration: their records are loaded together and their
+// terms computed side by side, then added in order (6.15 -> 5.76 ms on the
+// 1M-particle dam break against two, 123 registers; with the larger per-hit
+// body before the range proofs three measured no faster than two; four
+// spill).
 constexpr bool kForceHitPairs = true;
 // Threads per block of the force pass: four blocks of 128 per SM (its
 // registers).
@@ -622,16 +625,26 @@ __device__ __forceinline__ void force_predict_one(
     MaskWalk m;
     m.init(R, mask_words + off);
     if (kForceHitPairs) {
-      uint32_t j0, j1;
+      uint32_t j0, j1, j2;
       while (m.next(R, j0)) {
         if (!m.next(R, j1)) {
           body(j0);
           break;
         }
-        const Terms t0 = terms(j0, load(j0), dv_check);
-        const Terms t1 = terms(j1, load(j1), dv_check);
+        if (!m.next(R, j2)) {
+          const Terms t0 = terms(j0, load(j0), dv_check);
+          const Terms t1 = terms(j1, load(j1), dv_check);
+          add(t0);
+          add(t1);
+          break;
+        }
+        const Rec q0 = load(j0), q1 = load(j1), q2 = load(j2);
+        const Terms t0 = terms(j0, q0, dv_check);
+        const Terms t1 = terms(j1, q1, dv_check);
+        const Terms t2 = terms(j2, q2, dv_check);
         add(t0);
         add(t1);
+        add(t2);
       }
     } else {
       walk_mask(R, mask_words + off, body);
