@@ -420,7 +420,7 @@ __device__ __forceinline__ bool small_coord(float c) {
 // 1M-particle dam break against two, 123 registers; with the larger per-hit
 // body before the range proofs three measured no faster than two; four
 // spill).
-constexpr bool kForceHitPairs = true;
+constexpr bool kForceHitTriples = true;
 // Threads per block of the force pass: four blocks of 128 per SM (its
 // registers).
 constexpr int kForceThreads = 128;
@@ -624,7 +624,7 @@ __device__ __forceinline__ void force_predict_one(
     auto body = [&](uint32_t j) { add(terms(j, load(j), dv_check)); };
     MaskWalk m;
     m.init(R, mask_words + off);
-    if (kForceHitPairs) {
+    if (kForceHitTriples) {
       uint32_t j0, j1, j2;
       while (m.next(R, j0)) {
         if (!m.next(R, j1)) {
