@@ -53,6 +53,10 @@ def test_create_rejects_bad_arguments(fslib):
     assert rc == -1
     assert fslib.fs_step(None, 1) == -1
     assert fslib.fs_destroy(None) == 0
+    # the batched loss call checks its handle before any device work
+    losses = (C.c_double * 2)()
+    assert fslib.fs_adj_splat_mse_losses(None, 2, None, None, None, None, 0, losses) == -1
+    assert b"null handle" in fslib.fs_last_error()
 
 
 def test_create_without_gpu_reports_no_device(fslib):
