@@ -61,16 +61,21 @@ struct FsSim {
   // bucket (floor(log2 hashed particles), one or many scenes, PCISPH
   // iterations) is in the process-wide table takes its entry; otherwise,
   // once it has run kTuneAfterSteps steps, its next kTuneSteps steps run each
-  // candidate depth twice (palindromic order) with events around the density,
-  // XSPH and solve stages, whatever the fs_step call sizes, the next call
-  // waits for them once, and each pass keeps its fastest depth, which also
-  // enters the table.
+  // candidate depth of the density and solve passes twice (palindromic
+  // order) and every XSPH depth in every one of those steps (rotating order;
+  // XSPH rewrites the same velocities from the same inputs), with events
+  // around the passes, whatever the fs_step call sizes; the next call waits
+  // for them once, and each pass keeps its fastest depth (density and solve
+  // by the mean of their two samples, XSPH by the median of its ten), which
+  // also enters the table.
   fs::KernelForms forms;
   int tune_state = 0;   // 0 measuring (phase), 1 measured (events pending), 2 decided
   int tune_source = 0;  // how the forms were decided: 1 measured, 2 table, 3 set by the caller
   int tune_phase = 0;   // measured steps so far
-  cudaEvent_t tune_ev[2 * fs::kNumLoadDepths][FS_STAGE_COUNT] = {};
-  float tune_ms[3][fs::kNumLoadDepths] = {};  // measured ms per pass (density, XSPH, solve) and depth
+  // per measured step: the stage marks, then the boundaries of the XSPH
+  // launches (one per depth)
+  cudaEvent_t tune_ev[2 * fs::kNumLoadDepths][FS_STAGE_COUNT + fs::kNumLoadDepths + 1] = {};
+  float tune_ms[3][fs::kNumLoadDepths] = {};  // measured ms per step per pass (density, XSPH, solve) and depth
   uint64_t steps_done = 0;
   // stage timing
   bool timing = false;
@@ -97,8 +102,12 @@ int check_device_error(FsSim *s);
 // One step on the simulation's stream. timed: stage events into s->ev;
 // marks (if not null): stage events into marks[0..FS_STAGE_COUNT) instead;
 // forms (if not null): these load depths instead of the simulation's.
+// xsph_all >= 0 (a measured step, with marks): every XSPH depth is launched,
+// starting at depth index xsph_all, marks[FS_STAGE_COUNT + i] before launch i
+// and marks[FS_STAGE_COUNT + kNumLoadDepths] after the last.
 int enqueue_step(FsSim *s, bool timed, const DevState *dv = nullptr,
-                 const KernelForms *forms = nullptr, cudaEvent_t *marks = nullptr);
+                 const KernelForms *forms = nullptr, cudaEvent_t *marks = nullptr,
+                 int xsph_all = -1);
 // Enqueue only the grid build (clear, hash, scan, reorder) of the current state.
 int enqueue_grid_build(FsSim *s);
 

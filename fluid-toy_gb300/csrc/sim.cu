@@ -277,7 +277,7 @@ int write_particles(FsSim *s, const SphParticle3D *parts, uint32_t offset, uint3
 // scenes at once, on the simulation's buffers or on `dv` (the same buffers
 // with some replaced, e.g. by a recording for the reverse pass).
 int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv, const KernelForms *forms,
-                     cudaEvent_t *marks) {
+                     cudaEvent_t *marks, int xsph_all) {
   const uint32_t n = s->hb.n_sorted;
   const uint32_t n_canon = s->hb.n_canon;
   const uint32_t G = s->cells_total;
@@ -310,7 +310,17 @@ int fs::enqueue_step(FsSim *s, bool timed, const DevState *dv, const KernelForms
   FS_CUDA(launch_density(d, n, st), "density");
   FS_CUDA(launch_order_hits(d, n, st), "neighbour-pass work order (hits)");
   if ((rc = mark(5))) return rc;
-  FS_CUDA(launch_xsph(d, n, st), "xsph");
+  if (xsph_all >= 0 && marks) {
+    for (int i = 0; i < kNumLoadDepths; i++) {
+      FS_CUDA(cudaEventRecord(marks[FS_STAGE_COUNT + i], st), "record XSPH event");
+      d.load_xsph = uint8_t((xsph_all + i) % kNumLoadDepths);
+      FS_CUDA(launch_xsph(d, n, st), "xsph");
+    }
+    FS_CUDA(cudaEventRecord(marks[FS_STAGE_COUNT + kNumLoadDepths], st), "record XSPH event");
+    d.load_xsph = f.xsph;
+  } else {
+    FS_CUDA(launch_xsph(d, n, st), "xsph");
+  }
   if ((rc = mark(6))) return rc;
   FS_CUDA(launch_force_predict(d, n, st), "force + predict");
   if ((rc = mark(7))) return rc;
@@ -385,15 +395,30 @@ int tune_decide(FsSim *s) {
   if (s->tune_state != 1 || capturing(s)) return FS_OK;
   FS_CUDA(cudaEventSynchronize(s->tune_ev[kTuneSteps - 1][8]), "kernel-form measurement");
   float ms[3][kNumLoadDepths] = {};
+  float xs[kNumLoadDepths][kTuneSteps];
   for (int p = 0; p < kTuneSteps; p++) {
     const int c = tune_candidate(p);
-    float t[3];
-    // density (with the work-order kernels around it: the same for every depth),
-    // XSPH, the PCISPH solve iterations
+    float t[2];
+    // density (with the work-order kernels around it: the same for every
+    // depth) and the PCISPH solve iterations: one sample per step, two per
+    // depth, averaged
     FS_CUDA(cudaEventElapsedTime(&t[0], s->tune_ev[p][4], s->tune_ev[p][5]), "kernel-form measurement");
-    FS_CUDA(cudaEventElapsedTime(&t[1], s->tune_ev[p][5], s->tune_ev[p][6]), "kernel-form measurement");
-    FS_CUDA(cudaEventElapsedTime(&t[2], s->tune_ev[p][7], s->tune_ev[p][8]), "kernel-form measurement");
-    for (int k = 0; k < 3; k++) ms[k][c] += t[k];
+    FS_CUDA(cudaEventElapsedTime(&t[1], s->tune_ev[p][7], s->tune_ev[p][8]), "kernel-form measurement");
+    ms[0][c] += 0.5f * t[0];
+    ms[2][c] += 0.5f * t[1];
+    // XSPH: every depth in every step
+    for (int i = 0; i < kNumLoadDepths; i++) {
+      const int cx = (p + i) % kNumLoadDepths;
+      FS_CUDA(cudaEventElapsedTime(&xs[cx][p], s->tune_ev[p][FS_STAGE_COUNT + i],
+                                   s->tune_ev[p][FS_STAGE_COUNT + i + 1]),
+              "kernel-form measurement");
+    }
+  }
+  // XSPH: the median of each depth's samples (a disturbed step does not
+  // decide)
+  for (int c = 0; c < kNumLoadDepths; c++) {
+    std::sort(xs[c], xs[c] + kTuneSteps);
+    ms[1][c] = 0.5f * (xs[c][kTuneSteps / 2 - 1] + xs[c][kTuneSteps / 2]);
   }
   uint8_t best[3] = {0, 0, 0};
   for (int k = 0; k < 3; k++)
@@ -421,7 +446,7 @@ int tune_steps(FsSim *s, uint32_t &nsteps) {
     KernelForms f;  // depth 32 (the last candidate) is XSPH's alone
     f.xsph = uint8_t(c);
     f.density = f.solve = uint8_t(c < kPlainCandidates ? c : kPlainCandidates - 1);
-    const int rc = enqueue_step(s, false, nullptr, &f, s->tune_ev[p]);
+    const int rc = enqueue_step(s, false, nullptr, &f, s->tune_ev[p], p % kNumLoadDepths);
     if (rc) return rc;
     s->steps_done++;
     nsteps--;
