@@ -96,6 +96,10 @@ class DifferentiableRollout:
         all CUDA tensors); returns the losses."""
         n = len(targets)
         sc = list(range(n)) if scenes is None else [int(k) for k in scenes]
+        if n == 0:
+            return np.zeros(0, np.float64)
+        if not (len(mc_params) == len(container_geoms) == len(sc) == n):
+            raise ValueError("splat_mse_losses: one grid, geometry, target and scene per loss")
         grids = (type(mc_params[0]) * n)(*mc_params)
         geoms = (type(container_geoms[0]) * n)(*container_geoms)
         on_device = all(hasattr(t, "data_ptr") and getattr(t, "is_cuda", False) for t in targets)

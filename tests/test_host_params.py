@@ -146,3 +146,14 @@ def test_scenes_from_oracle_builders_are_identical(fslib):
             assert _struct_bytes(x) == _struct_bytes(y)
         if a.rigid is not None:
             assert _struct_bytes(a.rigid) == _struct_bytes(b.rigid)
+
+
+def test_batched_losses_check_their_lists():
+    """DifferentiableRollout.splat_mse_losses refuses lists of different
+    lengths before any library call (and returns no losses for none)."""
+    import pytest
+    from fluidsph.adjoint import DifferentiableRollout
+    fake = object.__new__(DifferentiableRollout)
+    assert DifferentiableRollout.splat_mse_losses(fake, [], [], []).shape == (0,)
+    with pytest.raises(ValueError):
+        DifferentiableRollout.splat_mse_losses(fake, [1, 2], [1], [np.zeros(1), np.zeros(1)])
